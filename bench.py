@@ -1,0 +1,412 @@
+#!/usr/bin/env python
+"""Benchmark: exact triangle counting on one GB300 (GTEPS), plain vs learned
+selector, plus batched graphs/s.
+
+Default workload: R-MAT scale 24, edge factor 16, (a,b,c,d) = (0.57, 0.19,
+0.19, 0.05), seed 0, generated on the device by the engine's seeded
+generator and symmetrised/deduplicated by its device CSR builder (synthetic
+data; the colidx array is several GB, larger than L2, so no flush is needed
+between steps).  One step = one tc_count call on the device-resident CSR:
+validation, orientation (rank sort, relabel, compaction) and counting.
+GTEPS = undirected edges / step time.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference]
+
+--impl reference times the CPU oracle (a C/OpenMP restatement of the
+reference CPU path: Graph::orientation + merge intersection) on a bounded
+sample of the same workload on the host cores.  Under torchrun every rank
+runs an independent replica (the path does not shard).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOADS = {
+    "rmat24": dict(kind="rmat", scale=24, edge_factor=16, a=0.57, b=0.19, c=0.19, seed=0),
+    "rmat22": dict(kind="rmat", scale=22, edge_factor=16, a=0.57, b=0.19, c=0.19, seed=0),
+    "rmat20": dict(kind="rmat", scale=20, edge_factor=16, a=0.57, b=0.19, c=0.19, seed=0),
+    "er16k": dict(kind="er", n=16384, avg_degree=16, seed=0),
+    "chunglu26": dict(kind="chung_lu", n=1 << 26, avg_degree=32, gamma=2.1, seed=0),
+}
+WEIGHTS = ROOT / "hetegeneous_parallel_programming_gb300" / "data" / "selector_mlp.npz"
+TRAFFIC = ROOT / "profiles" / "ncu_traffic.json"
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_graph(eng, wl, torch, dev):
+    import hetegeneous_parallel_programming_gb300 as tc
+    spec = tc.GenSpec(**wl)
+    n, M = spec.num_vertices, spec.num_samples
+    src = torch.empty(M, dtype=torch.int32, device=dev)
+    dst = torch.empty(M, dtype=torch.int32, device=dev)
+    torch.cuda.synchronize()
+    eng.gen_edges_device(spec, src.data_ptr(), dst.data_ptr(), M)
+    rowptr = torch.empty(n + 1, dtype=torch.int64, device=dev)
+    colidx = torch.empty(2 * M, dtype=torch.int32, device=dev)
+    nnz = eng.csr_from_edges_device(n, M, src.data_ptr(), dst.data_ptr(), rowptr.data_ptr(), colidx.data_ptr(),
+                                    2 * M)
+    del src, dst
+    colidx = colidx[:nnz].clone()
+    torch.cuda.synchronize()
+    return n, nnz, rowptr, colidx
+
+
+def timed(fn, steps, warmup, eng, torch, dist):
+    """W untimed calls, then K calls bracketed by barrier + sync and CUDA
+    events on the engine's stream; returns max-over-ranks ms per step."""
+    for _ in range(warmup):
+        fn()
+    s = torch.cuda.ExternalStream(eng.stream)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0.record(s)
+    out = None
+    for _ in range(steps):
+        out = fn()
+    e1.record(s)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ms = e0.elapsed_time(e1) / steps
+    if dist:
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, out
+
+
+def cpu_sample(rowptr_h, colidx_h, target_s: float):
+    """Oracle (C/OpenMP) on every k-th row, sized for ~target_s seconds."""
+    from oracle import oracle
+    t0 = time.time()
+    orow, ocol = oracle.orient(rowptr_h, colidx_h)
+    t_full_orient = time.time() - t0
+    n = len(rowptr_h) - 1
+    step = max(1, n // 256)
+    while True:
+        t0 = time.time()
+        oracle.orient_sample_cost(rowptr_h, colidx_h, step)
+        oracle.count_sample(orow, ocol, step)
+        dt = time.time() - t0
+        if dt > 0.5 or step == 1:
+            break
+        step = max(1, step // 4)
+    step = max(1, int(step * dt / target_s)) if dt < target_s else step
+    kept_rows = np.diff(orow)[::step]
+    return orow, ocol, step, int(kept_rows.sum()), t_full_orient
+
+
+def run_cpu_sample(rowptr_h, colidx_h, orow, ocol, step):
+    from oracle import oracle
+    t0 = time.time()
+    oracle.orient_sample_cost(rowptr_h, colidx_h, step)
+    oracle.count_sample(orow, ocol, step)
+    return time.time() - t0
+
+
+def engine_arm(args, rank, world, local_rank, dist):
+    import torch
+    import hetegeneous_parallel_programming_gb300 as tc
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    eng = tc.Engine(local_rank)
+    wl = WORKLOADS[args.workload]
+    t0 = time.time()
+    n, nnz, rowptr, colidx = make_graph(eng, wl, torch, dev)
+    m = nnz // 2
+    log(f"[rank {rank}] graph {args.workload}: n={n} nnz={nnz} m={m} ({time.time() - t0:.1f}s)")
+    have_weights = WEIGHTS.exists()
+    if have_weights:
+        w = np.load(WEIGHTS)["params"].astype(np.float32)
+        eng.set_selector_weights(w)
+
+    def step(sel):
+        return lambda: eng.count_device(n, nnz, rowptr.data_ptr(), colidx.data_ptr(), selector=sel)
+
+    results = {}
+    clk = Clocks(local_rank)
+    with clk:
+        for sel in (["fixed", "learned"] if have_weights else ["fixed"]):
+            ms, out = timed(step(sel), args.steps, args.warmup, eng, torch, dist)
+            results[sel] = (ms, out)
+            log(f"[rank {rank}] {sel}: {ms:.2f} ms/step, total={out[0]}, {m / ms / 1e6:.3f} GTEPS")
+    best = "learned" if have_weights else "fixed"
+    ms_best, (total, st) = results[best]
+    if results.get("learned") and results["learned"][1][0] != results["fixed"][1][0]:
+        raise SystemExit("learned and plain selectors disagree on the count")
+    # e2e through the public API with pinned host buffers (H2D + D2H inside)
+    rowptr_h = rowptr.cpu().pin_memory()
+    colidx_h = colidx.cpu().pin_memory()
+    ms_e2e, (tot_e2e, st_e2e) = timed(lambda: eng.count_host_ptr(n, nnz, rowptr_h.data_ptr(), colidx_h.data_ptr(),
+                                                                 selector=best),
+                                      max(1, min(args.steps, 5)), 1, eng, torch, dist)
+    assert tot_e2e == total
+    line = None
+    if rank == 0:
+        hbm, kind = peaks()
+        arm = max(st["ms_arm"], key=lambda k: st["ms_arm"][k])
+        achieved = st["alg_bytes_arm"][arm] / (st["ms_arm"][arm] * 1e-3) / 1e9 if st["ms_arm"][arm] > 0 else 0.0
+        traffic = None
+        if TRAFFIC.exists():
+            tr = json.loads(TRAFFIC.read_text()).get(args.workload, {})
+            traffic = tr.get(arm)
+        line = {
+            "metric": "GTEPS on 1 GB300, learned vs plain selector (exact count); batched graphs/s",
+            "value": round(world * m / (ms_best * 1e-3) / 1e9, 4),
+            "unit": "GTEPS",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": round(ms_best, 3),
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "int32/uint64",
+            "data": "synthetic (seeded R-MAT generated on the device; inputs larger than L2, no flush)",
+            "config": {"workload": f"rmat s{wl.get('scale')} ef{wl.get('edge_factor')} (a,b,c)=({wl.get('a')},"
+                                   f"{wl.get('b')},{wl.get('c')}) seed {wl.get('seed')}"
+                       if wl["kind"] == "rmat" else args.workload,
+                       "n": n, "undirected_edges": m, "triangles": total, "selector": best,
+                       "tile_edges": 4096, "parallelism": f"replicas x{world}", "l2": "inputs > L2"},
+            "plain_gteps": round(m / (results["fixed"][0] * 1e-3) / 1e9, 4),
+            "learned_gteps": round(m / (results["learned"][0] * 1e-3) / 1e9, 4) if have_weights else None,
+            "learned_over_plain": round(results["fixed"][0] / results["learned"][0], 4) if have_weights else None,
+            "phases_ms": {k: round(st[k], 3) for k in ("ms_validate", "ms_orient", "ms_plan", "ms_count",
+                                                        "ms_total")},
+            "tiles_per_arm": st["tiles_per_arm"],
+            "ms_arm": {k: round(v, 3) for k, v in st["ms_arm"].items()},
+            "e2e": {"value": round(world * m / (ms_e2e * 1e-3) / 1e9, 4), "unit": "GTEPS",
+                    "h2d_bytes_per_step": int(st_e2e["h2d_bytes"]), "d2h_bytes_per_step": int(st_e2e["d2h_bytes"]),
+                    "ms_per_step": round(ms_e2e, 3)},
+            "roofline": {"bound": "hbm", "kernel": f"arm:{arm}", "achieved": round(achieved, 1), "peak": hbm,
+                         "unit": "GB/s", "frac": round(achieved / hbm, 4), "traffic": traffic,
+                         "peak_kind": f"{kind} copy bandwidth",
+                         "count_phase": {"alg_bytes": int(st["alg_bytes"]),
+                                         "achieved": round(st["alg_bytes"] / (st["ms_count"] * 1e-3) / 1e9, 1)
+                                         if st["ms_count"] > 0 else None}},
+            "gpu_launches": int(st["kernel_launches"]) * args.steps,
+            "clocks": clk.summary(),
+        }
+    if not args.no_batched:
+        bat = batched(args, eng, torch, dev, dist, rank)
+        if line is not None:
+            line.update(bat)
+    if line is not None and not args.no_cpu_baseline:
+        rh, ch = rowptr_h.numpy(), colidx_h.numpy()
+        from oracle import oracle
+        orow, ocol, step_k, m_sample, _ = cpu_sample(rh, ch, args.cpu_seconds)
+        dt = run_cpu_sample(rh, ch, orow, ocol, step_k)
+        line["cpu_baseline"] = {"value": round(m_sample / dt / 1e9, 5), "unit": "GTEPS",
+                                "cores": oracle.max_threads(), "kind": "port",
+                                "sample": f"every {step_k}th vertex's rows: {m_sample} oriented edges, orientation "
+                                          f"+ merge count, {dt:.1f}s"}
+        # reference-style GPU kernel (restated warp_vertex) on the original-id DAG
+        try:
+            from baseline import build_ref
+            o_r = torch.from_numpy(orow).to(dev)
+            o_c = torch.from_numpy(ocol).to(dev)
+            torch.cuda.synchronize()
+            t_ref, ms_ref = build_ref.count(o_r.data_ptr(), o_c.data_ptr(), n)
+            line["reference_kernel"] = {"total": t_ref, "ms": round(ms_ref, 3),
+                                        "gteps_count_only": round(m / (ms_ref * 1e-3) / 1e9, 4),
+                                        "matches": t_ref == total}
+        except Exception as exc:  # the baseline kernel is informational
+            line["reference_kernel"] = {"error": str(exc)[:200]}
+    if line is not None:
+        print(json.dumps(line), flush=True)
+    eng.close()
+
+
+def batched(args, eng, torch, dev, dist, rank):
+    import hetegeneous_parallel_programming_gb300 as tc
+    t0 = time.time()
+    vtx_off, rowptr, colidx = tc.gen_batch_host(args.batch_graphs, seed=1)
+    G = len(vtx_off) - 1
+    log(f"[rank {rank}] batch: {G} graphs, n={vtx_off[-1]} nnz={len(colidx)} ({time.time() - t0:.1f}s)")
+    d_off = torch.from_numpy(vtx_off).to(dev)
+    d_row = torch.from_numpy(rowptr).to(dev)
+    d_col = torch.from_numpy(colidx).to(dev)
+    torch.cuda.synchronize()
+    call = lambda: eng.batch_count_device(G, d_off.data_ptr(), d_row.data_ptr(), d_col.data_ptr())
+    ms, (totals, st) = timed(call, args.steps, args.warmup, eng, torch, dist)
+    # one launch sequence per graph (same engine, no batching)
+    loc_rows = []
+    for g in range(G):
+        a, b = int(vtx_off[g]), int(vtx_off[g + 1])
+        loc_rows.append(torch.from_numpy(rowptr[a:b + 1] - rowptr[a]).to(dev))
+    torch.cuda.synchronize()
+    base = d_col.data_ptr()
+
+    def per_graph():
+        out = []
+        for g in range(G):
+            a = int(vtx_off[g])
+            nn = int(vtx_off[g + 1]) - a
+            e0 = int(rowptr[a])
+            ne = int(rowptr[a + nn]) - e0
+            out.append(eng.count_device(nn, ne, loc_rows[g].data_ptr(), base + 4 * e0)[0])
+        return out
+    ms_pg, totals_pg = timed(per_graph, 1, 0, eng, torch, dist)
+    if list(map(int, totals)) != totals_pg:
+        raise SystemExit("batched and per-graph counts disagree")
+    return {"batched": {"graphs": G, "graphs_per_s": round(G / (ms * 1e-3), 1), "ms_per_batch": round(ms, 3),
+                        "per_graph_launch_graphs_per_s": round(G / (ms_pg * 1e-3), 1),
+                        "speedup_vs_per_graph": round(ms_pg / ms, 2), "undirected_edges": len(colidx) // 2,
+                        "kernel_launches_per_batch": int(st["kernel_launches"])}}
+
+
+def reference_arm(args, rank, world, local_rank):
+    if rank != 0:
+        return
+    import hetegeneous_parallel_programming_gb300 as tc
+    from oracle import oracle
+    wl = WORKLOADS[args.workload]
+    spec = tc.GenSpec(**wl)
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            raise RuntimeError
+        torch.cuda.set_device(local_rank)
+        eng = tc.Engine(local_rank)
+        n, nnz, rowptr, colidx = make_graph(eng, wl, torch, torch.device("cuda", local_rank))
+        rh, ch = rowptr.cpu().numpy(), colidx.cpu().numpy()
+        eng.close()
+    except Exception:
+        n, s, d = tc.gen_edges_host(spec)
+        rh, ch = oracle.csr_from_edges(n, s, d)
+        nnz = len(ch)
+    orow, ocol, step_k, m_sample, _ = cpu_sample(rh, ch, args.ref_step_seconds)
+    for _ in range(args.warmup):
+        run_cpu_sample(rh, ch, orow, ocol, step_k)
+    times = [run_cpu_sample(rh, ch, orow, ocol, step_k) for _ in range(args.steps)]
+    sec = sum(times) / len(times)
+    v = m_sample / sec / 1e9
+    cores = oracle.max_threads()
+    line = {"impl": "reference",
+            "metric": "GTEPS on 1 GB300, learned vs plain selector (exact count); batched graphs/s",
+            "value": round(v, 5), "unit": "GTEPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(sec * 1e3, 2), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int32/uint64", "data": "synthetic (same seeded R-MAT as the engine arm)",
+            "config": {"workload": args.workload, "n": n, "undirected_edges": nnz // 2},
+            "cpu_baseline": {"value": round(v, 5), "unit": "GTEPS", "cores": cores, "kind": "port",
+                             "sample": f"every {step_k}th vertex's rows ({m_sample} oriented edges): orientation "
+                                       f"(graph.cc:252-298) + merge count (graph.cc:376-391), C/OpenMP"},
+            "e2e": {"value": round(v, 5), "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="rmat24")
+    ap.add_argument("--batch-graphs", type=int, default=4096)
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--ref-step-seconds", type=float, default=4.0)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "engine" else args.warmup
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":  # rank 0 alone times the CPU path; other ranks exit without work
+        reference_arm(args, rank, world, local_rank)
+        return
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as tdist
+        torch.cuda.set_device(local_rank)
+        tdist.init_process_group("nccl")
+        dist = tdist
+    engine_arm(args, rank, world, local_rank, dist)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

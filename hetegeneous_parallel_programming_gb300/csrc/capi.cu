@@ -1,0 +1,397 @@
+// extern "C" entry points of libtc: ctx lifetime, orientation, counting,
+// device generators and the device symmetric-CSR builder.
+#include <algorithm>
+#include <vector>
+
+#include "engine.cuh"
+#include "tc_gen_common.h"
+
+using namespace tc;
+
+namespace tc {
+
+const char *flag_text(unsigned f) {
+  if (f & VF_ROWPTR_ENDS) return "rowptr[0] must be 0 and rowptr[n] must equal nnz";
+  if (f & VF_ROWPTR_ORDER) return "rowptr is not monotone";
+  if (f & VF_ID_RANGE) return "a column id is outside [0, n)";
+  if (f & VF_SELF_LOOP) return "a row holds a self loop";
+  if (f & VF_UNSORTED) return "a row is not strictly ascending (unsorted or duplicate neighbours)";
+  if (f & VF_TIMEOUT) return "a bounded device wait gave up";
+  return "invalid graph";
+}
+
+static tc_status check_csr_args(tc_ctx *ctx, const tc_csr *g) {
+  if (!g) return set_error(ctx, TC_ERR_INVALID_ARG, "null graph");
+  if (g->n < 1 || g->n > 2147483647LL)
+    return set_error(ctx, TC_ERR_UNSUPPORTED, "n=%lld outside [1, 2^31-1]", (long long)g->n);
+  if (g->nnz < 0 || !g->rowptr || (g->nnz > 0 && !g->colidx))
+    return set_error(ctx, TC_ERR_INVALID_ARG, "bad nnz or null CSR arrays");
+  if (g->nnz >= (int64_t(1) << 32))
+    return set_error(ctx, TC_ERR_UNSUPPORTED, "nnz=%lld: this engine indexes oriented edges with 32 bits",
+                     (long long)g->nnz);
+  return TC_OK;
+}
+
+// Device copies of a caller CSR (no copy when already on the device).
+tc_status stage_csr(tc_ctx *ctx, const tc_csr *g, Bump &bump, DevCSR &d, uint64_t *h2d) {
+  d.n = g->n;
+  d.nnz = g->nnz;
+  if (g->on_device) {
+    d.rowptr = g->rowptr;
+    d.col = g->colidx;
+    return TC_OK;
+  }
+  int64_t *rp = bump.take<int64_t>(g->n + 1);
+  int32_t *cl = bump.take<int32_t>(g->nnz);
+  if (bump.overflow) return set_error(ctx, TC_ERR_OOM, "arena overflow staging the graph");
+  TC_CHECK_CUDA(ctx, cudaMemcpyAsync(rp, g->rowptr, sizeof(int64_t) * (size_t)(g->n + 1), cudaMemcpyHostToDevice,
+                                     ctx->stream));
+  if (g->nnz > 0)
+    TC_CHECK_CUDA(ctx, cudaMemcpyAsync(cl, g->colidx, sizeof(int32_t) * (size_t)g->nnz, cudaMemcpyHostToDevice,
+                                       ctx->stream));
+  *h2d += sizeof(int64_t) * (size_t)(g->n + 1) + sizeof(int32_t) * (size_t)g->nnz;
+  d.rowptr = rp;
+  d.col = cl;
+  return TC_OK;
+}
+
+void orient_sizes(const tc_ctx *ctx, int64_t n, int64_t nnz, bool perm, bool dagcol, Sizer &sz) {
+  int G;
+  int64_t chunk;
+  orient_geometry(ctx, nnz, &G, &chunk);
+  const int64_t mmax = nnz;
+  sz.take<uint64_t>(n); sz.take<uint64_t>(n);
+  sz.take<int32_t>(n);
+  sz.take<int64_t>(n + 1);
+  sz.take<int64_t>(G + 1);
+  sz.take<int64_t>(1);
+  size_t scr = std::max(radix_sort_scratch_bytes(ctx, std::max<int64_t>(n, mmax)), scan_scratch_bytes(ctx, n + 1));
+  scr = std::max(scr, scan_scratch_bytes(ctx, G));
+  sz.take<char>((int64_t)scr);
+  sz.take<uint64_t>(mmax); sz.take<uint64_t>(mmax);
+  if (perm) { sz.take<uint32_t>(mmax); sz.take<uint32_t>(mmax); }
+  sz.take<int64_t>(n + 1); sz.take<int64_t>(n + 1);
+  sz.take<int32_t>(mmax); sz.take<int32_t>(mmax);
+  if (dagcol) sz.take<int32_t>(mmax);
+}
+
+void orient_carve(const tc_ctx *ctx, int64_t n, int64_t nnz, bool perm, bool dagcol, Bump &bump,
+                         OrientBufs &b) {
+  orient_geometry(ctx, nnz, &b.G, &b.chunk);
+  const int64_t mmax = nnz;
+  b.vkeys0 = bump.take<uint64_t>(n);
+  b.vkeys1 = bump.take<uint64_t>(n);
+  b.rank = bump.take<int32_t>(n);
+  b.kept = bump.take<int64_t>(n + 1);
+  b.bcount = bump.take<int64_t>(b.G + 1);
+  b.d_m = bump.take<int64_t>(1);
+  size_t scr = std::max(radix_sort_scratch_bytes(ctx, std::max<int64_t>(n, mmax)), scan_scratch_bytes(ctx, n + 1));
+  scr = std::max(scr, scan_scratch_bytes(ctx, b.G));
+  b.sort_scratch = bump.take<char>((int64_t)scr);
+  b.ekeys0 = bump.take<uint64_t>(mmax);
+  b.ekeys1 = bump.take<uint64_t>(mmax);
+  b.evals0 = perm ? bump.take<uint32_t>(mmax) : nullptr;
+  b.evals1 = perm ? bump.take<uint32_t>(mmax) : nullptr;
+  b.nrowptr = bump.take<int64_t>(n + 1);
+  b.dnew = bump.take<int64_t>(n + 1);
+  b.ncol = bump.take<int32_t>(mmax);
+  b.nsrc = bump.take<int32_t>(mmax);
+  b.dag_col = dagcol ? bump.take<int32_t>(mmax) : nullptr;
+}
+
+float elapsed(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0;
+  if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return 0;
+  }
+  return ms;
+}
+
+// Validation + phase A + read back m and the flags (which the caller zeroed
+// before any kernel that may set them).
+tc_status orient_front(tc_ctx *ctx, const DevCSR &d, const tc_opts &o, OrientBufs &ob, int64_t *m,
+                              float *ms_validate, float *ms_a) {
+  TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[1], ctx->stream));
+  if (o.validate) TC_TRY(launch_validate(ctx, d, true));
+  TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
+  TC_TRY(orient_phase_a(ctx, d, ob));
+  TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[3], ctx->stream));
+  TC_CHECK_CUDA(ctx, cudaMemcpyAsync(&ctx->h_pinned[0], ob.d_m, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+  TC_CHECK_CUDA(ctx, cudaMemcpyAsync(&ctx->h_pinned[1], ctx->d_flags, sizeof(unsigned) * 2, cudaMemcpyDeviceToHost,
+                                     ctx->stream));
+  TC_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  const unsigned flags = (unsigned)(ctx->h_pinned[1] & 0xffffffffu);
+  if (flags) return set_error(ctx, TC_ERR_INVALID_GRAPH, "%s", flag_text(flags));
+  *m = (int64_t)ctx->h_pinned[0];
+  *ms_validate = elapsed(ctx->ev[1], ctx->ev[2]);
+  *ms_a = elapsed(ctx->ev[2], ctx->ev[3]);
+  return TC_OK;
+}
+
+}  // namespace tc
+
+extern "C" {
+
+tc_status tc_ctx_create(int device, tc_ctx **out) {
+  if (!out) return set_error(nullptr, TC_ERR_INVALID_ARG, "null out");
+  *out = nullptr;
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || count == 0) {
+    (void)cudaGetLastError();
+    return set_error(nullptr, TC_ERR_NO_DEVICE, "no CUDA device (%s)", cudaGetErrorString(e));
+  }
+  if (device < 0 || device >= count)
+    return set_error(nullptr, TC_ERR_INVALID_ARG, "device %d outside [0,%d)", device, count);
+  tc_ctx *ctx = new tc_ctx();
+  ctx->device = device;
+  auto fail = [&](tc_status st) {
+    tc_ctx_destroy(ctx);
+    return st;
+  };
+  if (cudaSetDevice(device) != cudaSuccess) return fail(set_error(nullptr, TC_ERR_CUDA, "cudaSetDevice failed"));
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess)
+    return fail(set_error(nullptr, TC_ERR_CUDA, "cudaGetDeviceProperties failed"));
+  ctx->num_sms = prop.multiProcessorCount;
+  if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(set_error(nullptr, TC_ERR_CUDA, "stream creation failed"));
+  for (auto &ev : ctx->ev)
+    if (cudaEventCreate(&ev) != cudaSuccess) return fail(set_error(nullptr, TC_ERR_CUDA, "event creation failed"));
+  if (cudaMalloc((void **)&ctx->d_total, 256) != cudaSuccess || cudaMalloc((void **)&ctx->d_flags, 256) != cudaSuccess ||
+      cudaMalloc((void **)&ctx->d_heads, 256) != cudaSuccess ||
+      cudaMalloc((void **)&ctx->d_mlp, TC_MLP_PARAM_COUNT * sizeof(float)) != cudaSuccess ||
+      cudaMallocHost((void **)&ctx->h_pinned, 64 * sizeof(unsigned long long)) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return fail(set_error(nullptr, TC_ERR_OOM, "ctx state allocation failed"));
+  }
+  tc_status st = init_arm_occupancy(ctx);
+  if (st != TC_OK) return fail(st);
+  *out = ctx;
+  return TC_OK;
+}
+
+void tc_ctx_destroy(tc_ctx *ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  cudaFree(ctx->arena);
+  cudaFree(ctx->d_total);
+  cudaFree(ctx->d_flags);
+  cudaFree(ctx->d_heads);
+  cudaFree(ctx->d_mlp);
+  if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
+  if (ctx->batch_exec) cudaGraphExecDestroy(ctx->batch_exec);
+  for (auto &ev : ctx->ev)
+    if (ev) cudaEventDestroy(ev);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  (void)cudaGetLastError();
+  delete ctx;
+}
+
+const char *tc_last_error(const tc_ctx *ctx) { return ctx ? ctx->err : global_error(); }
+
+int64_t tc_ctx_arena_bytes(const tc_ctx *ctx) { return ctx ? (int64_t)ctx->arena_cap : 0; }
+
+void *tc_ctx_stream(tc_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+tc_status tc_ctx_sync(tc_ctx *ctx) {
+  if (!ctx) return set_error(nullptr, TC_ERR_INVALID_ARG, "null ctx");
+  TC_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return TC_OK;
+}
+
+tc_status tc_count(tc_ctx *ctx, const tc_csr *g, const tc_opts *opts_in, uint64_t *total, uint32_t *edge_counts,
+                   int64_t edge_capacity, tc_stats *stats) {
+  if (!ctx || !total) return set_error(ctx, TC_ERR_INVALID_ARG, "null ctx or total");
+  TC_TRY(check_csr_args(ctx, g));
+  tc_opts o;
+  tc_opts_default(&o);
+  if (opts_in) o = *opts_in;
+  TC_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
+  ctx->launches = 0;
+  tc_stats st;
+  memset(&st, 0, sizeof(st));
+  const bool want_edges = edge_counts != nullptr;
+  // arena: staged input + orientation + counting + output staging
+  Sizer sz;
+  if (!g->on_device) { sz.take<int64_t>(g->n + 1); sz.take<int32_t>(g->nnz); }
+  orient_sizes(ctx, g->n, g->nnz, want_edges, false, sz);
+  sz.used += count_scratch_bytes(ctx, g->nnz);
+  if (want_edges && !g->on_device) sz.take<uint32_t>(g->nnz);
+  TC_TRY(arena_reserve(ctx, sz.used));
+  Bump bump{ctx->arena, ctx->arena_cap};
+  TC_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->d_flags, 0, sizeof(unsigned) * 8, ctx->stream));
+  TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[0], ctx->stream));
+  DevCSR d;
+  TC_TRY(stage_csr(ctx, g, bump, d, &st.h2d_bytes));
+  OrientBufs ob;
+  orient_carve(ctx, d.n, d.nnz, want_edges, false, bump, ob);
+  CountBufs cb;
+  if (count_carve(ctx, d.nnz, bump, cb, o.record_tile_costs != 0) != TC_OK || bump.overflow)
+    return set_error(ctx, TC_ERR_OOM, "arena overflow");
+  uint32_t *d_out = nullptr;
+  if (want_edges) d_out = g->on_device ? edge_counts : bump.take<uint32_t>(d.nnz);
+  int64_t m = 0;
+  float ms_a = 0;
+  TC_TRY(orient_front(ctx, d, o, ob, &m, &st.ms_validate, &ms_a));
+  st.ms_h2d = elapsed(ctx->ev[0], ctx->ev[1]);
+  if (want_edges && edge_capacity < m)
+    return set_error(ctx, TC_ERR_INVALID_ARG, "edge_counts holds %lld entries, %lld oriented edges",
+                     (long long)edge_capacity, (long long)m);
+  TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[4], ctx->stream));
+  DevDag dag;
+  TC_TRY(orient_phase_b(ctx, d, ob, m, want_edges, false, &dag));
+  TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[5], ctx->stream));
+  TC_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->d_total, 0, sizeof(unsigned long long), ctx->stream));
+  TC_TRY(run_count(ctx, dag, o, cb, d_out, true));
+  TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[6], ctx->stream));
+  if (want_edges && !g->on_device && m > 0) {
+    TC_CHECK_CUDA(ctx, cudaMemcpyAsync(edge_counts, d_out, sizeof(uint32_t) * (size_t)m, cudaMemcpyDeviceToHost,
+                                       ctx->stream));
+    st.d2h_bytes += sizeof(uint32_t) * (size_t)m;
+  }
+  TC_CHECK_CUDA(ctx, cudaMemcpyAsync(&ctx->h_pinned[2], ctx->d_total, sizeof(unsigned long long),
+                                     cudaMemcpyDeviceToHost, ctx->stream));
+  st.d2h_bytes += sizeof(unsigned long long);
+  TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[7], ctx->stream));
+  TC_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  *total = ctx->h_pinned[2];
+  count_stats(ctx, &st, true);
+  st.ms_orient = ms_a + elapsed(ctx->ev[4], ctx->ev[5]);
+  st.ms_d2h = elapsed(ctx->ev[6], ctx->ev[7]);
+  st.ms_total = elapsed(ctx->ev[0], ctx->ev[7]);
+  st.m = m;
+  st.tiles = (m + TILE_EDGES - 1) / TILE_EDGES;
+  st.kernel_launches = ctx->launches;
+  if (stats) *stats = st;
+  return TC_OK;
+}
+
+tc_status tc_count_dag(tc_ctx *ctx, const tc_csr *dag_in, const tc_opts *opts_in, uint64_t *total,
+                       uint32_t *edge_counts, int64_t edge_capacity, tc_stats *stats) {
+  if (!ctx || !total) return set_error(ctx, TC_ERR_INVALID_ARG, "null ctx or total");
+  TC_TRY(check_csr_args(ctx, dag_in));
+  tc_opts o;
+  tc_opts_default(&o);
+  if (opts_in) o = *opts_in;
+  TC_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
+  ctx->launches = 0;
+  tc_stats st;
+  memset(&st, 0, sizeof(st));
+  const int64_t m = dag_in->nnz;
+  const bool want_edges = edge_counts != nullptr;
+  if (want_edges && edge_capacity < m)
+    return set_error(ctx, TC_ERR_INVALID_ARG, "edge_counts holds %lld entries, %lld edges", (long long)edge_capacity,
+                     (long long)m);
+  Sizer sz;
+  if (!dag_in->on_device) { sz.take<int64_t>(dag_in->n + 1); sz.take<int32_t>(m); }
+  sz.take<int32_t>(m);
+  sz.used += count_scratch_bytes(ctx, m);
+  if (want_edges && !dag_in->on_device) sz.take<uint32_t>(m);
+  TC_TRY(arena_reserve(ctx, sz.used));
+  Bump bump{ctx->arena, ctx->arena_cap};
+  TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[0], ctx->stream));
+  DevCSR d;
+  TC_TRY(stage_csr(ctx, dag_in, bump, d, &st.h2d_bytes));
+  int32_t *src = bump.take<int32_t>(m);
+  CountBufs cb;
+  if (count_carve(ctx, m, bump, cb, o.record_tile_costs != 0) != TC_OK || bump.overflow)
+    return set_error(ctx, TC_ERR_OOM, "arena overflow");
+  uint32_t *d_out = nullptr;
+  if (want_edges) d_out = dag_in->on_device ? edge_counts : bump.take<uint32_t>(m);
+  TC_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->d_flags, 0, sizeof(unsigned) * 8, ctx->stream));
+  TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[1], ctx->stream));
+  // A DAG row may hold any larger-or-smaller ids; only sortedness is required.
+  if (o.validate) TC_TRY(launch_validate(ctx, d, true));
+  TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
+  TC_CHECK_CUDA(ctx, cudaMemcpyAsync(&ctx->h_pinned[1], ctx->d_flags, sizeof(unsigned) * 2, cudaMemcpyDeviceToHost,
+                                     ctx->stream));
+  TC_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  const unsigned flags = (unsigned)(ctx->h_pinned[1] & 0xffffffffu);
+  if (flags) return set_error(ctx, TC_ERR_INVALID_GRAPH, "%s", flag_text(flags));
+  TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[4], ctx->stream));
+  TC_TRY(launch_expand_src(ctx, d.rowptr, d.n, m, src));
+  TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[5], ctx->stream));
+  DevDag dag;
+  dag.n = d.n;
+  dag.m = m;
+  dag.rowptr = d.rowptr;
+  dag.col = d.col;
+  dag.src = src;
+  dag.perm = nullptr;
+  dag.restrict_after = 0;
+  TC_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->d_total, 0, sizeof(unsigned long long), ctx->stream));
+  TC_TRY(run_count(ctx, dag, o, cb, d_out, true));
+  TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[6], ctx->stream));
+  if (want_edges && !dag_in->on_device && m > 0) {
+    TC_CHECK_CUDA(ctx, cudaMemcpyAsync(edge_counts, d_out, sizeof(uint32_t) * (size_t)m, cudaMemcpyDeviceToHost,
+                                       ctx->stream));
+    st.d2h_bytes += sizeof(uint32_t) * (size_t)m;
+  }
+  TC_CHECK_CUDA(ctx, cudaMemcpyAsync(&ctx->h_pinned[2], ctx->d_total, sizeof(unsigned long long),
+                                     cudaMemcpyDeviceToHost, ctx->stream));
+  st.d2h_bytes += sizeof(unsigned long long);
+  TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[7], ctx->stream));
+  TC_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  *total = ctx->h_pinned[2];
+  count_stats(ctx, &st, true);
+  st.ms_h2d = elapsed(ctx->ev[0], ctx->ev[1]);
+  st.ms_validate = elapsed(ctx->ev[1], ctx->ev[2]);
+  st.ms_orient = elapsed(ctx->ev[4], ctx->ev[5]);
+  st.ms_d2h = elapsed(ctx->ev[6], ctx->ev[7]);
+  st.ms_total = elapsed(ctx->ev[0], ctx->ev[7]);
+  st.m = m;
+  st.tiles = (m + TILE_EDGES - 1) / TILE_EDGES;
+  st.kernel_launches = ctx->launches;
+  if (stats) *stats = st;
+  return TC_OK;
+}
+
+tc_status tc_orient(tc_ctx *ctx, const tc_csr *g, int64_t *dag_rowptr, int32_t *dag_colidx, int64_t dag_capacity,
+                    int64_t *m_out) {
+  if (!ctx || !dag_rowptr || !m_out) return set_error(ctx, TC_ERR_INVALID_ARG, "null argument");
+  TC_TRY(check_csr_args(ctx, g));
+  tc_opts o;
+  tc_opts_default(&o);
+  TC_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
+  ctx->launches = 0;
+  Sizer sz;
+  if (!g->on_device) { sz.take<int64_t>(g->n + 1); sz.take<int32_t>(g->nnz); }
+  orient_sizes(ctx, g->n, g->nnz, false, true, sz);
+  if (!g->on_device) sz.take<int64_t>(g->n + 1);
+  TC_TRY(arena_reserve(ctx, sz.used));
+  Bump bump{ctx->arena, ctx->arena_cap};
+  TC_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->d_flags, 0, sizeof(unsigned) * 8, ctx->stream));
+  uint64_t h2d = 0;
+  DevCSR d;
+  TC_TRY(stage_csr(ctx, g, bump, d, &h2d));
+  OrientBufs ob;
+  orient_carve(ctx, d.n, d.nnz, false, true, bump, ob);
+  int64_t *d_rp = g->on_device ? dag_rowptr : bump.take<int64_t>(g->n + 1);
+  if (bump.overflow) return set_error(ctx, TC_ERR_OOM, "arena overflow");
+  int64_t m = 0;
+  float a, b;
+  TC_TRY(orient_front(ctx, d, o, ob, &m, &a, &b));
+  *m_out = m;
+  if (m > dag_capacity || (m > 0 && !dag_colidx))
+    return set_error(ctx, TC_ERR_INVALID_ARG, "dag_colidx holds %lld entries, %lld needed", (long long)dag_capacity,
+                     (long long)m);
+  if (g->on_device) ob.dag_col = dag_colidx;
+  DevDag dag;
+  TC_TRY(orient_phase_b(ctx, d, ob, m, false, true, &dag));
+  // original-id rowptr: exclusive scan of the kept out-degrees (kept[n] == 0)
+  TC_TRY(exclusive_scan_i64(ctx, ob.kept, d_rp, d.n + 1, ob.sort_scratch, nullptr));
+  if (!g->on_device) {
+    TC_CHECK_CUDA(ctx, cudaMemcpyAsync(dag_rowptr, d_rp, sizeof(int64_t) * (size_t)(d.n + 1), cudaMemcpyDeviceToHost,
+                                       ctx->stream));
+    if (m > 0)
+      TC_CHECK_CUDA(ctx, cudaMemcpyAsync(dag_colidx, ob.dag_col, sizeof(int32_t) * (size_t)m, cudaMemcpyDeviceToHost,
+                                         ctx->stream));
+  }
+  TC_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return TC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,609 @@
+// Triangle counting over an oriented graph: per-edge |N+(u) n N+(v)|.
+//
+// Work is cut into 4096-edge tiles.  A planning pass computes per-tile
+// degree features and picks an exact intersection strategy ("arm") for each
+// tile, either with fixed degree thresholds or with the MLP cost model.
+// Tiles are radix-sorted into one queue per arm (heaviest first) and each
+// arm runs as a persistent kernel whose blocks pull tiles with an atomic
+// head, so load balance does not depend on the launch grid.
+//
+// Arms (all exact; they replace the reference's warp_vertex +
+// intersect_num, bs_warp_vertex.cuh:13-21, graph_gpu.h:228-252):
+//   BSEARCH_G  G lanes per edge; each lane binary-searches keys of the
+//              shorter list in the longer one (the reference's warp_intersect
+//              pattern, with the search window carried between keys).
+//   MERGE_G    G lanes per edge walk both lists in G-wide windows; each lane
+//              locates its A element in the B window with log2(G) shuffles;
+//              the window with the smaller last element advances.
+//   BITMAP     a block stages the row's remaining out-list as a bitmap over
+//              its id window in shared memory and probes every N+(v) against
+//              it; rows whose window does not fit fall back to warp search.
+#include "engine.cuh"
+
+namespace tc {
+
+constexpr int CT_THREADS = 256;
+constexpr int BM_THREADS = 512;
+constexpr int BM_SMEM_BYTES = 100 * 1024;
+constexpr int64_t BM_BITS = (int64_t)BM_SMEM_BYTES * 8;
+constexpr int PLAN_THREADS = 256;
+
+// ---- plan: features + selection ------------------------------------------------
+
+struct PlanStats {
+  float mean_da, mean_db, mean_min, mean_max, lr, alr;
+  float nrows, maxdr, maxwin, frac;
+  float bins[6];
+};
+
+__device__ __forceinline__ float flog2p1(float x) { return __log2f(1.0f + x); }
+
+// Fixed degree-threshold selector: the engine's fallback and the judge of the
+// learned one.
+__device__ __forceinline__ int fixed_select(const PlanStats &s) {
+  if (s.nrows <= 8.f && s.maxwin <= (float)BM_BITS && s.mean_db >= 4.f && s.frac >= 0.25f) return TC_ARM_BITMAP;
+  if (s.mean_min >= 48.f && s.mean_max <= 8.f * s.mean_min) return TC_ARM_MERGE_32;
+  if (s.mean_min >= 8.f && s.mean_max <= 4.f * s.mean_min) return TC_ARM_MERGE_8;
+  if (s.mean_min >= 16.f) return TC_ARM_BSEARCH_32;
+  if (s.mean_min >= 4.f) return TC_ARM_BSEARCH_8;
+  return TC_ARM_BSEARCH_4;
+}
+
+// MLP cost model (16 -> 64 -> 64 -> arms, ReLU); weights staged in shared
+// memory rounded to bf16, fp32 accumulation.  Returns the arm with the lowest
+// predicted cost.
+__device__ int mlp_select(const float *__restrict__ w, const float *f, int lane) {
+  const float *W1 = w, *b1 = W1 + TC_MLP_FEATURES * TC_MLP_HIDDEN;
+  const float *W2 = b1 + TC_MLP_HIDDEN, *b2 = W2 + TC_MLP_HIDDEN * TC_MLP_HIDDEN;
+  const float *W3 = b2 + TC_MLP_HIDDEN, *b3 = W3 + TC_MLP_HIDDEN * TC_NUM_ARMS;
+  float h1[2], h2[2];
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    const int j = lane + 32 * q;
+    float a = b1[j];
+#pragma unroll
+    for (int i = 0; i < TC_MLP_FEATURES; ++i) a = fmaf(f[i], W1[i * TC_MLP_HIDDEN + j], a);
+    h1[q] = fmaxf(a, 0.f);
+  }
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    const int j = lane + 32 * q;
+    float a = b2[j];
+    for (int i = 0; i < TC_MLP_HIDDEN; ++i) {
+      const float hi = __shfl_sync(TC_FULL_MASK, h1[i >> 5], i & 31);
+      a = fmaf(hi, W2[i * TC_MLP_HIDDEN + j], a);
+    }
+    h2[q] = fmaxf(a, 0.f);
+  }
+  int best = 0;
+  float bestv = 0.f;
+#pragma unroll
+  for (int k = 0; k < TC_NUM_ARMS; ++k) {
+    float p = h2[0] * W3[lane * TC_NUM_ARMS + k] + h2[1] * W3[(lane + 32) * TC_NUM_ARMS + k];
+    p = warp_sum(p) + b3[k];
+    if (k == 0 || p < bestv) { bestv = p; best = k; }
+  }
+  return best;
+}
+
+__global__ void __launch_bounds__(PLAN_THREADS) plan_kernel(DevDag g, int64_t T, int selector, int force_arm,
+                                                           const float *__restrict__ mlp, float *__restrict__ feats,
+                                                           int32_t *__restrict__ arm_out,
+                                                           uint64_t *__restrict__ qkeys,
+                                                           uint32_t *__restrict__ qvals,
+                                                           unsigned long long *__restrict__ tile_bytes) {
+  extern __shared__ float s_w[];
+  const int lane = threadIdx.x & 31;
+  if (selector == TC_SELECT_LEARNED) {
+    for (int i = threadIdx.x; i < TC_MLP_PARAM_COUNT; i += blockDim.x)
+      s_w[i] = __bfloat162float(__float2bfloat16(mlp[i]));
+    __syncthreads();
+  }
+  const int64_t t = (int64_t)blockIdx.x * (PLAN_THREADS / 32) + (threadIdx.x >> 5);
+  if (t >= T) return;
+  const int64_t e0 = t * TILE_EDGES, e1 = min(g.m, e0 + TILE_EDGES);
+  float sda = 0, sdb = 0, smin = 0, smax = 0, slr = 0, salr = 0;
+  float bins[6] = {0, 0, 0, 0, 0, 0};
+  unsigned long long work = 0, alg = 0;
+  int nrows = 0;
+  long long maxdr = 0, maxwin = 0;
+  for (int64_t e = e0 + lane; e < e1; e += 32) {
+    const int32_t r = g.src[e], s = g.col[e];
+    const int64_t rb = g.rowptr[r], re = g.rowptr[r + 1];
+    const int64_t a0 = g.restrict_after ? e + 1 : rb;
+    const float da = (float)(re - a0);
+    const float db = (float)(g.rowptr[s + 1] - g.rowptr[s]);
+    sda += da;
+    sdb += db;
+    const float mn = fminf(da, db), mx = fmaxf(da, db);
+    smin += mn;
+    smax += mx;
+    const float lr = flog2p1(da) - flog2p1(db);
+    slr += lr;
+    salr += fabsf(lr);
+    const int bin = mn < 2.f ? 0 : mn < 8.f ? 1 : mn < 32.f ? 2 : mn < 128.f ? 3 : mn < 512.f ? 4 : 5;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) bins[k] += (bin == k) ? 1.f : 0.f;
+    work += (unsigned long long)(da + db);
+    alg += 4ULL * (unsigned long long)((re - rb) + (g.rowptr[s + 1] - g.rowptr[s])) + 4ULL;
+    if (e == e0 || g.src[e - 1] != r) {
+      ++nrows;
+      maxdr = max(maxdr, (long long)(re - rb));
+      const int64_t s0 = g.restrict_after ? e + 1 : rb;
+      if (s0 < re) maxwin = max(maxwin, (long long)g.col[re - 1] - (long long)g.col[s0] + 1);
+    }
+  }
+  sda = warp_sum(sda); sdb = warp_sum(sdb); smin = warp_sum(smin); smax = warp_sum(smax);
+  slr = warp_sum(slr); salr = warp_sum(salr);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) bins[k] = warp_sum(bins[k]);
+  work = warp_sum(work);
+  alg = warp_sum(alg);
+  nrows = warp_sum(nrows);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    maxdr = max(maxdr, __shfl_xor_sync(TC_FULL_MASK, maxdr, o));
+    maxwin = max(maxwin, __shfl_xor_sync(TC_FULL_MASK, maxwin, o));
+  }
+  const float ne = (float)(e1 - e0);
+  PlanStats st;
+  st.mean_da = sda / ne; st.mean_db = sdb / ne; st.mean_min = smin / ne; st.mean_max = smax / ne;
+  st.lr = slr / ne; st.alr = salr / ne;
+  st.nrows = (float)nrows; st.maxdr = (float)maxdr; st.maxwin = (float)maxwin; st.frac = ne / (float)TILE_EDGES;
+  float f[TC_MLP_FEATURES];
+  f[0] = flog2p1(st.mean_da) / 16.f;
+  f[1] = flog2p1(st.mean_db) / 16.f;
+  f[2] = st.lr / 16.f;
+  f[3] = st.alr / 16.f;
+  f[4] = flog2p1(st.mean_min) / 16.f;
+  f[5] = flog2p1(st.mean_max) / 16.f;
+  f[6] = flog2p1(st.nrows) / 12.f;
+  f[7] = flog2p1(st.maxdr) / 16.f;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) f[8 + k] = bins[k] / ne;
+  f[14] = flog2p1(st.maxwin) / 24.f;
+  f[15] = st.frac;
+  int arm;
+  if (selector == TC_SELECT_FORCE) arm = force_arm;
+  else if (selector == TC_SELECT_LEARNED) arm = mlp_select(s_w, f, lane);
+  else arm = fixed_select(st);
+  if (lane < TC_MLP_FEATURES) feats[t * TC_MLP_FEATURES + lane] = f[lane];
+  if (lane == 0) {
+    arm_out[t] = arm;
+    const unsigned long long W40 = (1ULL << 40) - 1;
+    qkeys[t] = ((unsigned long long)arm << 40) | (W40 - min(work, W40));
+    qvals[t] = (uint32_t)t;
+    tile_bytes[t] = alg;
+  }
+}
+
+// Algorithmic bytes of every arm's tiles (block a sums queue a).
+__global__ void arm_bytes_kernel(const uint32_t *__restrict__ qtiles, const int64_t *__restrict__ qoff,
+                                 const unsigned long long *__restrict__ tile_bytes,
+                                 unsigned long long *__restrict__ out) {
+  __shared__ unsigned long long part[8];
+  const int a = blockIdx.x;
+  unsigned long long s = 0;
+  for (int64_t i = qoff[a] + threadIdx.x; i < qoff[a + 1]; i += blockDim.x) s += tile_bytes[qtiles[i]];
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += part[w];
+    out[a] = t;
+  }
+}
+
+__global__ void qoff_kernel(const uint64_t *__restrict__ keys, int64_t T, int64_t *__restrict__ qoff) {
+  const int k = threadIdx.x;
+  if (k > TC_NUM_ARMS) return;
+  int64_t lo = 0, hi = T;  // first index with arm >= k
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if ((int64_t)(keys[mid] >> 40) < k) lo = mid + 1; else hi = mid;
+  }
+  qoff[k] = lo;
+}
+
+// ---- shared pieces of the arm kernels -----------------------------------------
+
+struct EdgeLists {
+  const int32_t *a;  // remaining out-list of the row
+  const int32_t *b;  // out-list of the column vertex
+  int na, nb;
+};
+
+__device__ __forceinline__ EdgeLists edge_lists(const DevDag &g, int64_t e, int32_t &s_out) {
+  const int32_t r = g.src[e], s = g.col[e];
+  s_out = s;
+  const int64_t rb = g.rowptr[r], re = g.rowptr[r + 1];
+  const int64_t a0 = g.restrict_after ? e + 1 : rb;
+  const int64_t sb = g.rowptr[s], se = g.rowptr[s + 1];
+  EdgeLists L;
+  L.a = g.col + a0;
+  L.na = (int)(re - a0);
+  L.b = g.col + sb;
+  L.nb = (int)(se - sb);
+  return L;
+}
+
+__device__ __forceinline__ void put_edge_count(const DevDag &g, uint32_t *out, int64_t e, uint32_t c) {
+  if (out) out[g.perm ? (int64_t)g.perm[e] : e] = c;
+}
+
+// Pull the next tile of this arm's queue (block-uniform result).
+__device__ __forceinline__ int64_t next_tile(const uint32_t *__restrict__ qtiles, int64_t qb, int64_t qn,
+                                             unsigned *head, int64_t *s_tile) {
+  if (threadIdx.x == 0) {
+    const unsigned it = atomicAdd(head, 1u);
+    *s_tile = (int64_t)it < qn ? (int64_t)qtiles[qb + it] : -1;
+  }
+  __syncthreads();
+  const int64_t t = *s_tile;
+  __syncthreads();
+  return t;
+}
+
+__device__ __forceinline__ void flush_total(unsigned long long acc, unsigned long long *total) {
+  __shared__ unsigned long long s_acc;
+  if (threadIdx.x == 0) s_acc = 0;
+  __syncthreads();
+  acc = warp_sum(acc);
+  if ((threadIdx.x & 31) == 0 && acc) atomicAdd(&s_acc, acc);
+  __syncthreads();
+  if (threadIdx.x == 0 && s_acc) atomicAdd(total, s_acc);
+}
+
+// Count of keys of sorted `l` (nl) present in sorted `s` (ns), lanes
+// gl, gl+G, ... of a G-lane group; the search window's lower end only moves
+// forward because keys grow.
+template <int G>
+__device__ __forceinline__ uint32_t bsearch_count(const int32_t *__restrict__ l, int nl,
+                                                  const int32_t *__restrict__ s, int ns, int gl) {
+  uint32_t c = 0;
+  int lo = 0;
+  for (int i = gl; i < nl; i += G) {
+    const int32_t key = __ldg(l + i);
+    int hi = ns;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (__ldg(s + mid) < key) lo = mid + 1; else hi = mid;
+    }
+    if (lo < ns && __ldg(s + lo) == key) ++c;
+  }
+  return c;
+}
+
+template <int G>
+__device__ __forceinline__ uint32_t group_sum(uint32_t v, unsigned gmask) {
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(gmask, v, o, G);
+  return v;
+}
+
+template <int G>
+__device__ __forceinline__ unsigned group_mask(int lane) {
+  if (G == 32) return TC_FULL_MASK;
+  return ((1u << G) - 1u) << (lane & ~(G - 1));
+}
+
+// ---- BSEARCH_G ------------------------------------------------------------------
+
+template <int G>
+__global__ void __launch_bounds__(CT_THREADS) bsearch_kernel(DevDag g, const uint32_t *__restrict__ qtiles,
+                                                            const int64_t *__restrict__ qoff, int arm,
+                                                            unsigned *head, uint32_t *out,
+                                                            unsigned long long *total,
+                                                            unsigned long long *tile_cycles) {
+  __shared__ int64_t s_tile;
+  const int64_t qb = qoff[arm], qn = qoff[arm + 1] - qb;
+  const int lane = threadIdx.x & 31, gl = threadIdx.x % G, gid = threadIdx.x / G;
+  constexpr int NG = CT_THREADS / G;
+  const unsigned gm = group_mask<G>(lane);
+  unsigned long long acc = 0;
+  for (;;) {
+    const int64_t tile = next_tile(qtiles, qb, qn, head, &s_tile);
+    if (tile < 0) break;
+    const long long c0 = clock64();
+    const int64_t e0 = tile * TILE_EDGES, e1 = min(g.m, e0 + TILE_EDGES);
+    for (int64_t e = e0 + gid; e < e1; e += NG) {
+      int32_t s;
+      const EdgeLists L = edge_lists(g, e, s);
+      uint32_t c = 0;
+      if (L.na > 0 && L.nb > 0) {
+        if (L.na <= L.nb) c = bsearch_count<G>(L.a, L.na, L.b, L.nb, gl);
+        else c = bsearch_count<G>(L.b, L.nb, L.a, L.na, gl);
+      }
+      c = group_sum<G>(c, gm);
+      if (gl == 0) {
+        put_edge_count(g, out, e, c);
+        acc += c;
+      }
+    }
+    if (tile_cycles) {
+      __syncthreads();
+      if (threadIdx.x == 0) tile_cycles[tile] = (unsigned long long)(clock64() - c0);
+    }
+  }
+  flush_total(acc, total);
+}
+
+// ---- MERGE_G ---------------------------------------------------------------------
+
+template <int G>
+__device__ __forceinline__ uint32_t merge_count(const int32_t *__restrict__ A, int na, const int32_t *__restrict__ B,
+                                                int nb, int gl, unsigned gm) {
+  uint32_t c = 0;
+  int i = 0, j = 0;
+  while (i < na && j < nb) {
+    const int32_t av = (i + gl < na) ? __ldg(A + i + gl) : INT32_MAX;
+    const int32_t bv = (j + gl < nb) ? __ldg(B + j + gl) : INT32_MAX;
+    const int32_t alast = __shfl_sync(gm, av, min(G - 1, na - i - 1), G);
+    const int32_t blast = __shfl_sync(gm, bv, min(G - 1, nb - j - 1), G);
+    int pos = 0;
+#pragma unroll
+    for (int step = G / 2; step > 0; step >>= 1) {
+      const int32_t probe = __shfl_sync(gm, bv, pos + step - 1, G);
+      if (probe < av) pos += step;
+    }
+    const int32_t hit = __shfl_sync(gm, bv, pos, G);
+    if (av != INT32_MAX && hit == av) ++c;
+    if (alast <= blast) i += G;
+    if (blast <= alast) j += G;
+  }
+  return c;
+}
+
+template <int G>
+__global__ void __launch_bounds__(CT_THREADS) merge_kernel(DevDag g, const uint32_t *__restrict__ qtiles,
+                                                          const int64_t *__restrict__ qoff, int arm, unsigned *head,
+                                                          uint32_t *out, unsigned long long *total,
+                                                          unsigned long long *tile_cycles) {
+  __shared__ int64_t s_tile;
+  const int64_t qb = qoff[arm], qn = qoff[arm + 1] - qb;
+  const int lane = threadIdx.x & 31, gl = threadIdx.x % G, gid = threadIdx.x / G;
+  constexpr int NG = CT_THREADS / G;
+  const unsigned gm = group_mask<G>(lane);
+  unsigned long long acc = 0;
+  for (;;) {
+    const int64_t tile = next_tile(qtiles, qb, qn, head, &s_tile);
+    if (tile < 0) break;
+    const long long c0 = clock64();
+    const int64_t e0 = tile * TILE_EDGES, e1 = min(g.m, e0 + TILE_EDGES);
+    for (int64_t e = e0 + gid; e < e1; e += NG) {
+      int32_t s;
+      const EdgeLists L = edge_lists(g, e, s);
+      uint32_t c = 0;
+      if (L.na > 0 && L.nb > 0) c = merge_count<G>(L.a, L.na, L.b, L.nb, gl, gm);
+      c = group_sum<G>(c, gm);
+      if (gl == 0) {
+        put_edge_count(g, out, e, c);
+        acc += c;
+      }
+    }
+    if (tile_cycles) {
+      __syncthreads();
+      if (threadIdx.x == 0) tile_cycles[tile] = (unsigned long long)(clock64() - c0);
+    }
+  }
+  flush_total(acc, total);
+}
+
+// ---- BITMAP ------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(BM_THREADS) bitmap_kernel(DevDag g, const uint32_t *__restrict__ qtiles,
+                                                           const int64_t *__restrict__ qoff, int arm, unsigned *head,
+                                                           uint32_t *out, unsigned long long *total,
+                                                           unsigned long long *tile_cycles) {
+  extern __shared__ uint32_t bm[];
+  __shared__ int64_t s_tile;
+  const int64_t qb = qoff[arm], qn = qoff[arm + 1] - qb;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int NW = BM_THREADS / 32;
+  unsigned long long acc = 0;
+  for (;;) {
+    const int64_t tile = next_tile(qtiles, qb, qn, head, &s_tile);
+    if (tile < 0) break;
+    const long long c0 = clock64();
+    const int64_t e0 = tile * TILE_EDGES, e1 = min(g.m, e0 + TILE_EDGES);
+    for (int64_t sb = e0; sb < e1;) {
+      const int32_t r = g.src[sb];
+      const int64_t rb = g.rowptr[r], re = g.rowptr[r + 1];
+      const int64_t se = min(e1, re);
+      const int64_t a0 = g.restrict_after ? sb + 1 : rb;
+      const int64_t win = (a0 < re) ? (int64_t)g.col[re - 1] - (int64_t)g.col[a0] + 1 : 0;
+      if (a0 < re && win <= BM_BITS) {
+        const int32_t lo = g.col[a0], hi = g.col[re - 1];
+        const int words = (int)((win + 31) >> 5);
+        for (int w = threadIdx.x; w < words; w += BM_THREADS) bm[w] = 0u;
+        __syncthreads();
+        for (int64_t k = a0 + threadIdx.x; k < re; k += BM_THREADS) {
+          const uint32_t x = (uint32_t)(g.col[k] - lo);
+          atomicOr(&bm[x >> 5], 1u << (x & 31));
+        }
+        __syncthreads();
+        for (int64_t e = sb + warp; e < se; e += NW) {
+          const int32_t s = g.col[e];
+          const int32_t *B = g.col + g.rowptr[s];
+          const int nb = (int)(g.rowptr[s + 1] - g.rowptr[s]);
+          uint32_t c = 0;
+          for (int k = lane; k < nb; k += 32) {
+            const int32_t w = __ldg(B + k);
+            if (w > hi) break;
+            if (w >= lo) {
+              const uint32_t x = (uint32_t)(w - lo);
+              c += (bm[x >> 5] >> (x & 31)) & 1u;
+            }
+          }
+          c = warp_sum(c);
+          if (lane == 0) {
+            put_edge_count(g, out, e, c);
+            acc += c;
+          }
+        }
+        __syncthreads();
+      } else {
+        for (int64_t e = sb + warp; e < se; e += NW) {
+          int32_t s;
+          const EdgeLists L = edge_lists(g, e, s);
+          uint32_t c = 0;
+          if (L.na > 0 && L.nb > 0) {
+            if (L.na <= L.nb) c = bsearch_count<32>(L.a, L.na, L.b, L.nb, lane);
+            else c = bsearch_count<32>(L.b, L.nb, L.a, L.na, lane);
+          }
+          c = warp_sum(c);
+          if (lane == 0) {
+            put_edge_count(g, out, e, c);
+            acc += c;
+          }
+        }
+      }
+      sb = se;
+    }
+    if (tile_cycles) {
+      __syncthreads();
+      if (threadIdx.x == 0) tile_cycles[tile] = (unsigned long long)(clock64() - c0);
+    }
+  }
+  flush_total(acc, total);
+}
+
+// ---- host side ---------------------------------------------------------------------
+
+typedef void (*ArmKernel)(DevDag, const uint32_t *, const int64_t *, int, unsigned *, uint32_t *,
+                          unsigned long long *, unsigned long long *);
+
+static ArmKernel arm_kernel(int arm) {
+  switch (arm) {
+    case TC_ARM_BSEARCH_4: return bsearch_kernel<4>;
+    case TC_ARM_BSEARCH_8: return bsearch_kernel<8>;
+    case TC_ARM_BSEARCH_32: return bsearch_kernel<32>;
+    case TC_ARM_MERGE_8: return merge_kernel<8>;
+    case TC_ARM_MERGE_32: return merge_kernel<32>;
+    default: return bitmap_kernel;
+  }
+}
+static int arm_threads(int arm) { return arm == TC_ARM_BITMAP ? BM_THREADS : CT_THREADS; }
+static int arm_smem(int arm) { return arm == TC_ARM_BITMAP ? BM_SMEM_BYTES : 0; }
+
+tc_status init_arm_occupancy(tc_ctx *ctx) {
+  TC_CHECK_CUDA(ctx, cudaFuncSetAttribute(bitmap_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, BM_SMEM_BYTES));
+  TC_CHECK_CUDA(ctx, cudaFuncSetAttribute(plan_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)(TC_MLP_PARAM_COUNT * sizeof(float))));
+  for (int a = 0; a < TC_NUM_ARMS; ++a) {
+    int nb = 0;
+    TC_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, arm_kernel(a), arm_threads(a), arm_smem(a)));
+    ctx->arm_blocks_per_sm[a] = nb > 0 ? nb : 1;
+  }
+  return TC_OK;
+}
+
+size_t count_scratch_bytes(const tc_ctx *ctx, int64_t m) {
+  const int64_t T = (m + TILE_EDGES - 1) / TILE_EDGES;
+  Sizer sz;
+  sz.take<float>(T * TC_MLP_FEATURES);
+  sz.take<uint64_t>(T);
+  sz.take<uint64_t>(T);
+  sz.take<uint32_t>(T);
+  sz.take<uint32_t>(T);
+  sz.take<int32_t>(T);
+  sz.take<int64_t>(TC_NUM_ARMS + 1);
+  sz.take<unsigned long long>(T);
+  sz.take<unsigned long long>(T);
+  sz.take<unsigned long long>(TC_NUM_ARMS);
+  return sz.used + radix_sort_scratch_bytes(ctx, T > 0 ? T : 1) + 256;
+}
+
+tc_status count_carve(const tc_ctx *ctx, int64_t m, Bump &bump, CountBufs &cb, bool want_cycles) {
+  const int64_t T = (m + TILE_EDGES - 1) / TILE_EDGES;
+  cb.features = bump.take<float>(T * TC_MLP_FEATURES);
+  cb.qkeys0 = bump.take<uint64_t>(T);
+  cb.qkeys1 = bump.take<uint64_t>(T);
+  cb.qvals0 = bump.take<uint32_t>(T);
+  cb.qvals1 = bump.take<uint32_t>(T);
+  cb.arm = bump.take<int32_t>(T);
+  cb.qoff = bump.take<int64_t>(TC_NUM_ARMS + 1);
+  unsigned long long *cyc = bump.take<unsigned long long>(T);
+  cb.tile_cycles = want_cycles ? cyc : nullptr;
+  cb.tile_bytes = bump.take<unsigned long long>(T);
+  cb.arm_bytes = bump.take<unsigned long long>(TC_NUM_ARMS);
+  cb.sort_scratch = bump.take<char>((int64_t)radix_sort_scratch_bytes(ctx, T > 0 ? T : 1));
+  return bump.overflow ? TC_ERR_OOM : TC_OK;
+}
+
+// Pinned host scratch layout used by run_count / count_stats.
+constexpr int PIN_QOFF = 16;   // TC_NUM_ARMS + 1 int64
+constexpr int PIN_BYTES = 24;  // TC_NUM_ARMS uint64
+
+tc_status run_count(tc_ctx *ctx, const DevDag &g, const tc_opts &opts, CountBufs &cb, uint32_t *out, bool timing) {
+  const int64_t T = (g.m + TILE_EDGES - 1) / TILE_EDGES;
+  if (opts.selector == TC_SELECT_LEARNED && !ctx->mlp_loaded)
+    return set_error(ctx, TC_ERR_INVALID_ARG, "learned selector requested but no MLP weights are loaded");
+  if (opts.selector == TC_SELECT_FORCE && (opts.force_arm < 0 || opts.force_arm >= TC_NUM_ARMS))
+    return set_error(ctx, TC_ERR_INVALID_ARG, "force_arm %d outside [0,%d)", opts.force_arm, TC_NUM_ARMS);
+  if (timing) TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[8], ctx->stream));
+  if (T == 0) {
+    TC_CHECK_CUDA(ctx, cudaMemsetAsync(cb.qoff, 0, sizeof(int64_t) * (TC_NUM_ARMS + 1), ctx->stream));
+    TC_CHECK_CUDA(ctx, cudaMemsetAsync(cb.arm_bytes, 0, sizeof(unsigned long long) * TC_NUM_ARMS, ctx->stream));
+  } else {
+    const int plan_blocks = (int)((T + (PLAN_THREADS / 32) - 1) / (PLAN_THREADS / 32));
+    const size_t plan_smem = opts.selector == TC_SELECT_LEARNED ? TC_MLP_PARAM_COUNT * sizeof(float) : 0;
+    plan_kernel<<<plan_blocks, PLAN_THREADS, plan_smem, ctx->stream>>>(g, T, opts.selector, opts.force_arm,
+                                                                       ctx->d_mlp, cb.features, cb.arm, cb.qkeys0,
+                                                                       cb.qvals0, cb.tile_bytes);
+    TC_CHECK_LAUNCH(ctx);
+  }
+  uint64_t *sk = cb.qkeys0;
+  uint32_t *sv = cb.qvals0;
+  if (T > 1) TC_TRY(radix_sort(ctx, cb.qkeys0, cb.qkeys1, cb.qvals0, cb.qvals1, T, 43, cb.sort_scratch, &sk, &sv));
+  if (T > 0) {
+    qoff_kernel<<<1, 32, 0, ctx->stream>>>(sk, T, cb.qoff);
+    TC_CHECK_LAUNCH(ctx);
+    arm_bytes_kernel<<<TC_NUM_ARMS, 256, 0, ctx->stream>>>(sv, cb.qoff, cb.tile_bytes, cb.arm_bytes);
+    TC_CHECK_LAUNCH(ctx);
+  }
+  TC_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->d_heads, 0, sizeof(unsigned) * 64, ctx->stream));
+  if (timing) TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[9], ctx->stream));
+  for (int a = 0; a < TC_NUM_ARMS; ++a) {
+    if (T > 0) {
+      const int grid = ctx->num_sms * ctx->arm_blocks_per_sm[a];
+      arm_kernel(a)<<<grid, arm_threads(a), arm_smem(a), ctx->stream>>>(g, sv, cb.qoff, a, ctx->d_heads + a, out,
+                                                                        ctx->d_total, cb.tile_cycles);
+      TC_CHECK_LAUNCH(ctx);
+    }
+    if (timing) TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[10 + a], ctx->stream));
+  }
+  TC_CHECK_CUDA(ctx, cudaMemcpyAsync(&ctx->h_pinned[PIN_QOFF], cb.qoff, sizeof(int64_t) * (TC_NUM_ARMS + 1),
+                                     cudaMemcpyDeviceToHost, ctx->stream));
+  TC_CHECK_CUDA(ctx, cudaMemcpyAsync(&ctx->h_pinned[PIN_BYTES], cb.arm_bytes, sizeof(unsigned long long) * TC_NUM_ARMS,
+                                     cudaMemcpyDeviceToHost, ctx->stream));
+  return TC_OK;
+}
+
+static float ev_ms(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0;
+  if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return 0;
+  }
+  return ms;
+}
+
+void count_stats(tc_ctx *ctx, tc_stats *st, bool timing) {
+  const int64_t *hq = reinterpret_cast<const int64_t *>(&ctx->h_pinned[PIN_QOFF]);
+  const unsigned long long *hb = &ctx->h_pinned[PIN_BYTES];
+  uint64_t tot = 0;
+  for (int a = 0; a < TC_NUM_ARMS; ++a) {
+    st->tiles_per_arm[a] = hq[a + 1] - hq[a];
+    st->alg_bytes_arm[a] = hb[a];
+    tot += hb[a];
+  }
+  st->alg_bytes = tot;
+  if (!timing) return;
+  st->ms_plan = ev_ms(ctx->ev[8], ctx->ev[9]);
+  st->ms_count = ev_ms(ctx->ev[9], ctx->ev[10 + TC_NUM_ARMS - 1]);
+  for (int a = 0; a < TC_NUM_ARMS; ++a) st->ms_arm[a] = ev_ms(ctx->ev[a == 0 ? 9 : 9 + a], ctx->ev[10 + a]);
+}
+
+}  // namespace tc

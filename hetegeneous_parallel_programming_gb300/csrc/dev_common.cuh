@@ -1,0 +1,222 @@
+// Device-side building blocks shared by the engine's .cu files: the ctx
+// struct, error plumbing, the grow-only device arena and block/warp
+// primitives (scans, row expansion of CSR tiles).
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#include "tc_internal.h"
+
+#define TC_FULL_MASK 0xffffffffu
+
+struct tc_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  // grow-only arena
+  char *arena = nullptr;
+  size_t arena_cap = 0;
+  size_t arena_used = 0;
+  // small always-resident device state
+  unsigned long long *d_total = nullptr;  // [1] running total
+  unsigned int *d_flags = nullptr;        // [8] error flags / counters
+  unsigned int *d_heads = nullptr;        // [64] work-queue heads
+  unsigned long long *h_pinned = nullptr; // [64] pinned host scratch
+  cudaEvent_t ev[16] = {};
+  // learned selector
+  float *d_mlp = nullptr;                 // TC_MLP_PARAM_COUNT floats
+  bool mlp_loaded = false;
+  // per-arm kernel occupancy (blocks per SM), filled at create
+  int arm_blocks_per_sm[TC_NUM_ARMS] = {};
+  int64_t launches = 0;                   // kernels launched by the current call
+  // captured back half of the batched pipeline (batch.cu), keyed by shape,
+  // options and the buffers it reads
+  cudaGraphExec_t batch_exec = nullptr;
+  int64_t batch_key[12] = {};
+  int64_t batch_launches = 0;
+  char err[1024] = {0};
+};
+
+namespace tc {
+
+tc_status set_error(tc_ctx *ctx, tc_status st, const char *fmt, ...);
+
+#define TC_CHECK_CUDA(ctx, call)                                                                \
+  do {                                                                                          \
+    cudaError_t e_ = (call);                                                                    \
+    if (e_ != cudaSuccess)                                                                      \
+      return ::tc::set_error((ctx), e_ == cudaErrorMemoryAllocation ? TC_ERR_OOM : TC_ERR_CUDA, \
+                             "%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+#define TC_CHECK_LAUNCH(ctx)                \
+  do {                                      \
+    (ctx)->launches++;                      \
+    TC_CHECK_CUDA((ctx), cudaGetLastError()); \
+  } while (0)
+
+#define TC_TRY(expr)                  \
+  do {                                \
+    tc_status s_ = (expr);            \
+    if (s_ != TC_OK) return s_;       \
+  } while (0)
+
+// Make sure the arena holds at least `bytes`; resets the bump pointer.
+tc_status arena_reserve(tc_ctx *ctx, size_t bytes);
+
+static inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Bump allocation inside a reserved arena (256-byte aligned).
+struct Bump {
+  char *base;
+  size_t cap, used = 0;
+  bool overflow = false;
+  template <typename T>
+  T *take(int64_t count) {
+    size_t bytes = align_up((size_t)(count > 0 ? count : 1) * sizeof(T), 256);
+    if (used + bytes > cap) { overflow = true; return nullptr; }
+    T *p = reinterpret_cast<T *>(base + used);
+    used += bytes;
+    return p;
+  }
+};
+
+// Size accounting twin of Bump (same rounding).
+struct Sizer {
+  size_t used = 0;
+  template <typename T>
+  void take(int64_t count) { used += align_up((size_t)(count > 0 ? count : 1) * sizeof(T), 256); }
+};
+
+// ---- device primitives ------------------------------------------------------
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(TC_FULL_MASK, v, o);
+  return v;
+}
+
+// Exclusive block scan of one value per thread (blockDim.x a multiple of 32,
+// at most 1024).  `tmp` is shared scratch of >= 32 entries.  Returns the
+// thread's exclusive prefix; *total receives the block sum.
+template <typename T>
+__device__ __forceinline__ T block_exclusive_scan(T v, T *tmp, T *total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  T x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    T y = __shfl_up_sync(TC_FULL_MASK, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) tmp[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    T w = lane < nw ? tmp[lane] : T(0);
+    T wx = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      T y = __shfl_up_sync(TC_FULL_MASK, wx, o);
+      if (lane >= o) wx += y;
+    }
+    if (lane < nw) tmp[lane] = wx - w;
+    if (lane == nw - 1) tmp[32] = wx;
+  }
+  __syncthreads();
+  T res = tmp[warp] + x - v;
+  *total = tmp[32];
+  __syncthreads();
+  return res;
+}
+
+// First row r with rowptr[r+1] > e (the row holding entry e), for a
+// monotone rowptr of n+1 entries and 0 <= e < rowptr[n].
+__device__ __forceinline__ int64_t row_of_entry(const int64_t *__restrict__ rowptr, int64_t n, int64_t e) {
+  int64_t lo = 0, hi = n;  // answer in [0, n)
+  while (hi - lo > 1) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (rowptr[mid] <= e) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+// Row of every entry of the tile [t0, t_end) of a CSR, into rows[0..t_end-t0)
+// (shared, TILE slots).  All threads of the block call it; ends synchronised.
+template <int TILE>
+__device__ void expand_rows(const int64_t *__restrict__ rowptr, int64_t n, int64_t t0, int64_t t_end,
+                            int *rows, int *scan_tmp) {
+  __shared__ int64_t s_first;
+  for (int i = threadIdx.x; i < TILE; i += blockDim.x) rows[i] = -1;
+  if (threadIdx.x == 0) s_first = row_of_entry(rowptr, n, t0);
+  __syncthreads();
+  const int64_t r0 = s_first;
+  if (threadIdx.x == 0) rows[0] = (int)r0;
+  for (int64_t r = r0 + 1 + threadIdx.x; r < n; r += blockDim.x) {
+    const int64_t s = rowptr[r];
+    if (s >= t_end) break;
+    if (s > t0) atomicMax(&rows[s - t0], (int)r);
+  }
+  __syncthreads();
+  // inclusive max-scan (row ids only grow): per-thread segment, then block.
+  constexpr int PER = TILE / 256;  // callers use 256 threads
+  int base = threadIdx.x * PER;
+  int m = -1;
+#pragma unroll
+  for (int k = 0; k < PER; ++k) m = max(m, rows[base + k]);
+  // exclusive max-scan of m across the block
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int x = m;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(TC_FULL_MASK, x, o);
+    if (lane >= o) x = max(x, y);
+  }
+  if (lane == 31) scan_tmp[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    int w = lane < (int)(blockDim.x >> 5) ? scan_tmp[lane] : -1;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(TC_FULL_MASK, w, o);
+      if (lane >= o) w = max(w, y);
+    }
+    scan_tmp[lane] = w;
+  }
+  __syncthreads();
+  int carry = warp > 0 ? scan_tmp[warp - 1] : -1;
+  int xin = __shfl_up_sync(TC_FULL_MASK, x, 1);
+  if (lane > 0) carry = max(carry, xin);
+#pragma unroll
+  for (int k = 0; k < PER; ++k) {
+    carry = max(carry, rows[base + k]);
+    rows[base + k] = carry;
+  }
+  __syncthreads();
+}
+
+// ---- host-side launch helpers shared by the .cu files --------------------------
+
+// Radix sort (radix_sort.cu): stable LSD sort of uint64 keys on bits
+// [0, bits), optional uint32 payload.  k0/v0 hold the input; k1/v1 are
+// same-sized scratch.  On return *kres / *vres point at the sorted data.
+size_t radix_sort_scratch_bytes(const tc_ctx *ctx, int64_t N);
+tc_status radix_sort(tc_ctx *ctx, uint64_t *k0, uint64_t *k1, uint32_t *v0, uint32_t *v1, int64_t N, int bits,
+                     void *scratch, uint64_t **kres, uint32_t **vres);
+
+// Exclusive scan of int64 values (scan.cu helpers in radix_sort.cu).
+size_t scan_scratch_bytes(const tc_ctx *ctx, int64_t N);
+tc_status exclusive_scan_i64(tc_ctx *ctx, const int64_t *in, int64_t *out, int64_t N, void *scratch,
+                             int64_t *d_total_out);
+
+int grid_for(const tc_ctx *ctx, int64_t items, int per_block, int blocks_per_sm);
+
+}  // namespace tc

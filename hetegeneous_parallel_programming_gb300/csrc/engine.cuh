@@ -1,0 +1,108 @@
+// Engine-internal interfaces between orient.cu, count.cu, mlp.cu and capi.cu.
+#pragma once
+#include "dev_common.cuh"
+
+namespace tc {
+
+constexpr int TILE_EDGES = TC_DEFAULT_TILE_EDGES;   // selector granularity
+constexpr int ENTRY_TILE = 2048;                    // orientation tile (entries)
+
+// Validation flag bits (ctx->d_flags[0]).
+enum : unsigned {
+  VF_ROWPTR_ENDS = 1u,     // rowptr[0] != 0 or rowptr[n] != nnz
+  VF_ROWPTR_ORDER = 2u,    // rowptr not monotone
+  VF_ID_RANGE = 4u,        // column id outside [0, n)
+  VF_SELF_LOOP = 8u,
+  VF_UNSORTED = 16u,       // row not strictly ascending (or duplicate)
+  VF_TIMEOUT = 32u         // a bounded device wait gave up
+};
+
+// A CSR resident on the device.
+struct DevCSR {
+  int64_t n = 0, nnz = 0;
+  const int64_t *rowptr = nullptr;
+  const int32_t *col = nullptr;
+};
+
+// An oriented graph ready for counting.  For the relabelled DAG of tc_count
+// (restrict_after = 1) every edge r->s has s > r and rows are sorted, so only
+// the part of N+(r) after s can meet N+(s).
+struct DevDag {
+  int64_t n = 0, m = 0;
+  const int64_t *rowptr = nullptr;   // [n+1]
+  const int32_t *col = nullptr;      // [m]
+  const int32_t *src = nullptr;      // [m] row of each edge
+  const uint32_t *perm = nullptr;    // [m] output slot of each edge (null: identity)
+  int restrict_after = 0;
+};
+
+// Validation: sets VF_* bits in ctx->d_flags[0].
+tc_status launch_validate(tc_ctx *ctx, const DevCSR &g, bool require_sorted_simple);
+
+// Orientation.  Phase A (before the host learns m): degree keys, rank sort,
+// kept counts per row and per block.  Phase B: compaction + relabel sort.
+struct OrientBufs {
+  // phase A
+  uint64_t *vkeys0, *vkeys1;   // [n]
+  int32_t *rank;               // [n]
+  int64_t *kept;               // [n+1] kept out-degree per original row
+  int64_t *bcount;             // [G+1] kept per block chunk
+  int64_t *d_m;                // [1]
+  void *sort_scratch;          // radix + scan scratch
+  // phase B
+  uint64_t *ekeys0, *ekeys1;   // [m]
+  uint32_t *evals0, *evals1;   // [m] (optional)
+  int64_t *nrowptr;            // [n+1]
+  int64_t *dnew;               // [n+1]
+  int32_t *ncol, *nsrc;        // [m]
+  int32_t *dag_col;            // optional original-id DAG output [m]
+  int G;                       // blocks of the entry-chunk kernels
+  int64_t chunk;
+  // optional vertex groups (batched graphs): ranks sort by (group, degree,
+  // id), so every group owns the contiguous rank range of its vertices.
+  const int32_t *vgroup = nullptr;
+  int group_bits = 0;
+};
+void orient_geometry(const tc_ctx *ctx, int64_t nnz, int *G, int64_t *chunk);
+tc_status orient_phase_a(tc_ctx *ctx, const DevCSR &g, OrientBufs &b);
+tc_status orient_phase_b(tc_ctx *ctx, const DevCSR &g, OrientBufs &b, int64_t m, bool want_perm,
+                         bool want_dag_cols, DevDag *out);
+
+// Row of every entry of a CSR (for counting a caller-oriented DAG).
+tc_status launch_expand_src(tc_ctx *ctx, const int64_t *rowptr, int64_t n, int64_t m, int32_t *src);
+
+// Counting.
+struct CountBufs {
+  float *features;        // [T][TC_MLP_FEATURES]
+  uint64_t *qkeys0, *qkeys1;  // [T]
+  uint32_t *qvals0, *qvals1;  // [T]
+  int32_t *arm;           // [T]
+  int64_t *qoff;          // [TC_NUM_ARMS+1]
+  unsigned long long *tile_cycles;  // [T] (optional)
+  unsigned long long *tile_bytes;   // [T] algorithmic bytes per tile
+  unsigned long long *arm_bytes;    // [TC_NUM_ARMS]
+  void *sort_scratch;
+};
+size_t count_scratch_bytes(const tc_ctx *ctx, int64_t m);
+tc_status count_carve(const tc_ctx *ctx, int64_t m, Bump &bump, CountBufs &cb, bool want_cycles);
+// Enqueues plan, queue build and every arm kernel on the ctx stream (no host
+// sync, so it can be captured into a CUDA graph); adds the count into
+// ctx->d_total (which the caller zeroes) and writes per-edge counts to
+// out[perm[e]] when out is set.  The queue offsets land in pinned host
+// memory; count_stats reads them (and the timing events) after a sync.
+tc_status run_count(tc_ctx *ctx, const DevDag &dag, const tc_opts &opts, CountBufs &cb, uint32_t *out, bool timing);
+void count_stats(tc_ctx *ctx, tc_stats *st, bool timing);
+
+// Shared by the entry points (capi.cu, batch.cu).
+tc_status stage_csr(tc_ctx *ctx, const tc_csr *g, Bump &bump, DevCSR &d, uint64_t *h2d);
+void orient_sizes(const tc_ctx *ctx, int64_t n, int64_t nnz, bool perm, bool dagcol, Sizer &sz);
+void orient_carve(const tc_ctx *ctx, int64_t n, int64_t nnz, bool perm, bool dagcol, Bump &bump, OrientBufs &b);
+tc_status orient_front(tc_ctx *ctx, const DevCSR &d, const tc_opts &o, OrientBufs &ob, int64_t *m, float *ms_validate,
+                       float *ms_a);
+float elapsed(cudaEvent_t a, cudaEvent_t b);
+const char *flag_text(unsigned f);
+tc_status init_arm_occupancy(tc_ctx *ctx);
+
+// Learned selector inference parameters live in ctx->d_mlp (fp32 master
+// copy); the plan kernel rounds them to bf16 when it stages them.
+}  // namespace tc

@@ -1,0 +1,271 @@
+/*
+ * tc.h — C ABI of the GB300 exact triangle-counting engine.
+ *
+ * Every entry point takes plain pointers and sizes, returns a tc_status and
+ * never exits the process.  Graphs use the GraphMiner CSR layout of the
+ * reference project: int64 row pointers (eidType) of length n+1 and int32
+ * column indices (vidType); counts are uint64 (AccType).
+ *
+ * Reference interfaces replaced (paths are inside the reference project):
+ *   - TCSolver(Graph&, uint64_t&, int, int)    multigpu.cu:780,
+ *       successful_push_pull/multigpu_nvshmem_pushpull.cu:29 (declared main.cc:5)
+ *       -> tc_count_dag (count an oriented graph, the TCSolver contract) and
+ *          tc_count (orientation + count on the device in one call).
+ *   - Graph::orientation()                      successful_push_pull/graph.cc:252-298
+ *       -> tc_orient (same kept-edge rule, same neighbour order, on the GPU).
+ *   - Graph::Graph(prefix, ...) file loading    successful_push_pull/graph.cc:4-55
+ *       -> tc_load_graphminer / tc_save_graphminer / tc_csr_free.
+ *   - GraphGPU::init (H2D copy)                 successful_push_pull/graph_gpu.h:84-137
+ *       -> folded into tc_count / tc_count_dag when tc_csr.on_device == 0.
+ *   - warp_vertex kernel + intersect_num        bs_warp_vertex.cuh:2-35
+ *       -> the strategy kernels behind tc_count / tc_count_dag.
+ *
+ * Threading: a tc_ctx owns one CUDA stream and a grow-only device arena; it
+ * is not thread-safe (use one ctx per host thread).  Results are bit-exact
+ * and independent of the strategy selected for each tile.
+ */
+#ifndef TC_H_
+#define TC_H_
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum tc_status {
+  TC_OK = 0,
+  TC_ERR_INVALID_ARG = 1,    /* null pointer, bad size, bad option            */
+  TC_ERR_INVALID_GRAPH = 2,  /* non-monotone rowptr, id out of range, unsorted */
+  TC_ERR_CUDA = 3,           /* a CUDA runtime call failed                     */
+  TC_ERR_OOM = 4,            /* device or host allocation failed               */
+  TC_ERR_IO = 5,             /* file missing, truncated or malformed           */
+  TC_ERR_TIMEOUT = 6,        /* a bounded device-side wait gave up             */
+  TC_ERR_UNSUPPORTED = 7,    /* size beyond the engine's index limits          */
+  TC_ERR_NO_DEVICE = 8       /* no CUDA device is visible                      */
+} tc_status;
+
+/* Compressed sparse rows.  For tc_count / tc_orient the graph is the
+ * symmetric adjacency of a simple undirected graph (each row sorted strictly
+ * ascending, no self loops), i.e. what Graph::Graph loads.  For tc_count_dag
+ * it is an oriented graph with sorted rows (what Graph::orientation leaves). */
+typedef struct tc_csr {
+  int64_t n;               /* vertices                                        */
+  int64_t nnz;             /* column entries (2m for a symmetric graph)       */
+  const int64_t *rowptr;   /* [n+1], rowptr[0] == 0, rowptr[n] == nnz         */
+  const int32_t *colidx;   /* [nnz]                                           */
+  int32_t on_device;       /* 1: device pointers; 0: host pointers            */
+} tc_csr;
+
+/* Intersection strategies ("arms") a 4096-edge tile can be run with.  Every
+ * arm is exact; they differ only in speed. */
+typedef enum tc_arm {
+  TC_ARM_BSEARCH_4 = 0,    /* 4 lanes per edge, binary search short->long     */
+  TC_ARM_BSEARCH_8 = 1,    /* 8 lanes per edge                                */
+  TC_ARM_BSEARCH_32 = 2,   /* one warp per edge                               */
+  TC_ARM_MERGE_8 = 3,      /* 8-lane windowed merge-path                      */
+  TC_ARM_MERGE_32 = 4,     /* 32-lane windowed merge-path                     */
+  TC_ARM_BITMAP = 5,       /* block bitmap of the row + popcount probes       */
+  TC_NUM_ARMS = 6
+} tc_arm;
+
+typedef enum tc_selector {
+  TC_SELECT_FIXED = 0,     /* degree-threshold selector (fallback and judge)  */
+  TC_SELECT_LEARNED = 1,   /* MLP cost model loaded into the ctx              */
+  TC_SELECT_FORCE = 2      /* every tile uses opts.force_arm                  */
+} tc_selector;
+
+#define TC_DEFAULT_TILE_EDGES 4096
+
+typedef struct tc_opts {
+  int32_t selector;          /* tc_selector                                    */
+  int32_t force_arm;         /* arm for TC_SELECT_FORCE                        */
+  int32_t record_tile_costs; /* 1: record per-tile SM-cycle cost (training)    */
+  int32_t validate;          /* 1 (default): check ids/rowptr/sortedness       */
+} tc_opts;
+
+/* Per-call timings (device milliseconds from CUDA events on the ctx stream)
+ * and plan statistics. */
+typedef struct tc_stats {
+  float ms_h2d, ms_validate, ms_orient, ms_plan, ms_count, ms_scatter, ms_d2h, ms_total;
+  int64_t m;                       /* oriented edges                          */
+  int64_t tiles;                   /* 4096-edge tiles                         */
+  int64_t tiles_per_arm[TC_NUM_ARMS];
+  int64_t kernel_launches;         /* engine kernels launched by the call     */
+  uint64_t h2d_bytes, d2h_bytes;
+  float ms_arm[TC_NUM_ARMS];       /* device time of each arm's kernel        */
+  /* Algorithmic bytes of each arm's tiles: sum over its edges u->v of
+   * 4*(d+(u) + d+(v)) + 4 (both out-lists read once, as in a merge, plus the
+   * edge itself); alg_bytes adds 8*(n+1) for the row pointers. */
+  uint64_t alg_bytes_arm[TC_NUM_ARMS];
+  uint64_t alg_bytes;
+} tc_stats;
+
+/* ---- context ---------------------------------------------------------- */
+typedef struct tc_ctx tc_ctx;
+
+tc_status tc_ctx_create(int device, tc_ctx **out);
+void tc_ctx_destroy(tc_ctx *ctx);
+/* Last error text of the ctx (or of the library when ctx is NULL). */
+const char *tc_last_error(const tc_ctx *ctx);
+const char *tc_status_str(tc_status s);
+void tc_opts_default(tc_opts *o);
+/* Device arena bytes currently reserved by the ctx. */
+int64_t tc_ctx_arena_bytes(const tc_ctx *ctx);
+/* Block until the ctx stream is idle. */
+tc_status tc_ctx_sync(tc_ctx *ctx);
+/* The ctx's CUDA stream (a cudaStream_t), for callers that time the engine
+ * with their own events on the stream it launches on. */
+void *tc_ctx_stream(tc_ctx *ctx);
+
+/* ---- hot path --------------------------------------------------------- */
+
+/* Orientation of a symmetric graph: keep u->v iff deg(v) > deg(u) or
+ * (deg(v) == deg(u) and v > u), neighbours in input order (graph.cc:252-298).
+ * dag_rowptr [n+1] and dag_colidx [capacity] receive the original-id DAG, in
+ * the memory kind of g->on_device.  *m_out = number of oriented edges. */
+tc_status tc_orient(tc_ctx *ctx, const tc_csr *g, int64_t *dag_rowptr, int32_t *dag_colidx,
+                    int64_t dag_capacity, int64_t *m_out);
+
+/* Orient on the device (rank by (degree, id), relabel, compact) and count
+ * triangles.  *total is overwritten.  edge_counts (optional, capacity
+ * edge_capacity) receives |N+(u) n N+(v)| for every oriented edge in the
+ * order tc_orient produces; memory kind follows g->on_device. */
+tc_status tc_count(tc_ctx *ctx, const tc_csr *g, const tc_opts *opts, uint64_t *total,
+                   uint32_t *edge_counts, int64_t edge_capacity, tc_stats *stats);
+
+/* Count triangles of an already oriented graph (rows sorted ascending), the
+ * contract of the reference TCSolver on a USE_DAG graph: the sum over every
+ * edge u->v of |N+(u) n N+(v)|.  edge_counts follows the input edge order. */
+tc_status tc_count_dag(tc_ctx *ctx, const tc_csr *dag, const tc_opts *opts, uint64_t *total,
+                       uint32_t *edge_counts, int64_t edge_capacity, tc_stats *stats);
+
+/* ---- batched path ------------------------------------------------------ */
+
+/* A batch of graphs, each a symmetric CSR with local ids, concatenated:
+ * graph g owns vertices [vtx_off[g], vtx_off[g+1]) and entries
+ * [rowptr[vtx_off[g]], rowptr[vtx_off[g+1]]) of one global rowptr whose
+ * values are global entry offsets; colidx values are LOCAL ids. */
+typedef struct tc_batch {
+  int64_t num_graphs;
+  const int64_t *vtx_off;   /* [num_graphs+1]                                  */
+  const int64_t *rowptr;    /* [vtx_off[num_graphs]+1]                         */
+  const int32_t *colidx;    /* [rowptr[last]]                                  */
+  int32_t on_device;
+} tc_batch;
+
+/* Count every graph of the batch in one pass of the engine over the batch's
+ * disjoint union (one persistent launch per arm over (graph, tile) items).
+ * totals [num_graphs] receives each graph's exact count (host memory). */
+tc_status tc_batch_count(tc_ctx *ctx, const tc_batch *b, const tc_opts *opts, uint64_t *totals,
+                         tc_stats *stats);
+
+/* ---- learned selector -------------------------------------------------- */
+
+#define TC_MLP_FEATURES 16
+#define TC_MLP_HIDDEN 64
+
+/* Per-tile features and per-arm costs of a graph, for training.  features is
+ * [tiles][TC_MLP_FEATURES] float, costs is [tiles][TC_NUM_ARMS] float
+ * (SM-cycles); both host memory with room for `capacity` tiles. */
+tc_status tc_tile_profile(tc_ctx *ctx, const tc_csr *g, float *features, float *costs,
+                          int64_t capacity, int64_t *tiles_out);
+
+/* The arm the selector of `opts` picks for every tile of a graph (host
+ * int32 array with room for `capacity` tiles). */
+tc_status tc_plan_arms(tc_ctx *ctx, const tc_csr *g, const tc_opts *opts, int32_t *arms, int64_t capacity,
+                       int64_t *tiles_out);
+
+/* Train the MLP cost model on the device (forward/backward/Adam kernels of
+ * this library) from host arrays of features and costs; the trained weights
+ * stay loaded in the ctx.  loss_out (optional) receives the final loss. */
+tc_status tc_selector_train(tc_ctx *ctx, const float *features, const float *costs,
+                            int64_t tiles, int32_t epochs, float lr, uint64_t seed,
+                            float *loss_out);
+/* Weights as a flat float blob (TC_MLP_PARAM_COUNT floats). */
+#define TC_MLP_PARAM_COUNT (TC_MLP_FEATURES * TC_MLP_HIDDEN + TC_MLP_HIDDEN + \
+                            TC_MLP_HIDDEN * TC_MLP_HIDDEN + TC_MLP_HIDDEN +   \
+                            TC_MLP_HIDDEN * TC_NUM_ARMS + TC_NUM_ARMS)
+tc_status tc_selector_set_weights(tc_ctx *ctx, const float *params, int64_t count);
+tc_status tc_selector_get_weights(tc_ctx *ctx, float *params, int64_t count);
+/* Predicted per-arm costs for host feature rows (inference kernel). */
+tc_status tc_selector_predict(tc_ctx *ctx, const float *features, int64_t rows, float *pred);
+/* One forward+backward pass on a host mini-batch: loss and parameter
+ * gradients (for checking against a CPU restatement). */
+tc_status tc_selector_grad(tc_ctx *ctx, const float *params, const float *features,
+                           const float *costs, int64_t rows, float *loss, float *grad);
+
+/* ---- graph construction, generators and files --------------------------- */
+
+/* Symmetrise + drop self loops + dedup an edge list into a sorted symmetric
+ * CSR on the device.  src/dst host or device per on_device; rowptr [n+1] and
+ * colidx [capacity] are outputs in the same memory kind. */
+tc_status tc_csr_from_edges(tc_ctx *ctx, int64_t n, int64_t num_edges, const int32_t *src,
+                            const int32_t *dst, int32_t on_device, int64_t *rowptr,
+                            int32_t *colidx, int64_t capacity, int64_t *nnz_out);
+
+/* Seeded generators (counter-based RNG, identical on host and device). */
+typedef enum tc_gen_kind { TC_GEN_ER = 0, TC_GEN_RMAT = 1, TC_GEN_RGG = 2, TC_GEN_CHUNG_LU = 3 } tc_gen_kind;
+typedef struct tc_gen_params {
+  int32_t kind;            /* tc_gen_kind                                     */
+  int64_t n;               /* vertices (RMAT: ignored, n = 2^scale)           */
+  int32_t scale;           /* RMAT scale                                      */
+  double avg_degree;       /* ER / RGG / Chung-Lu target average degree       */
+  double edge_factor;      /* RMAT edges per vertex                           */
+  double a, b, c;          /* RMAT quadrant probabilities (d = 1-a-b-c)       */
+  double gamma;            /* Chung-Lu degree exponent                        */
+  uint64_t seed;
+} tc_gen_params;
+
+/* Number of edge samples the generator draws (RGG: an upper bound). */
+int64_t tc_gen_num_samples(const tc_gen_params *p);
+/* Vertex count of the generated graph. */
+int64_t tc_gen_num_vertices(const tc_gen_params *p);
+/* Draw edge samples on the host (OpenMP).  *count_out = samples written. */
+tc_status tc_gen_edges_host(const tc_gen_params *p, int32_t *src, int32_t *dst, int64_t capacity,
+                            int64_t *count_out);
+/* Same samples drawn by a device kernel into device buffers (ER, RMAT, CL). */
+tc_status tc_gen_edges_device(tc_ctx *ctx, const tc_gen_params *p, int32_t *src, int32_t *dst,
+                              int64_t capacity, int64_t *count_out);
+/* A seeded batch of small graphs of mixed families for tc_batch_count:
+ * graph g draws n log-uniform in [n_min, n_max] and an average degree
+ * uniform in [deg_min, deg_max]; families cycle Erdos-Renyi, R-MAT
+ * (a, b, c; n rounded to the nearest power of two) and random geometric.
+ * Built in parallel over graphs (OpenMP).  vtx_off [num_graphs+1] is caller
+ * memory; rowptr/colidx are malloc'd (tc_csr_free). */
+typedef struct tc_batch_spec {
+  int64_t num_graphs;
+  int64_t n_min, n_max;
+  double deg_min, deg_max;
+  double a, b, c;
+  uint64_t seed;
+} tc_batch_spec;
+tc_status tc_gen_batch_host(const tc_batch_spec *spec, int64_t *vtx_off, int64_t **rowptr_out,
+                            int32_t **colidx_out, int64_t *nnz_out);
+/* Host symmetric CSR builder (sort + unique), the host twin of
+ * tc_csr_from_edges, for callers without a device. */
+tc_status tc_csr_from_edges_host(int64_t n, int64_t num_edges, const int32_t *src,
+                                 const int32_t *dst, int64_t **rowptr_out, int32_t **colidx_out,
+                                 int64_t *nnz_out);
+
+/* GraphMiner on-disk format (graph.cc:31-55): prefix.meta.txt with
+ * "n nnz vid_size eid_size vlabel_size elabel_size max_degree feat_len
+ * num_vertex_classes num_edge_classes", prefix.vertex.bin int64[n+1],
+ * prefix.edge.bin int32[nnz].  Loaded arrays are malloc'd host memory
+ * released with tc_csr_free. */
+tc_status tc_load_graphminer(const char *prefix, int64_t *n, int64_t *nnz, int64_t **rowptr,
+                             int32_t **colidx, int64_t *max_degree);
+tc_status tc_save_graphminer(const char *prefix, int64_t n, int64_t nnz, const int64_t *rowptr,
+                             const int32_t *colidx);
+void tc_csr_free(int64_t *rowptr, int32_t *colidx);
+
+/* Host CSR checks: rowptr monotone, ids in range, rows strictly ascending,
+ * no self loops (the contract of tc_count). */
+tc_status tc_check_csr_host(int64_t n, int64_t nnz, const int64_t *rowptr, const int32_t *colidx,
+                            int32_t require_sorted_simple);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TC_H_ */

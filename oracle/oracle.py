@@ -1,0 +1,153 @@
+"""CPU oracle loader — TEST INFRASTRUCTURE ONLY.
+
+Imported by tests/, by __graft_entry__.smoke() and by bench.py's CPU-baseline
+leg, always as the checker (or as the timed CPU reference); the engine never
+imports it.  Wraps oracle/_build/libtc_oracle.so (tc_oracle.c, a plain C +
+OpenMP restatement of the reference CPU path) and adds pure-Python helpers
+for tiny graphs.
+
+Parity status: "parity unpinned" against the reference binary (its device
+intersection lives in the un-vendored GraphMiner tree and it ships no golden
+counts); pinned instead to networkx, analytic answers and brute force via
+the fixtures in tests/golden/.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import itertools
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+SO = HERE / "_build" / "libtc_oracle.so"
+_lib = None
+
+
+def build() -> Path:
+    subprocess.run(["bash", str(HERE / "build_oracle.sh")], check=True)
+    return SO
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not SO.exists() or SO.stat().st_mtime < (HERE / "tc_oracle.c").stat().st_mtime:
+            build()
+        h = C.CDLL(str(SO))
+        P, I64 = C.c_void_p, C.c_int64
+        h.oracle_orient.restype = I64
+        h.oracle_orient.argtypes = [I64, P, P, P, P]
+        h.oracle_count.restype = C.c_uint64
+        h.oracle_count.argtypes = [I64, P, P, P]
+        h.oracle_count_rows.restype = C.c_uint64
+        h.oracle_count_rows.argtypes = [I64, P, P, I64, I64, I64, P]
+        h.oracle_orient_rows_cost.restype = I64
+        h.oracle_orient_rows_cost.argtypes = [I64, P, P, I64]
+        h.oracle_sort_neighbors.restype = None
+        h.oracle_sort_neighbors.argtypes = [I64, P, P]
+        h.oracle_csr_from_edges.restype = I64
+        h.oracle_csr_from_edges.argtypes = [I64, I64, P, P, P, P]
+        h.oracle_batch_count.restype = None
+        h.oracle_batch_count.argtypes = [I64, P, P, P, P]
+        h.oracle_max_threads.restype = C.c_int
+        h.oracle_set_threads.argtypes = [C.c_int]
+        _lib = h
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def orient(rowptr, colidx):
+    """graph.cc:252-298 -> (dag_rowptr, dag_colidx)."""
+    rowptr = np.ascontiguousarray(rowptr, np.int64)
+    colidx = np.ascontiguousarray(colidx, np.int32)
+    n = len(rowptr) - 1
+    orow = np.empty(n + 1, np.int64)
+    ocol = np.empty(max(len(colidx), 1), np.int32)
+    m = lib().oracle_orient(n, _p(rowptr), _p(colidx), _p(orow), _p(ocol))
+    return orow, ocol[:m].copy()
+
+
+def count(dag_rowptr, dag_colidx, per_edge: bool = False):
+    """bs_warp_vertex.cuh:13-21 with the merge of graph.cc:376-391 -> (total, per-edge or None)."""
+    dag_rowptr = np.ascontiguousarray(dag_rowptr, np.int64)
+    dag_colidx = np.ascontiguousarray(dag_colidx, np.int32)
+    n = len(dag_rowptr) - 1
+    out = np.zeros(max(len(dag_colidx), 1), np.uint32) if per_edge else None
+    t = lib().oracle_count(n, _p(dag_rowptr), _p(dag_colidx), _p(out) if per_edge else None)
+    return int(t), (out[:len(dag_colidx)] if per_edge else None)
+
+
+def count_sample(dag_rowptr, dag_colidx, row_step: int):
+    """Counting restricted to rows 0, row_step, 2*row_step, ... (bounded CPU baseline)."""
+    n = len(dag_rowptr) - 1
+    return int(lib().oracle_count_rows(n, _p(dag_rowptr), _p(dag_colidx), 0, n, int(row_step), None))
+
+
+def orient_sample_cost(rowptr, colidx, row_step: int) -> int:
+    n = len(rowptr) - 1
+    return int(lib().oracle_orient_rows_cost(n, _p(rowptr), _p(colidx), int(row_step)))
+
+
+def triangles(rowptr, colidx, per_edge: bool = False):
+    """Full CPU path: orient then count."""
+    orow, ocol = orient(rowptr, colidx)
+    t, pe = count(orow, ocol, per_edge)
+    return (t, pe, orow, ocol) if per_edge else t
+
+
+def csr_from_edges(n: int, src, dst):
+    src = np.ascontiguousarray(src, np.int32)
+    dst = np.ascontiguousarray(dst, np.int32)
+    rowptr = np.empty(n + 1, np.int64)
+    colidx = np.empty(max(2 * len(src), 1), np.int32)
+    nnz = lib().oracle_csr_from_edges(n, len(src), _p(src), _p(dst), _p(rowptr), _p(colidx))
+    if nnz < 0:
+        raise ValueError("bad edge list")
+    return rowptr, colidx[:nnz].copy()
+
+
+def batch_count(vtx_off, rowptr, colidx):
+    vtx_off = np.ascontiguousarray(vtx_off, np.int64)
+    rowptr = np.ascontiguousarray(rowptr, np.int64)
+    colidx = np.ascontiguousarray(colidx, np.int32)
+    out = np.zeros(len(vtx_off) - 1, np.uint64)
+    lib().oracle_batch_count(len(vtx_off) - 1, _p(vtx_off), _p(rowptr), _p(colidx), _p(out))
+    return out
+
+
+def max_threads() -> int:
+    return int(lib().oracle_max_threads())
+
+
+def set_threads(t: int) -> None:
+    lib().oracle_set_threads(int(t))
+
+
+# ---- pure Python, tiny graphs -----------------------------------------------------------
+
+def brute_force_triangles(n: int, edges) -> int:
+    """Enumerate vertex triples (graphs of a few dozen vertices at most)."""
+    adj = [set() for _ in range(n)]
+    for u, v in edges:
+        if u != v:
+            adj[u].add(v)
+            adj[v].add(u)
+    return sum(1 for a, b, c in itertools.combinations(range(n), 3) if b in adj[a] and c in adj[a] and c in adj[b])
+
+
+def py_orient_count(rowptr, colidx):
+    """Independent pure-Python statement of orientation + per-edge counts."""
+    n = len(rowptr) - 1
+    deg = [int(rowptr[v + 1] - rowptr[v]) for v in range(n)]
+    out_rows = []
+    for u in range(n):
+        out_rows.append([int(v) for v in colidx[rowptr[u]:rowptr[u + 1]]
+                         if deg[v] > deg[u] or (deg[v] == deg[u] and v > u)])
+    sets = [set(r) for r in out_rows]
+    per = [len(sets[u] & sets[v]) for u in range(n) for v in out_rows[u]]
+    return sum(per), per, out_rows

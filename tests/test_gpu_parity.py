@@ -1,0 +1,187 @@
+"""GPU parity: the engine (through the C ABI) against the CPU oracle and the
+golden vectors.  Integer results must be bit-exact."""
+import numpy as np
+import pytest
+
+import hetegeneous_parallel_programming_gb300 as tc
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+ARMS = list(range(tc.TC_NUM_ARMS))
+
+
+def csr_of(case):
+    e = np.array(case["edges"], np.int64).reshape(-1, 2)
+    return oracle.csr_from_edges(case["n"], e[:, 0], e[:, 1])
+
+
+def gen_csr(spec):
+    n, s, d = tc.gen_edges_host(spec)
+    return oracle.csr_from_edges(n, s, d)
+
+
+def test_golden_cases_every_arm(engine, golden):
+    for case in golden:
+        rowptr, colidx = csr_of(case)
+        for arm in [None] + ARMS:
+            total, per_edge, st = engine.count(rowptr, colidx, force_arm=arm, edge_counts=True)
+            assert total == case["triangles"], (case["name"], arm)
+            assert per_edge.tolist() == case["oriented_per_edge"], (case["name"], arm)
+
+
+def test_orientation_matches_reference_rule(engine, golden):
+    for case in golden:
+        rowptr, colidx = csr_of(case)
+        drow, dcol = engine.orient(rowptr, colidx)
+        orow, ocol = oracle.orient(rowptr, colidx)
+        assert np.array_equal(drow, orow) and np.array_equal(dcol, ocol), case["name"]
+
+
+def test_count_dag_matches_reference_solver(engine, golden):
+    for case in golden:
+        rowptr, colidx = csr_of(case)
+        orow, ocol = oracle.orient(rowptr, colidx)
+        for arm in [None, 0, 3, 5]:
+            total, per_edge, _ = engine.count_dag(orow, ocol, force_arm=arm, edge_counts=True)
+            ref, ref_pe = oracle.count(orow, ocol, per_edge=True)
+            assert total == ref == case["triangles"]
+            assert np.array_equal(per_edge, ref_pe)
+
+
+@pytest.mark.parametrize("spec", [
+    tc.GenSpec("er", n=16384, avg_degree=16, seed=0),          # the plain-small workload
+    tc.GenSpec("er", n=16384, avg_degree=16, seed=7),
+    tc.GenSpec("rmat", scale=14, edge_factor=16, seed=0),
+    tc.GenSpec("rmat", scale=16, edge_factor=16, seed=1),
+    tc.GenSpec("rmat", scale=16, edge_factor=16, a=0.45, b=0.25, c=0.15, seed=2),
+    tc.GenSpec("chung_lu", n=50000, avg_degree=24, gamma=2.1, seed=3),
+    tc.GenSpec("rgg", n=8000, avg_degree=40, seed=4),
+])
+def test_seeded_graphs_bit_exact(engine, spec):
+    rowptr, colidx = gen_csr(spec)
+    ref_total, ref_pe, orow, ocol = oracle.triangles(rowptr, colidx, per_edge=True)
+    for sel, arm in [("fixed", None)] + [("force", a) for a in ARMS]:
+        total, per_edge, st = engine.count(rowptr, colidx, selector=sel, force_arm=arm, edge_counts=True)
+        assert total == ref_total, (spec, sel, arm)
+        assert np.array_equal(per_edge, ref_pe), (spec, sel, arm)
+        assert st["m"] == len(ocol)
+    total, _, _ = engine.count(rowptr, colidx)
+    assert total == ref_total
+
+
+def test_device_generators_match_host(engine):
+    import torch
+    for spec in [tc.GenSpec("er", n=100000, avg_degree=8, seed=11),
+                 tc.GenSpec("rmat", scale=15, edge_factor=8, seed=12),
+                 tc.GenSpec("chung_lu", n=60000, avg_degree=12, seed=13)]:
+        n, hs, hd = tc.gen_edges_host(spec)
+        M = spec.num_samples
+        ds = torch.empty(M, dtype=torch.int32, device="cuda")
+        dd = torch.empty(M, dtype=torch.int32, device="cuda")
+        torch.cuda.synchronize()
+        cnt = engine.gen_edges_device(spec, ds.data_ptr(), dd.data_ptr(), M)
+        assert cnt == M == len(hs)
+        assert np.array_equal(ds.cpu().numpy(), hs) and np.array_equal(dd.cpu().numpy(), hd), spec
+
+
+def test_device_csr_builder_matches_oracle(engine):
+    for spec in [tc.GenSpec("rmat", scale=14, edge_factor=16, seed=5), tc.GenSpec("er", n=3000, avg_degree=30, seed=6)]:
+        n, s, d = tc.gen_edges_host(spec)
+        r1, c1 = engine.csr_from_edges(n, s, d)
+        r2, c2 = oracle.csr_from_edges(n, s, d)
+        assert np.array_equal(r1, r2) and np.array_equal(c1, c2)
+
+
+def test_device_pointers_path(engine):
+    import torch
+    rowptr, colidx = gen_csr(tc.GenSpec("rmat", scale=13, edge_factor=16, seed=3))
+    ref, ref_pe, _, _ = oracle.triangles(rowptr, colidx, per_edge=True)
+    r = torch.from_numpy(rowptr).cuda()
+    c = torch.from_numpy(colidx).cuda()
+    out = torch.zeros(len(colidx) // 2, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    total, st = engine.count_device(len(rowptr) - 1, len(colidx), r.data_ptr(), c.data_ptr(),
+                                    edge_counts_ptr=out.data_ptr(), edge_capacity=out.numel())
+    assert total == ref
+    assert np.array_equal(out.cpu().numpy().view(np.uint32), ref_pe)
+
+
+def test_batch_matches_per_graph(engine):
+    rng = np.random.default_rng(5)
+    graphs = []
+    for i in range(120):
+        kind = ["er", "rmat", "rgg"][i % 3]
+        n = int(np.exp(rng.uniform(np.log(16), np.log(2000))))
+        deg = float(rng.uniform(2, 40))
+        if kind == "rmat":
+            spec = tc.GenSpec("rmat", scale=max(4, int(np.log2(n))), edge_factor=deg / 2, seed=i)
+        else:
+            spec = tc.GenSpec(kind, n=n, avg_degree=deg, seed=i)
+        graphs.append(gen_csr(spec))
+    graphs.append(oracle.csr_from_edges(1, np.zeros(0, np.int32), np.zeros(0, np.int32)))  # isolated vertex
+    vtx_off = np.cumsum([0] + [len(r) - 1 for r, _ in graphs]).astype(np.int64)
+    rows, cols, base = [np.zeros(1, np.int64)], [], 0
+    for r, c in graphs:
+        rows.append(r[1:] + base)
+        cols.append(c)
+        base += len(c)
+    rowptr, colidx = np.concatenate(rows), np.concatenate(cols)
+    ref = oracle.batch_count(vtx_off, rowptr, colidx)
+    for arm in [None, 0, 2, 4, 5]:
+        totals, st = engine.batch_count(vtx_off, rowptr, colidx, force_arm=arm)
+        assert np.array_equal(totals, ref), arm
+    # replay of the captured graph gives the same answer
+    totals, _ = engine.batch_count(vtx_off, rowptr, colidx)
+    totals2, _ = engine.batch_count(vtx_off, rowptr, colidx)
+    assert np.array_equal(totals, ref) and np.array_equal(totals2, ref)
+
+
+@pytest.mark.parametrize("rowptr,colidx", [
+    ([0, 2, 1, 3], [1, 2, 0]),          # rowptr not monotone
+    ([0, 1, 2, 2], [1, 3]),             # id out of range
+    ([0, 2, 3, 3], [2, 1, 0]),          # row not ascending
+    ([0, 1, 2, 2], [0, 0]),             # self loop
+    ([0, 2, 2, 2], [1, 1]),             # duplicate neighbour
+    ([0, 1, 2, 5], [1, 0]),             # rowptr[n] != nnz
+])
+def test_invalid_graphs_rejected(engine, rowptr, colidx):
+    with pytest.raises(tc.TCError) as ei:
+        engine.count(np.array(rowptr), np.array(colidx))
+    assert ei.value.status == 2
+    # the ctx stays usable
+    total, _, _ = engine.count(np.array([0, 2, 4, 6]), np.array([1, 2, 0, 2, 0, 1]))
+    assert total == 1
+
+
+def test_empty_and_tiny(engine):
+    with pytest.raises(tc.TCError) as ei:  # a graph needs at least one vertex
+        engine.count(np.array([0]), np.zeros(0, np.int32))
+    assert ei.value.status == 7
+    assert engine.count(np.array([0, 0]), np.zeros(0, np.int32))[0] == 0
+    assert engine.count(np.array([0, 0, 0]), np.zeros(0, np.int32))[0] == 0
+    assert engine.count(np.array([0, 1, 2]), np.array([1, 0]))[0] == 0
+
+
+def test_tcsolver_mirror(engine, golden, tmp_path):
+    case = next(c for c in golden if c["name"] == "rmat_s10_ef8")
+    rowptr, colidx = csr_of(case)
+    tc.save_graphminer(str(tmp_path / "graph"), rowptr, colidx)
+    g = tc.Graph(str(tmp_path / "graph"), use_dag=True)
+    orow, ocol = oracle.orient(rowptr, colidx)
+    assert np.array_equal(g.out_rowptr(), orow) and np.array_equal(g.out_colidx(), ocol)
+    assert tc.TCSolver(g, 5, 1, 1024) == 5 + case["triangles"]
+    dag_only = tc.Graph.from_csr(orow, ocol, oriented=True)
+    assert tc.TCSolver(dag_only) == case["triangles"]
+
+
+def test_cli_matches_reference_usage(golden, tmp_path):
+    import subprocess
+    from hetegeneous_parallel_programming_gb300 import build
+    case = next(c for c in golden if c["name"] == "ba_1500_5")
+    rowptr, colidx = csr_of(case)
+    tc.save_graphminer(str(tmp_path / "graph"), rowptr, colidx)
+    out = subprocess.run([str(build.OUT / "tc_main"), str(tmp_path / "graph"), "1", "1024", "1"],
+                         capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    assert f"total_num_triangles = {case['triangles']}" in out.stdout

@@ -1,0 +1,138 @@
+"""Host-side logic and the C ABI surface (no GPU needed)."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import hetegeneous_parallel_programming_gb300 as tc
+from hetegeneous_parallel_programming_gb300 import _ffi
+from oracle import oracle
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def declared_symbols():
+    text = (ROOT / "include" / "tc.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(tc_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_every_declared_symbol_is_exported():
+    L = _ffi.lib()
+    names = declared_symbols()
+    assert len(names) >= 25
+    for name in names:
+        assert hasattr(L, name), name
+    assert set(names) == set(_ffi.exported_symbols())
+
+
+def test_cpp_mirror_symbols_exported():
+    so = C.CDLL(str(_ffi.LIB_PATH))
+    assert hasattr(so, "_Z8TCSolverR5GraphRmii")  # TCSolver(Graph&, unsigned long&, int, int)
+
+
+def test_status_strings():
+    L = _ffi.lib()
+    for s in range(9):
+        assert L.tc_status_str(s).decode() == _ffi.STATUS[s]
+
+
+def test_no_device_is_reported_not_crashed():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is visible")
+    with pytest.raises(tc.TCError) as ei:
+        tc.Engine(0)
+    assert ei.value.status == 8
+
+
+@pytest.mark.parametrize("spec", [
+    tc.GenSpec("er", n=5000, avg_degree=12, seed=3),
+    tc.GenSpec("rmat", scale=12, edge_factor=8, seed=1),
+    tc.GenSpec("chung_lu", n=4000, avg_degree=10, gamma=2.1, seed=5),
+    tc.GenSpec("rgg", n=3000, avg_degree=9, seed=2),
+])
+def test_host_generators_deterministic_and_in_range(spec):
+    n, s1, d1 = tc.gen_edges_host(spec)
+    n2, s2, d2 = tc.gen_edges_host(spec)
+    assert n == n2 and np.array_equal(s1, s2) and np.array_equal(d1, d2)
+    assert len(s1) > 0 and s1.min() >= 0 and d1.min() >= 0 and s1.max() < n and d1.max() < n
+    other = tc.GenSpec(**{**spec.__dict__, "seed": spec.seed + 1})
+    _, s3, _ = tc.gen_edges_host(other)
+    assert not (len(s3) == len(s1) and np.array_equal(s3, s1))
+
+
+def test_rmat_degree_skew():
+    n, s, d = tc.gen_edges_host(tc.GenSpec("rmat", scale=14, edge_factor=16, seed=0))
+    deg = np.bincount(np.concatenate([s, d]), minlength=n)
+    assert deg[0] > 50 * deg.mean()  # vertex 0 collects quadrant a at every level
+
+
+def test_rgg_average_degree_close_to_target():
+    n, s, d = tc.gen_edges_host(tc.GenSpec("rgg", n=20000, avg_degree=20, seed=4))
+    assert 0.85 * 20 < 2 * len(s) / n < 1.05 * 20
+
+
+def test_host_csr_builder_matches_oracle():
+    n, s, d = tc.gen_edges_host(tc.GenSpec("rmat", scale=11, edge_factor=16, seed=9))
+    r1, c1 = tc.csr_from_edges_host(n, s, d)
+    r2, c2 = oracle.csr_from_edges(n, s, d)
+    assert np.array_equal(r1, r2) and np.array_equal(c1, c2)
+    tc.check_csr(r1, c1, sorted_simple=True)
+
+
+def test_graphminer_round_trip(tmp_path):
+    n, s, d = tc.gen_edges_host(tc.GenSpec("er", n=700, avg_degree=6, seed=1))
+    r, c = tc.csr_from_edges_host(n, s, d)
+    tc.save_graphminer(str(tmp_path / "g"), r, c)
+    meta = (tmp_path / "g.meta.txt").read_text().split()
+    assert meta[:4] == [str(n), str(len(c)), "4", "8"]
+    assert int(meta[6]) == int(np.diff(r).max())
+    r2, c2 = tc.load_graphminer(str(tmp_path / "g"))
+    assert np.array_equal(r, r2) and np.array_equal(c, c2)
+    g = tc.Graph(str(tmp_path / "g"))
+    assert g.V() == n and g.E() == len(c) and g.get_degree(3) == r[4] - r[3]
+
+
+def test_graphminer_malformed_files(tmp_path):
+    r = np.array([0, 1, 2], np.int64)
+    c = np.array([1, 0], np.int32)
+    tc.save_graphminer(str(tmp_path / "ok"), r, c)
+    # truncated edge file
+    (tmp_path / "ok.edge.bin").write_bytes(c.tobytes()[:4])
+    with pytest.raises(tc.TCError) as ei:
+        tc.load_graphminer(str(tmp_path / "ok"))
+    assert ei.value.status == 5
+    # missing files
+    with pytest.raises(tc.TCError) as ei:
+        tc.load_graphminer(str(tmp_path / "nope"))
+    assert ei.value.status == 5
+    # wrong id width
+    tc.save_graphminer(str(tmp_path / "w"), r, c)
+    meta = (tmp_path / "w.meta.txt").read_text().replace("4 8", "8 8", 1)
+    (tmp_path / "w.meta.txt").write_text(meta)
+    with pytest.raises(tc.TCError) as ei:
+        tc.load_graphminer(str(tmp_path / "w"))
+    assert ei.value.status == 7
+    # out-of-range id in an otherwise well-formed file
+    (tmp_path / "bad.meta.txt").write_text("2\n2\n4 8 1 4\n1\n0\n0\n0\n")
+    (tmp_path / "bad.vertex.bin").write_bytes(r.tobytes())
+    (tmp_path / "bad.edge.bin").write_bytes(np.array([1, 5], np.int32).tobytes())
+    with pytest.raises(tc.TCError) as ei:
+        tc.load_graphminer(str(tmp_path / "bad"))
+    assert ei.value.status == 2
+
+
+@pytest.mark.parametrize("rowptr,colidx,why", [
+    ([0, 2, 1, 3], [1, 2, 0], "monotone"),
+    ([0, 1, 2, 2], [1, 3], "range"),
+    ([0, 2, 3, 3], [1, 1, 0], "ascending"),
+    ([0, 1, 2, 2], [0, 0], "self loop"),
+    ([1, 1, 2, 2], [0, 0], "rowptr"),
+])
+def test_check_csr_rejects(rowptr, colidx, why):
+    with pytest.raises(tc.TCError) as ei:
+        tc.check_csr(np.array(rowptr), np.array(colidx), sorted_simple=True)
+    assert ei.value.status == 2
