@@ -331,7 +331,7 @@ tc_status tc_tile_profile(tc_ctx *ctx, const tc_csr *g, float *features, float *
     else if (ctx->h_pinned[2] != first_total)
       return set_error(ctx, TC_ERR_CUDA, "arm %d counted %llu triangles, arm 0 counted %llu", arm,
                        (unsigned long long)ctx->h_pinned[2], (unsigned long long)first_total);
-    const float occ = (float)ctx->arm_blocks_per_sm[arm];
+    const float occ = (float)ctx->arm_units_per_sm[arm];  // SM-cycles per tile
     for (int64_t t = 0; t < T; ++t) costs[t * TC_NUM_ARMS + arm] = (float)cyc[(size_t)t] / occ;
   }
   return TC_OK;

@@ -41,12 +41,10 @@ __device__ __forceinline__ float flog2p1(float x) { return __log2f(1.0f + x); }
 // Fixed degree-threshold selector: the engine's fallback and the judge of the
 // learned one.
 __device__ __forceinline__ int fixed_select(const PlanStats &s) {
-  if (s.nrows <= 8.f && s.maxwin <= (float)BM_BITS && s.mean_db >= 4.f && s.frac >= 0.25f) return TC_ARM_BITMAP;
-  if (s.mean_min >= 48.f && s.mean_max <= 8.f * s.mean_min) return TC_ARM_MERGE_32;
-  if (s.mean_min >= 8.f && s.mean_max <= 4.f * s.mean_min) return TC_ARM_MERGE_8;
-  if (s.mean_min >= 16.f) return TC_ARM_BSEARCH_32;
-  if (s.mean_min >= 4.f) return TC_ARM_BSEARCH_8;
-  return TC_ARM_BSEARCH_4;
+  if (s.maxdr > 512.f && s.nrows <= 16.f && s.maxwin <= (float)BM_BITS) return TC_ARM_BITMAP;
+  if (s.mean_max <= 4.f) return TC_ARM_BSEARCH_4;
+  if (s.mean_min >= 128.f && s.mean_max <= 2.f * s.mean_min) return TC_ARM_MERGE_32;
+  return TC_ARM_HASH;
 }
 
 // MLP cost model (16 -> 64 -> 64 -> arms, ReLU); weights staged in shared
@@ -323,7 +321,7 @@ __global__ void __launch_bounds__(CT_THREADS) bsearch_kernel(DevDag g, const uin
     }
     if (tile_cycles) {
       __syncthreads();
-      if (threadIdx.x == 0) tile_cycles[tile] = (unsigned long long)(clock64() - c0);
+      if (threadIdx.x == 0) atomicAdd(&tile_cycles[tile], (unsigned long long)(clock64() - c0));
     }
   }
   flush_total(acc, total);
@@ -384,8 +382,149 @@ __global__ void __launch_bounds__(CT_THREADS) merge_kernel(DevDag g, const uint3
     }
     if (tile_cycles) {
       __syncthreads();
-      if (threadIdx.x == 0) tile_cycles[tile] = (unsigned long long)(clock64() - c0);
+      if (threadIdx.x == 0) atomicAdd(&tile_cycles[tile], (unsigned long long)(clock64() - c0));
     }
+  }
+  flush_total(acc, total);
+}
+
+// ---- HASH (warp-level, row-staged) ---------------------------------------------------
+//
+// A warp owns a 512-edge sub-tile pulled from the arm's queue.  For every
+// row segment in it, the warp hashes the row's remaining out-list (elements
+// after the segment's first edge: earlier ones are <= that edge's target
+// and cannot meet its out-list) into its own shared-memory table
+// (multiplicative hashing, linear probing, load <= 1/2), then streams the
+// out-lists of up to 32 of the segment's edges at once as one flattened
+// sequence: lane p of a pass reads element p of the concatenation, so short
+// lists do not idle lanes and each list is read with coalesced loads.  Hits
+// are rare (they are triangles) and go to a shared per-edge counter.
+
+constexpr int HT_THREADS = 256;
+constexpr int HT_WARPS = HT_THREADS / 32;
+constexpr int HT_SLOTS = 1024;               // per warp: rows with <= 512 remaining entries
+constexpr int SUB_EDGES = TILE_EDGES / 8;    // warp work item
+constexpr int32_t HT_EMPTY = -1;
+
+__device__ __forceinline__ uint32_t hslot(int32_t x, int bits) {
+  return ((uint32_t)x * 0x9E3779B1u) >> (32 - bits);
+}
+
+__global__ void __launch_bounds__(HT_THREADS) hash_kernel(DevDag g, const uint32_t *__restrict__ qtiles,
+                                                         const int64_t *__restrict__ qoff, int arm, unsigned *head,
+                                                         uint32_t *out, unsigned long long *total,
+                                                         unsigned long long *tile_cycles) {
+  __shared__ int32_t tab[HT_WARPS][HT_SLOTS];
+  __shared__ int32_t s_incl[HT_WARPS][32];
+  __shared__ long long s_base[HT_WARPS][32];  // list start minus the list's first flattened index
+  __shared__ uint32_t s_hits[HT_WARPS][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int32_t *T = tab[w];
+  const int64_t qb = qoff[arm], qn = qoff[arm + 1] - qb;
+  const int64_t items = qn * (TILE_EDGES / SUB_EDGES);
+  unsigned long long acc = 0;
+  for (;;) {
+    unsigned it = 0;
+    if (lane == 0) it = atomicAdd(head, 1u);
+    it = __shfl_sync(TC_FULL_MASK, it, 0);
+    if ((int64_t)it >= items) break;
+    const int64_t tile = qtiles[qb + it / (TILE_EDGES / SUB_EDGES)];
+    const int64_t e0 = tile * TILE_EDGES + (int64_t)(it % (TILE_EDGES / SUB_EDGES)) * SUB_EDGES;
+    const int64_t e1 = min(g.m, e0 + SUB_EDGES);
+    const long long c0 = clock64();
+    for (int64_t e = e0; e < e1;) {
+      const int32_t r = g.src[e];
+      const int64_t rb = g.rowptr[r], re = g.rowptr[r + 1];
+      const int64_t se = min(e1, re);
+      const int64_t a0 = g.restrict_after ? e + 1 : rb;
+      const int na = (int)(re - a0);
+      if (na <= 0) {  // nothing after the segment start can be shared
+        for (int64_t k = e + lane; k < se; k += 32) put_edge_count(g, out, k, 0u);
+        e = se;
+        continue;
+      }
+      if (na > HT_SLOTS / 2) {  // row too long for the warp table: binary search per edge
+        for (int64_t k = e; k < se; ++k) {
+          int32_t s;
+          const EdgeLists L = edge_lists(g, k, s);
+          uint32_t c = 0;
+          if (L.na > 0 && L.nb > 0) {
+            if (L.na <= L.nb) c = bsearch_count<32>(L.a, L.na, L.b, L.nb, lane);
+            else c = bsearch_count<32>(L.b, L.nb, L.a, L.na, lane);
+          }
+          c = warp_sum(c);
+          if (lane == 0) {
+            put_edge_count(g, out, k, c);
+            acc += c;
+          }
+        }
+        e = se;
+        continue;
+      }
+      int bits = 5;
+      while ((1 << bits) < 2 * na) ++bits;
+      const uint32_t mask = (1u << bits) - 1u;
+      for (int k = lane; k < (1 << bits); k += 32) T[k] = HT_EMPTY;
+      __syncwarp();
+      for (int k = lane; k < na; k += 32) {
+        const int32_t x = __ldg(g.col + a0 + k);
+        uint32_t sl = hslot(x, bits);
+        while (atomicCAS(&T[sl], HT_EMPTY, x) != HT_EMPTY) sl = (sl + 1) & mask;
+      }
+      const int32_t amax = __ldg(g.col + re - 1);
+      __syncwarp();
+      for (int64_t eb = e; eb < se; eb += 32) {
+        const int64_t ei = eb + lane;
+        int nb = 0;
+        long long bst = 0;
+        if (ei < se) {
+          const int32_t s = g.col[ei];
+          bst = g.rowptr[s];
+          nb = (int)(g.rowptr[s + 1] - bst);
+        }
+        int incl = nb;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(TC_FULL_MASK, incl, o);
+          if (lane >= o) incl += y;
+        }
+        const int P = __shfl_sync(TC_FULL_MASK, incl, 31);
+        s_incl[w][lane] = incl;
+        s_base[w][lane] = bst - (long long)(incl - nb);
+        s_hits[w][lane] = 0u;
+        __syncwarp();
+        int i = 0;
+        int cur_end = s_incl[w][0];
+        long long cur_base = s_base[w][0];
+        for (int p = lane; p < P; p += 32) {
+          if (p >= cur_end) {
+            do { ++i; } while (s_incl[w][i] <= p);
+            cur_end = s_incl[w][i];
+            cur_base = s_base[w][i];
+          }
+          const int32_t x = __ldg(g.col + cur_base + p);
+          if (x <= amax) {
+            uint32_t sl = hslot(x, bits);
+            for (;;) {
+              const int32_t v = T[sl];
+              if (v == x) { atomicAdd(&s_hits[w][i], 1u); break; }
+              if (v == HT_EMPTY) break;
+              sl = (sl + 1) & mask;
+            }
+          }
+        }
+        __syncwarp();
+        if (ei < se) {
+          const uint32_t c = s_hits[w][lane];
+          put_edge_count(g, out, ei, c);
+          acc += c;
+        }
+        __syncwarp();
+      }
+      e = se;
+      __syncwarp();
+    }
+    if (tile_cycles && lane == 0) atomicAdd(&tile_cycles[tile], (unsigned long long)(clock64() - c0));
   }
   flush_total(acc, total);
 }
@@ -463,7 +602,7 @@ __global__ void __launch_bounds__(BM_THREADS) bitmap_kernel(DevDag g, const uint
     }
     if (tile_cycles) {
       __syncthreads();
-      if (threadIdx.x == 0) tile_cycles[tile] = (unsigned long long)(clock64() - c0);
+      if (threadIdx.x == 0) atomicAdd(&tile_cycles[tile], (unsigned long long)(clock64() - c0));
     }
   }
   flush_total(acc, total);
@@ -477,14 +616,16 @@ typedef void (*ArmKernel)(DevDag, const uint32_t *, const int64_t *, int, unsign
 static ArmKernel arm_kernel(int arm) {
   switch (arm) {
     case TC_ARM_BSEARCH_4: return bsearch_kernel<4>;
-    case TC_ARM_BSEARCH_8: return bsearch_kernel<8>;
     case TC_ARM_BSEARCH_32: return bsearch_kernel<32>;
     case TC_ARM_MERGE_8: return merge_kernel<8>;
     case TC_ARM_MERGE_32: return merge_kernel<32>;
+    case TC_ARM_HASH: return hash_kernel;
     default: return bitmap_kernel;
   }
 }
-static int arm_threads(int arm) { return arm == TC_ARM_BITMAP ? BM_THREADS : CT_THREADS; }
+static int arm_threads(int arm) {
+  return arm == TC_ARM_BITMAP ? BM_THREADS : arm == TC_ARM_HASH ? HT_THREADS : CT_THREADS;
+}
 static int arm_smem(int arm) { return arm == TC_ARM_BITMAP ? BM_SMEM_BYTES : 0; }
 
 tc_status init_arm_occupancy(tc_ctx *ctx) {
@@ -495,6 +636,8 @@ tc_status init_arm_occupancy(tc_ctx *ctx) {
     int nb = 0;
     TC_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, arm_kernel(a), arm_threads(a), arm_smem(a)));
     ctx->arm_blocks_per_sm[a] = nb > 0 ? nb : 1;
+    // independent workers per SM: warps for the warp-level HASH arm, blocks otherwise
+    ctx->arm_units_per_sm[a] = ctx->arm_blocks_per_sm[a] * (a == TC_ARM_HASH ? HT_WARPS : 1);
   }
   return TC_OK;
 }
@@ -564,6 +707,8 @@ tc_status run_count(tc_ctx *ctx, const DevDag &g, const tc_opts &opts, CountBufs
     TC_CHECK_LAUNCH(ctx);
   }
   TC_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->d_heads, 0, sizeof(unsigned) * 64, ctx->stream));
+  if (cb.tile_cycles && T > 0)
+    TC_CHECK_CUDA(ctx, cudaMemsetAsync(cb.tile_cycles, 0, sizeof(unsigned long long) * T, ctx->stream));
   if (timing) TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[9], ctx->stream));
   for (int a = 0; a < TC_NUM_ARMS; ++a) {
     if (T > 0) {

@@ -31,6 +31,7 @@ struct tc_ctx {
   bool mlp_loaded = false;
   // per-arm kernel occupancy (blocks per SM), filled at create
   int arm_blocks_per_sm[TC_NUM_ARMS] = {};
+  int arm_units_per_sm[TC_NUM_ARMS] = {};   // independent workers (warps or blocks) per SM
   int64_t launches = 0;                   // kernels launched by the current call
   // captured back half of the batched pipeline (batch.cu), keyed by shape,
   // options and the buffers it reads

@@ -62,11 +62,11 @@ typedef struct tc_csr {
  * arm is exact; they differ only in speed. */
 typedef enum tc_arm {
   TC_ARM_BSEARCH_4 = 0,    /* 4 lanes per edge, binary search short->long     */
-  TC_ARM_BSEARCH_8 = 1,    /* 8 lanes per edge                                */
-  TC_ARM_BSEARCH_32 = 2,   /* one warp per edge                               */
-  TC_ARM_MERGE_8 = 3,      /* 8-lane windowed merge-path                      */
-  TC_ARM_MERGE_32 = 4,     /* 32-lane windowed merge-path                     */
-  TC_ARM_BITMAP = 5,       /* block bitmap of the row + popcount probes       */
+  TC_ARM_BSEARCH_32 = 1,   /* one warp per edge, binary search short->long    */
+  TC_ARM_MERGE_8 = 2,      /* 8-lane windowed merge-path                      */
+  TC_ARM_MERGE_32 = 3,     /* 32-lane windowed merge-path                     */
+  TC_ARM_HASH = 4,         /* warp hash of the row's out-list, flattened probes */
+  TC_ARM_BITMAP = 5,       /* block bitmap of the row's id window + probes    */
   TC_NUM_ARMS = 6
 } tc_arm;
 
