@@ -19,7 +19,7 @@ OUT = PKG / "_build"
 INCLUDE = PKG.parent / "include"
 LIB = OUT / "libtc.so"
 
-CU_SOURCES = ["radix_sort.cu", "orient.cu", "count.cu", "capi.cu", "build_graph.cu", "mlp.cu", "batch.cu"]
+CU_SOURCES = ["radix_sort.cu", "orient.cu", "count.cu", "capi.cu", "build_graph.cu", "mlp.cu", "batch.cu", "noalloc.cu"]
 CPP_SOURCES = ["host_graph.cpp", "solver.cpp"]
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"

@@ -141,6 +141,34 @@ tc_status tc_count(tc_ctx *ctx, const tc_csr *g, const tc_opts *opts, uint64_t *
 tc_status tc_count_dag(tc_ctx *ctx, const tc_csr *dag, const tc_opts *opts, uint64_t *total,
                        uint32_t *edge_counts, int64_t edge_capacity, tc_stats *stats);
 
+/* ---- allocation-free variant ------------------------------------------- */
+
+/* Size of the fixed device scratch array behind tc_count_dag_noalloc.  Every
+ * GPU that loads the library holds it until the process exits. */
+#define TC_NOALLOC_SCRATCH_BYTES (4u << 20)
+
+/* No counterpart in the reference: an extra entry point for callers that
+ * must not allocate device memory while counting — applications whose
+ * runtime owns the whole GPU through its own memory pool (and forbids
+ * cudaMalloc outside it), plugins loaded into such applications, and
+ * latency-bound loops that cannot afford cudaMalloc's implicit device
+ * synchronisation.  It counts the triangles of an oriented graph (the
+ * tc_count_dag contract, sorted rows, ids in [0, n)) with no ctx and no
+ * allocation of any kind: its scratch is a fixed static device array of
+ * TC_NOALLOC_SCRATCH_BYTES, which caps m at about 536 million edges; larger
+ * inputs are rejected with TC_ERR_UNSUPPORTED.
+ *   rowptr [n+1], colidx [m], total [1] and the optional edge_counts [m] are
+ *   DEVICE pointers on `device`; stream is a cudaStream_t (NULL: the legacy
+ *   default stream).  The call is asynchronous: *total is valid once the
+ *   stream has been synchronised.  Inputs are not validated on the device.
+ * The first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * All calls share the one array and every call overwrites it: calls whose
+ * work overlaps on the GPU (other streams or threads without ordering) race
+ * and return wrong counts.  Errors are reported by tc_last_error(NULL). */
+tc_status tc_count_dag_noalloc(int device, const int64_t *rowptr, const int32_t *colidx, int64_t n, int64_t m,
+                               uint64_t *total, uint32_t *edge_counts, void *stream);
+
 /* ---- batched path ------------------------------------------------------ */
 
 /* A batch of graphs, each a symmetric CSR with local ids, concatenated:
