@@ -162,16 +162,14 @@ def cpu_sample(rowptr_h, colidx_h, target_s: float):
     orow, ocol = oracle.orient(rowptr_h, colidx_h)
     t_full_orient = time.time() - t0
     n = len(rowptr_h) - 1
-    step = max(1, n // 256)
-    while True:
-        t0 = time.time()
-        oracle.orient_sample_cost(rowptr_h, colidx_h, step)
-        oracle.count_sample(orow, ocol, step)
-        dt = time.time() - t0
-        if dt > 0.5 or step == 1:
+    run_cpu_sample(rowptr_h, colidx_h, orow, ocol, max(1, n // 64))  # warm caches and the thread pool
+    step = max(1, n // 1024)
+    for _ in range(10):
+        dt = run_cpu_sample(rowptr_h, colidx_h, orow, ocol, step)
+        if dt >= 0.5 * target_s or step == 1:
             break
-        step = max(1, step // 4)
-    step = max(1, int(step * dt / target_s)) if dt < target_s else step
+        # sample cost scales as 1/step; aim at the target, at most 16x per round
+        step = max(1, int(step * max(dt, target_s / 16) / target_s))
     kept_rows = np.diff(orow)[::step]
     return orow, ocol, step, int(kept_rows.sum()), t_full_orient
 

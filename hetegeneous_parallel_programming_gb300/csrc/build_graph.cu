@@ -155,7 +155,7 @@ tc_status tc_csr_from_edges(tc_ctx *ctx, int64_t n, int64_t M, const int32_t *sr
     edge_keys_kernel<<<grid_for(ctx, M, 256, 8), 256, 0, ctx->stream>>>(dsrc, ddst, M, n, bits, k0);
     TC_CHECK_LAUNCH(ctx);
     uint64_t *sk = nullptr;
-    TC_TRY(radix_sort(ctx, k0, k1, nullptr, nullptr, N, 2 * bits, scratch, &sk, nullptr));
+    TC_TRY(radix_sort(ctx, k0, k1, nullptr, nullptr, N, 0, 2 * bits, scratch, &sk, nullptr));
     unique_flag_kernel<<<grid_for(ctx, N, 256, 8), 256, 0, ctx->stream>>>(sk, N, sentinel, flag);
     TC_CHECK_LAUNCH(ctx);
     TC_TRY(exclusive_scan_i64(ctx, flag, flag, N, scratch, (int64_t *)&ctx->d_total[0]));

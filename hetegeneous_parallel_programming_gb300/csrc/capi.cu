@@ -68,10 +68,10 @@ void orient_sizes(const tc_ctx *ctx, int64_t n, int64_t nnz, bool perm, bool dag
   size_t scr = std::max(radix_sort_scratch_bytes(ctx, std::max<int64_t>(n, mmax)), scan_scratch_bytes(ctx, n + 1));
   scr = std::max(scr, scan_scratch_bytes(ctx, G));
   sz.take<char>((int64_t)scr);
-  sz.take<uint64_t>(mmax); sz.take<uint64_t>(mmax);
-  if (perm) { sz.take<uint32_t>(mmax); sz.take<uint32_t>(mmax); }
-  sz.take<int64_t>(n + 1); sz.take<int64_t>(n + 1);
+  sz.take<int64_t>(n + 1); sz.take<int64_t>(n + 1); sz.take<int64_t>(n + 1);
+  sz.take<int32_t>(n); sz.take<int32_t>(n); sz.take<unsigned>(2);
   sz.take<int32_t>(mmax); sz.take<int32_t>(mmax);
+  if (perm) sz.take<uint32_t>(mmax);
   if (dagcol) sz.take<int32_t>(mmax);
 }
 
@@ -88,14 +88,15 @@ void orient_carve(const tc_ctx *ctx, int64_t n, int64_t nnz, bool perm, bool dag
   size_t scr = std::max(radix_sort_scratch_bytes(ctx, std::max<int64_t>(n, mmax)), scan_scratch_bytes(ctx, n + 1));
   scr = std::max(scr, scan_scratch_bytes(ctx, b.G));
   b.sort_scratch = bump.take<char>((int64_t)scr);
-  b.ekeys0 = bump.take<uint64_t>(mmax);
-  b.ekeys1 = bump.take<uint64_t>(mmax);
-  b.evals0 = perm ? bump.take<uint32_t>(mmax) : nullptr;
-  b.evals1 = perm ? bump.take<uint32_t>(mmax) : nullptr;
+  b.orowptr = bump.take<int64_t>(n + 1);
   b.nrowptr = bump.take<int64_t>(n + 1);
   b.dnew = bump.take<int64_t>(n + 1);
+  b.mid_list = bump.take<int32_t>(n);
+  b.huge_list = bump.take<int32_t>(n);
+  b.seg_counts = bump.take<unsigned>(2);
   b.ncol = bump.take<int32_t>(mmax);
   b.nsrc = bump.take<int32_t>(mmax);
+  b.perm = perm ? bump.take<uint32_t>(mmax) : nullptr;
   b.dag_col = dagcol ? bump.take<int32_t>(mmax) : nullptr;
 }
 
@@ -380,9 +381,10 @@ tc_status tc_orient(tc_ctx *ctx, const tc_csr *g, int64_t *dag_rowptr, int32_t *
                      (long long)m);
   if (g->on_device) ob.dag_col = dag_colidx;
   DevDag dag;
-  TC_TRY(orient_phase_b(ctx, d, ob, m, false, true, &dag));
-  // original-id rowptr: exclusive scan of the kept out-degrees (kept[n] == 0)
-  TC_TRY(exclusive_scan_i64(ctx, ob.kept, d_rp, d.n + 1, ob.sort_scratch, nullptr));
+  (void)dag;
+  TC_TRY(orient_phase_b(ctx, d, ob, m, false, true, nullptr));  // original-id columns only, no relabel
+  TC_CHECK_CUDA(ctx, cudaMemcpyAsync(d_rp, ob.orowptr, sizeof(int64_t) * (size_t)(d.n + 1), cudaMemcpyDeviceToDevice,
+                                     ctx->stream));
   if (!g->on_device) {
     TC_CHECK_CUDA(ctx, cudaMemcpyAsync(dag_rowptr, d_rp, sizeof(int64_t) * (size_t)(d.n + 1), cudaMemcpyDeviceToHost,
                                        ctx->stream));

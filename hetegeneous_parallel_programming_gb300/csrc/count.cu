@@ -41,10 +41,10 @@ __device__ __forceinline__ float flog2p1(float x) { return __log2f(1.0f + x); }
 // Fixed degree-threshold selector: the engine's fallback and the judge of the
 // learned one.
 __device__ __forceinline__ int fixed_select(const PlanStats &s) {
-  if (s.maxdr > 512.f && s.nrows <= 16.f && s.maxwin <= (float)BM_BITS) return TC_ARM_BITMAP;
-  if (s.mean_max <= 4.f) return TC_ARM_BSEARCH_4;
-  if (s.mean_min >= 128.f && s.mean_max <= 2.f * s.mean_min) return TC_ARM_MERGE_32;
-  return TC_ARM_HASH;
+  if (s.nrows <= 8.f && s.maxwin <= (float)BM_BITS && s.mean_db >= 4.f && s.frac >= 0.25f) return TC_ARM_BITMAP;
+  if (s.mean_min >= 48.f && s.mean_max <= 8.f * s.mean_min) return TC_ARM_MERGE_32;
+  if (s.mean_min >= 8.f) return TC_ARM_BSEARCH_32;
+  return TC_ARM_BSEARCH_4;
 }
 
 // MLP cost model (16 -> 64 -> 64 -> arms, ReLU); weights staged in shared
@@ -699,7 +699,7 @@ tc_status run_count(tc_ctx *ctx, const DevDag &g, const tc_opts &opts, CountBufs
   }
   uint64_t *sk = cb.qkeys0;
   uint32_t *sv = cb.qvals0;
-  if (T > 1) TC_TRY(radix_sort(ctx, cb.qkeys0, cb.qkeys1, cb.qvals0, cb.qvals1, T, 43, cb.sort_scratch, &sk, &sv));
+  if (T > 1) TC_TRY(radix_sort(ctx, cb.qkeys0, cb.qkeys1, cb.qvals0, cb.qvals1, T, 0, 43, cb.sort_scratch, &sk, &sv));
   if (T > 0) {
     qoff_kernel<<<1, 32, 0, ctx->stream>>>(sk, T, cb.qoff);
     TC_CHECK_LAUNCH(ctx);

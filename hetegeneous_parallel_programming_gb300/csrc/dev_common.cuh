@@ -207,11 +207,12 @@ __device__ void expand_rows(const int64_t *__restrict__ rowptr, int64_t n, int64
 // ---- host-side launch helpers shared by the .cu files --------------------------
 
 // Radix sort (radix_sort.cu): stable LSD sort of uint64 keys on bits
-// [0, bits), optional uint32 payload.  k0/v0 hold the input; k1/v1 are
-// same-sized scratch.  On return *kres / *vres point at the sorted data.
+// [begin_bit, end_bit), optional uint32 payload.  k0/v0 hold the input;
+// k1/v1 are same-sized scratch.  On return *kres / *vres point at the sorted
+// data.
 size_t radix_sort_scratch_bytes(const tc_ctx *ctx, int64_t N);
-tc_status radix_sort(tc_ctx *ctx, uint64_t *k0, uint64_t *k1, uint32_t *v0, uint32_t *v1, int64_t N, int bits,
-                     void *scratch, uint64_t **kres, uint32_t **vres);
+tc_status radix_sort(tc_ctx *ctx, uint64_t *k0, uint64_t *k1, uint32_t *v0, uint32_t *v1, int64_t N, int begin_bit,
+                     int end_bit, void *scratch, uint64_t **kres, uint32_t **vres);
 
 // Exclusive scan of int64 values (scan.cu helpers in radix_sort.cu).
 size_t scan_scratch_bytes(const tc_ctx *ctx, int64_t N);

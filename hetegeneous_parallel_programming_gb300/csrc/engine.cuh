@@ -49,12 +49,14 @@ struct OrientBufs {
   int64_t *bcount;             // [G+1] kept per block chunk
   int64_t *d_m;                // [1]
   void *sort_scratch;          // radix + scan scratch
+  int64_t *orowptr;            // [n+1] original-order DAG row pointers
+  int64_t *nrowptr;            // [n+1] relabelled row pointers
+  int64_t *dnew;               // [n+1] relabelled row lengths
+  int32_t *mid_list, *huge_list;  // [n] rows for the block sorts
+  unsigned *seg_counts;        // [2]
   // phase B
-  uint64_t *ekeys0, *ekeys1;   // [m]
-  uint32_t *evals0, *evals1;   // [m] (optional)
-  int64_t *nrowptr;            // [n+1]
-  int64_t *dnew;               // [n+1]
   int32_t *ncol, *nsrc;        // [m]
+  uint32_t *perm;              // [m] original slot of each relabelled edge (optional)
   int32_t *dag_col;            // optional original-id DAG output [m]
   int G;                       // blocks of the entry-chunk kernels
   int64_t chunk;
@@ -65,6 +67,7 @@ struct OrientBufs {
 };
 void orient_geometry(const tc_ctx *ctx, int64_t nnz, int *G, int64_t *chunk);
 tc_status orient_phase_a(tc_ctx *ctx, const DevCSR &g, OrientBufs &b);
+// out == nullptr: only the original-id DAG columns (b.dag_col) are written.
 tc_status orient_phase_b(tc_ctx *ctx, const DevCSR &g, OrientBufs &b, int64_t m, bool want_perm,
                          bool want_dag_cols, DevDag *out);
 

@@ -144,16 +144,51 @@ __global__ void __launch_bounds__(OR_THREADS) kept_count_kernel(const int64_t *_
   if (threadIdx.x == 0) bcount[blockIdx.x] = (int64_t)bsum;
 }
 
+
+__global__ void dnew_kernel(const int64_t *__restrict__ kept, const int32_t *__restrict__ rank, int64_t n,
+                            int64_t *__restrict__ dnew) {
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x)
+    dnew[rank[u]] = kept[u];
+  if (blockIdx.x == 0 && threadIdx.x == 0) dnew[n] = 0;
+}
+
+// Rows of the relabelled DAG longer than a warp go to the block sorts: the
+// shared-memory sort up to SEG_SMEM_MAX entries, the in-place global one
+// beyond.  Lists are filled with warp-aggregated atomics (order irrelevant).
+constexpr int SEG_SMEM_MAX = 4096;
+
+__global__ void classify_rows_kernel(const int64_t *__restrict__ len, int64_t n, int32_t *__restrict__ mid_list,
+                                     int32_t *__restrict__ huge_list, unsigned *counts) {
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = lanemask_lt();
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = base + threadIdx.x;
+    const int64_t L = r < n ? len[r] : 0;
+#pragma unroll
+    for (int cls = 0; cls < 2; ++cls) {
+      const bool mine = cls == 0 ? (L > 32 && L <= SEG_SMEM_MAX) : (L > SEG_SMEM_MAX);
+      const unsigned bal = __ballot_sync(TC_FULL_MASK, mine);
+      if (!bal) continue;
+      unsigned at = 0;
+      if (lane == 0) at = atomicAdd(&counts[cls], (unsigned)__popc(bal));
+      at = __shfl_sync(TC_FULL_MASK, at, 0);
+      if (mine) (cls == 0 ? mid_list : huge_list)[at + __popc(bal & lt)] = (int32_t)r;
+    }
+  }
+}
+
 tc_status orient_phase_a(tc_ctx *ctx, const DevCSR &g, OrientBufs &b) {
   const int bits = vertex_bits(g.n);
   orient_geometry(ctx, g.nnz, &b.G, &b.chunk);
-  if (2 * bits + b.group_bits > 64)
-    return set_error(ctx, TC_ERR_UNSUPPORTED, "rank key needs %d bits", 2 * bits + b.group_bits);
+  const int gbits = b.vgroup ? b.group_bits : 0;
+  if (2 * bits + gbits > 64) return set_error(ctx, TC_ERR_UNSUPPORTED, "rank key needs %d bits", 2 * bits + gbits);
   deg_key_kernel<<<grid_for(ctx, g.n, 256, 8), 256, 0, ctx->stream>>>(g.rowptr, g.n, bits, b.vgroup, b.vkeys0);
   TC_CHECK_LAUNCH(ctx);
+  // Ids start in ascending order and the sort is stable, so sorting on the
+  // (group, degree) bits alone yields the (group, degree, id) order.
   uint64_t *sorted = nullptr;
-  TC_TRY(radix_sort(ctx, b.vkeys0, b.vkeys1, nullptr, nullptr, g.n, 2 * bits + (b.vgroup ? b.group_bits : 0),
-                    b.sort_scratch, &sorted, nullptr));
+  TC_TRY(radix_sort(ctx, b.vkeys0, b.vkeys1, nullptr, nullptr, g.n, bits, 2 * bits + gbits, b.sort_scratch, &sorted,
+                    nullptr));
   rank_kernel<<<grid_for(ctx, g.n, 256, 8), 256, 0, ctx->stream>>>(sorted, g.n, (1ULL << bits) - 1, b.rank);
   TC_CHECK_LAUNCH(ctx);
   TC_CHECK_CUDA(ctx, cudaMemsetAsync(b.kept, 0, sizeof(int64_t) * (size_t)(g.n + 1), ctx->stream));
@@ -165,18 +200,32 @@ tc_status orient_phase_a(tc_ctx *ctx, const DevCSR &g, OrientBufs &b) {
   } else {
     TC_CHECK_CUDA(ctx, cudaMemsetAsync(b.d_m, 0, sizeof(int64_t), ctx->stream));
   }
+  // original-order DAG rowptr, relabelled rowptr, and the row classes
+  TC_TRY(exclusive_scan_i64(ctx, b.kept, b.orowptr, g.n + 1, b.sort_scratch, nullptr));
+  dnew_kernel<<<grid_for(ctx, g.n, 256, 8), 256, 0, ctx->stream>>>(b.kept, b.rank, g.n, b.dnew);
+  TC_CHECK_LAUNCH(ctx);
+  TC_TRY(exclusive_scan_i64(ctx, b.dnew, b.nrowptr, g.n + 1, b.sort_scratch, nullptr));
+  TC_CHECK_CUDA(ctx, cudaMemsetAsync(b.seg_counts, 0, sizeof(unsigned) * 2, ctx->stream));
+  classify_rows_kernel<<<grid_for(ctx, g.n, 256, 8), 256, 0, ctx->stream>>>(b.dnew, g.n, b.mid_list, b.huge_list,
+                                                                            b.seg_counts);
+  TC_CHECK_LAUNCH(ctx);
   return TC_OK;
 }
 
-// ---- phase B: compaction, relabel sort, DAG arrays ---------------------------
+// ---- phase B: direct placement + per-row sort ---------------------------------
 
-template <bool VALS, bool DAGCOL>
-__global__ void __launch_bounds__(OR_THREADS) emit_kernel(const int64_t *__restrict__ rowptr,
-                                                         const int32_t *__restrict__ col, int64_t n, int64_t nnz,
-                                                         int64_t chunk, const int32_t *__restrict__ rank,
-                                                         const int64_t *__restrict__ boff, int bits,
-                                                         uint64_t *__restrict__ keys, uint32_t *__restrict__ vals,
-                                                         int32_t *__restrict__ dag_col) {
+// Kept entry k (input order, original slot kpos) of row u goes to relabelled
+// slot nrowptr[rank u] + (kpos - orowptr[u]) with value rank v; rows are then
+// sorted by value.
+template <bool VALS, bool DAGCOL, bool RELABEL>
+__global__ void __launch_bounds__(OR_THREADS) place_kernel(const int64_t *__restrict__ rowptr,
+                                                          const int32_t *__restrict__ col, int64_t n, int64_t nnz,
+                                                          int64_t chunk, const int32_t *__restrict__ rank,
+                                                          const int64_t *__restrict__ boff,
+                                                          const int64_t *__restrict__ orowptr,
+                                                          const int64_t *__restrict__ nrowptr,
+                                                          int32_t *__restrict__ ncol, uint32_t *__restrict__ perm,
+                                                          int32_t *__restrict__ dag_col) {
   __shared__ int rows[ENTRY_TILE];
   __shared__ int scan_tmp[32];
   __shared__ long long stmp[33];
@@ -186,7 +235,6 @@ __global__ void __launch_bounds__(OR_THREADS) emit_kernel(const int64_t *__restr
     const int64_t t1 = min(e_end, t0 + ENTRY_TILE);
     expand_rows<ENTRY_TILE>(rowptr, n, t0, t1, rows, scan_tmp);
     int32_t vv[OR_PER];
-    int32_t ru = 0;
     unsigned keepm = 0;
     const int first = threadIdx.x * OR_PER;
 #pragma unroll
@@ -196,26 +244,23 @@ __global__ void __launch_bounds__(OR_THREADS) emit_kernel(const int64_t *__restr
       if (e < t1) {
         const int u = rows[first + k];
         const int32_t v = col[e];
-        if (u >= 0 && v >= 0 && (int64_t)v < n) {
-          const int32_t rv = rank[v], rr = rank[u];
-          if (rv > rr) {
-            keepm |= 1u << k;
-            vv[k] = v;
-            ru = rr;  // all kept entries of one thread may span rows; recomputed below
-          }
+        if (u >= 0 && v >= 0 && (int64_t)v < n && rank[v] > rank[u]) {
+          keepm |= 1u << k;
+          vv[k] = v;
         }
       }
     }
-    (void)ru;
     long long tot;
     long long pos = carry + block_exclusive_scan<long long>((long long)__popc(keepm), stmp, &tot);
 #pragma unroll
     for (int k = 0; k < OR_PER; ++k) {
       if (keepm & (1u << k)) {
         const int u = rows[first + k];
-        const uint64_t key = ((uint64_t)(uint32_t)rank[u] << bits) | (uint64_t)(uint32_t)rank[vv[k]];
-        keys[pos] = key;
-        if (VALS) vals[pos] = (uint32_t)pos;
+        if (RELABEL) {
+          const long long dst = nrowptr[rank[u]] + (pos - orowptr[u]);
+          ncol[dst] = rank[vv[k]];
+          if (VALS) perm[dst] = (uint32_t)pos;
+        }
         if (DAGCOL) dag_col[pos] = vv[k];
         ++pos;
       }
@@ -225,55 +270,165 @@ __global__ void __launch_bounds__(OR_THREADS) emit_kernel(const int64_t *__restr
   }
 }
 
-__global__ void extract_kernel(const uint64_t *__restrict__ keys, int64_t m, int bits, int32_t *__restrict__ ncol,
-                               int32_t *__restrict__ nsrc) {
-  const uint64_t mask = (1ULL << bits) - 1;
-  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
-    const uint64_t k = keys[j];
-    ncol[j] = (int32_t)(k & mask);
-    nsrc[j] = (int32_t)(k >> bits);
+// Ascending bitonic network in its "flip" form: every comparator puts the
+// smaller key at the lower index, so a list of any length L behaves as if
+// padded with +infinity and comparators reaching past L are skipped.
+template <bool VALS>
+__device__ __forceinline__ void cmp_swap(int32_t *key, uint32_t *val, int a, int b) {
+  const int32_t ka = key[a], kb = key[b];
+  if (kb < ka) {
+    key[a] = kb;
+    key[b] = ka;
+    if (VALS) {
+      const uint32_t t = val[a];
+      val[a] = val[b];
+      val[b] = t;
+    }
   }
 }
 
-__global__ void dnew_kernel(const int64_t *__restrict__ kept, const int32_t *__restrict__ rank, int64_t n,
-                            int64_t *__restrict__ dnew) {
-  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x)
-    dnew[rank[u]] = kept[u];
-  if (blockIdx.x == 0 && threadIdx.x == 0) dnew[n] = 0;
+template <bool VALS>
+__device__ void block_flip_bitonic(int32_t *key, uint32_t *val, int L) {
+  int P = 1;
+  while (P < L) P <<= 1;
+  for (int k = 2; k <= P; k <<= 1) {
+    const int h = k >> 1;
+    for (int t = threadIdx.x; t < P / 2; t += blockDim.x) {
+      const int blk = t / h, off = t % h;
+      const int a = blk * k + off, bb = blk * k + k - 1 - off;
+      if (bb < L) cmp_swap<VALS>(key, val, a, bb);
+    }
+    __syncthreads();
+    for (int j = k >> 2; j >= 1; j >>= 1) {
+      for (int t = threadIdx.x; t < P / 2; t += blockDim.x) {
+        const int a = (t / j) * 2 * j + (t % j), bb = a + j;
+        if (bb < L) cmp_swap<VALS>(key, val, a, bb);
+      }
+      __syncthreads();
+    }
+  }
+}
+
+template <bool VALS>
+__global__ void seg_sort_warp_kernel(const int64_t *__restrict__ nrowptr, int64_t n, int32_t *__restrict__ ncol,
+                                     uint32_t *__restrict__ perm) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += warps) {
+    const int64_t b = nrowptr[r];
+    const int L = (int)(nrowptr[r + 1] - b);
+    if (L < 2 || L > 32) continue;
+    int32_t key = lane < L ? ncol[b + lane] : INT32_MAX;
+    uint32_t val = (VALS && lane < L) ? perm[b + lane] : 0u;
+#pragma unroll
+    for (int k = 2; k <= 32; k <<= 1) {
+      {
+        const int partner = lane ^ (k - 1);
+        const int32_t ok = __shfl_sync(TC_FULL_MASK, key, partner);
+        const uint32_t ov = VALS ? __shfl_sync(TC_FULL_MASK, val, partner) : 0u;
+        const bool take = lane < partner ? ok < key : ok > key;
+        if (take) { key = ok; if (VALS) val = ov; }
+      }
+#pragma unroll
+      for (int j = k >> 2; j >= 1; j >>= 1) {
+        const int partner = lane ^ j;
+        const int32_t ok = __shfl_sync(TC_FULL_MASK, key, partner);
+        const uint32_t ov = VALS ? __shfl_sync(TC_FULL_MASK, val, partner) : 0u;
+        const bool take = lane < partner ? ok < key : ok > key;
+        if (take) { key = ok; if (VALS) val = ov; }
+      }
+    }
+    if (lane < L) {
+      ncol[b + lane] = key;
+      if (VALS) perm[b + lane] = val;
+    }
+  }
+}
+
+template <bool VALS>
+__global__ void __launch_bounds__(256) seg_sort_smem_kernel(const int64_t *__restrict__ nrowptr,
+                                                           const int32_t *__restrict__ list, const unsigned *count,
+                                                           int32_t *__restrict__ ncol, uint32_t *__restrict__ perm) {
+  __shared__ int32_t skey[SEG_SMEM_MAX];
+  __shared__ uint32_t sval[VALS ? SEG_SMEM_MAX : 1];
+  const unsigned cnt = *count;
+  for (unsigned i = blockIdx.x; i < cnt; i += gridDim.x) {
+    const int32_t r = list[i];
+    const int64_t b = nrowptr[r];
+    const int L = (int)(nrowptr[r + 1] - b);
+    for (int k = threadIdx.x; k < L; k += blockDim.x) {
+      skey[k] = ncol[b + k];
+      if (VALS) sval[k] = perm[b + k];
+    }
+    __syncthreads();
+    block_flip_bitonic<VALS>(skey, sval, L);
+    for (int k = threadIdx.x; k < L; k += blockDim.x) {
+      ncol[b + k] = skey[k];
+      if (VALS) perm[b + k] = sval[k];
+    }
+    __syncthreads();
+  }
+}
+
+template <bool VALS>
+__global__ void __launch_bounds__(1024) seg_sort_global_kernel(const int64_t *__restrict__ nrowptr,
+                                                              const int32_t *__restrict__ list, const unsigned *count,
+                                                              int32_t *ncol, uint32_t *perm) {
+  const unsigned cnt = *count;
+  for (unsigned i = blockIdx.x; i < cnt; i += gridDim.x) {
+    const int32_t r = list[i];
+    const int64_t b = nrowptr[r];
+    const int L = (int)(nrowptr[r + 1] - b);
+    block_flip_bitonic<VALS>(ncol + b, VALS ? perm + b : nullptr, L);
+    __syncthreads();
+  }
 }
 
 tc_status orient_phase_b(tc_ctx *ctx, const DevCSR &g, OrientBufs &b, int64_t m, bool want_perm, bool want_dag_cols,
                          DevDag *out) {
-  const int bits = vertex_bits(g.n);
+  const bool relabel = out != nullptr;
   if (g.nnz > 0 && m > 0) {
-#define TC_EMIT(V, D)                                                                                    \
-  emit_kernel<V, D><<<b.G, OR_THREADS, 0, ctx->stream>>>(g.rowptr, g.col, g.n, g.nnz, b.chunk, b.rank, b.bcount, \
-                                                         bits, b.ekeys0, b.evals0, b.dag_col)
-    if (want_perm && want_dag_cols) TC_EMIT(true, true);
-    else if (want_perm) TC_EMIT(true, false);
-    else if (want_dag_cols) TC_EMIT(false, true);
-    else TC_EMIT(false, false);
-#undef TC_EMIT
+#define TC_PLACE(V, D, R)                                                                                        \
+  place_kernel<V, D, R><<<b.G, OR_THREADS, 0, ctx->stream>>>(g.rowptr, g.col, g.n, g.nnz, b.chunk, b.rank, b.bcount, \
+                                                             b.orowptr, b.nrowptr, b.ncol, b.perm, b.dag_col)
+    if (!relabel) TC_PLACE(false, true, false);
+    else if (want_perm && want_dag_cols) TC_PLACE(true, true, true);
+    else if (want_perm) TC_PLACE(true, false, true);
+    else if (want_dag_cols) TC_PLACE(false, true, true);
+    else TC_PLACE(false, false, true);
+#undef TC_PLACE
     TC_CHECK_LAUNCH(ctx);
   }
-  uint64_t *skeys = b.ekeys0;
-  uint32_t *svals = want_perm ? b.evals0 : nullptr;
-  if (m > 1)
-    TC_TRY(radix_sort(ctx, b.ekeys0, b.ekeys1, want_perm ? b.evals0 : nullptr, want_perm ? b.evals1 : nullptr, m,
-                      2 * bits, b.sort_scratch, &skeys, want_perm ? &svals : nullptr));
-  if (m > 0) {
-    extract_kernel<<<grid_for(ctx, m, 256, 8), 256, 0, ctx->stream>>>(skeys, m, bits, b.ncol, b.nsrc);
-    TC_CHECK_LAUNCH(ctx);
+  if (!relabel) return TC_OK;
+  if (m > 1) {
+    const int wgrid = grid_for(ctx, g.n * 32, 256, 8);
+    const int mgrid = ctx->num_sms * 8;
+    if (want_perm) {
+      seg_sort_warp_kernel<true><<<wgrid, 256, 0, ctx->stream>>>(b.nrowptr, g.n, b.ncol, b.perm);
+      TC_CHECK_LAUNCH(ctx);
+      seg_sort_smem_kernel<true><<<mgrid, 256, 0, ctx->stream>>>(b.nrowptr, b.mid_list, b.seg_counts, b.ncol, b.perm);
+      TC_CHECK_LAUNCH(ctx);
+      seg_sort_global_kernel<true><<<ctx->num_sms, 1024, 0, ctx->stream>>>(b.nrowptr, b.huge_list, b.seg_counts + 1,
+                                                                            b.ncol, b.perm);
+      TC_CHECK_LAUNCH(ctx);
+    } else {
+      seg_sort_warp_kernel<false><<<wgrid, 256, 0, ctx->stream>>>(b.nrowptr, g.n, b.ncol, nullptr);
+      TC_CHECK_LAUNCH(ctx);
+      seg_sort_smem_kernel<false><<<mgrid, 256, 0, ctx->stream>>>(b.nrowptr, b.mid_list, b.seg_counts, b.ncol,
+                                                                  nullptr);
+      TC_CHECK_LAUNCH(ctx);
+      seg_sort_global_kernel<false><<<ctx->num_sms, 1024, 0, ctx->stream>>>(b.nrowptr, b.huge_list,
+                                                                             b.seg_counts + 1, b.ncol, nullptr);
+      TC_CHECK_LAUNCH(ctx);
+    }
   }
-  dnew_kernel<<<grid_for(ctx, g.n, 256, 8), 256, 0, ctx->stream>>>(b.kept, b.rank, g.n, b.dnew);
-  TC_CHECK_LAUNCH(ctx);
-  TC_TRY(exclusive_scan_i64(ctx, b.dnew, b.nrowptr, g.n + 1, b.sort_scratch, nullptr));
+  TC_TRY(launch_expand_src(ctx, b.nrowptr, g.n, m, b.nsrc));
   out->n = g.n;
   out->m = m;
   out->rowptr = b.nrowptr;
   out->col = b.ncol;
   out->src = b.nsrc;
-  out->perm = want_perm ? svals : nullptr;
+  out->perm = want_perm ? b.perm : nullptr;
   out->restrict_after = 1;
   return TC_OK;
 }

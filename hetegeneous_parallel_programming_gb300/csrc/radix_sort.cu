@@ -105,24 +105,38 @@ __global__ void __launch_bounds__(RS_THREADS) rs_hist_kernel(const uint64_t *__r
     uint32_t s = 0;
 #pragma unroll
     for (int w = 0; w < RS_WARPS; ++w) s += cnt[w][d];
-    hist[(int64_t)d * G + blockIdx.x] = s;
+    hist[(int64_t)blockIdx.x * 256 + d] = s;
   }
 }
 
-// Exclusive scan of `total` uint32 counts into uint64 offsets, one block.
+// Digit offsets from the block-major histogram hist[b][d]: offs[b][d] =
+// (keys with a smaller digit) + (keys with digit d in blocks before b).  One
+// block: 4 threads per digit, each owning a quarter of the blocks; reads are
+// coalesced across digits.
 __global__ void __launch_bounds__(1024) rs_scan_kernel(const uint32_t *__restrict__ hist, uint64_t *__restrict__ offs,
-                                                      int64_t total) {
+                                                      int G) {
+  __shared__ unsigned long long part[4][256];
+  __shared__ unsigned long long base[256];
   __shared__ unsigned long long tmp[33];
-  const int64_t per = (total + blockDim.x - 1) / blockDim.x;
-  const int64_t b = (int64_t)threadIdx.x * per;
-  const int64_t e = min(total, b + per);
+  const int d = threadIdx.x & 255, q = threadIdx.x >> 8;
+  const int per = (G + 3) / 4;
+  const int b0 = q * per, b1 = min(G, b0 + per);
   unsigned long long s = 0;
-  for (int64_t i = b; i < e; ++i) s += hist[i];
+  for (int b = b0; b < b1; ++b) s += hist[(int64_t)b * 256 + d];
+  part[q][d] = s;
+  __syncthreads();
+  unsigned long long dtot = 0;
+  if (threadIdx.x < 256) dtot = part[0][d] + part[1][d] + part[2][d] + part[3][d];
+  // exclusive scan of the 256 digit totals (threads 0..255; the rest add 0)
   unsigned long long tot;
-  unsigned long long run = block_exclusive_scan<unsigned long long>(s, tmp, &tot);
-  for (int64_t i = b; i < e; ++i) {
-    offs[i] = run;
-    run += hist[i];
+  const unsigned long long ex = block_exclusive_scan<unsigned long long>(dtot, tmp, &tot);
+  if (threadIdx.x < 256) base[d] = ex;
+  __syncthreads();
+  unsigned long long run = base[d];
+  for (int k = 0; k < q; ++k) run += part[k][d];
+  for (int b = b0; b < b1; ++b) {
+    offs[(int64_t)b * 256 + d] = run;
+    run += hist[(int64_t)b * 256 + d];
   }
 }
 
@@ -138,7 +152,7 @@ __global__ void __launch_bounds__(RS_THREADS) rs_scatter_kernel(const uint64_t *
   __shared__ uint32_t tcnt[256];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const unsigned lt = lanemask_lt();
-  for (int d = threadIdx.x; d < 256; d += RS_THREADS) boff[d] = offs[(int64_t)d * G + blockIdx.x];
+  for (int d = threadIdx.x; d < 256; d += RS_THREADS) boff[d] = offs[(int64_t)blockIdx.x * 256 + d];
   for (int i = threadIdx.x; i < RS_WARPS * 256; i += RS_THREADS) (&wcnt[0][0])[i] = 0;
   __syncthreads();
   const int64_t b = (int64_t)blockIdx.x * chunk;
@@ -200,21 +214,21 @@ __global__ void __launch_bounds__(RS_THREADS) rs_scatter_kernel(const uint64_t *
   }
 }
 
-tc_status radix_sort(tc_ctx *ctx, uint64_t *k0, uint64_t *k1, uint32_t *v0, uint32_t *v1, int64_t N, int bits,
-                     void *scratch, uint64_t **kres, uint32_t **vres) {
+tc_status radix_sort(tc_ctx *ctx, uint64_t *k0, uint64_t *k1, uint32_t *v0, uint32_t *v1, int64_t N, int begin_bit,
+                     int end_bit, void *scratch, uint64_t **kres, uint32_t **vres) {
   *kres = k0;
   if (vres) *vres = v0;
-  if (N <= 1 || bits <= 0) return TC_OK;
+  if (N <= 1 || end_bit <= begin_bit) return TC_OK;
   RsGeom g = rs_geom(ctx, N);
   uint32_t *hist = (uint32_t *)scratch;
   uint64_t *offs = (uint64_t *)((char *)scratch + align_up((size_t)256 * g.G * sizeof(uint32_t), 256));
   uint64_t *ka = k0, *kb = k1;
   uint32_t *va = v0, *vb = v1;
   const bool has_vals = v0 != nullptr;
-  for (int shift = 0; shift < bits; shift += 8) {
+  for (int shift = begin_bit; shift < end_bit; shift += 8) {
     rs_hist_kernel<<<g.G, RS_THREADS, 0, ctx->stream>>>(ka, N, shift, g.chunk, hist, g.G);
     TC_CHECK_LAUNCH(ctx);
-    rs_scan_kernel<<<1, 1024, 0, ctx->stream>>>(hist, offs, (int64_t)256 * g.G);
+    rs_scan_kernel<<<1, 1024, 0, ctx->stream>>>(hist, offs, g.G);
     TC_CHECK_LAUNCH(ctx);
     if (has_vals)
       rs_scatter_kernel<true><<<g.G, RS_THREADS, 0, ctx->stream>>>(ka, va, kb, vb, N, shift, g.chunk, offs, g.G);
