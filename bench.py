@@ -45,6 +45,15 @@ WEIGHTS = ROOT / "hetegeneous_parallel_programming_gb300" / "data" / "selector_m
 TRAFFIC = ROOT / "profiles" / "ncu_traffic.json"
 
 
+def workload_desc(wl: dict) -> str:
+    if wl["kind"] == "rmat":
+        return (f"R-MAT scale {wl['scale']} edge factor {wl['edge_factor']} (a,b,c)=({wl['a']},{wl['b']},{wl['c']}) "
+                f"seed {wl['seed']}")
+    if wl["kind"] == "er":
+        return f"Erdos-Renyi n={wl['n']} avg degree {wl['avg_degree']} seed {wl['seed']}"
+    return f"Chung-Lu n={wl['n']} avg degree {wl['avg_degree']} gamma {wl['gamma']} seed {wl['seed']}"
+
+
 def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
@@ -148,10 +157,8 @@ def timed(fn, steps, warmup, eng, torch, dist):
     if dist:
         dist.barrier()
     ms = e0.elapsed_time(e1) / steps
-    if dist:
-        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    from hetegeneous_parallel_programming_gb300 import shard
+    ms, _ = shard.aggregate(ms, 0.0, dist, device="cuda")
     return ms, out
 
 
@@ -196,11 +203,21 @@ def engine_arm(args, rank, world, local_rank, dist):
     have_weights = WEIGHTS.exists()
     if have_weights:
         w = np.load(WEIGHTS)["params"].astype(np.float32)
-        eng.set_selector_weights(w)
+        have_weights = w.size == tc.TC_MLP_PARAM_COUNT  # weights of another arm set are not used
+        if have_weights:
+            eng.set_selector_weights(w)
+
+    per_edge = torch.empty(m if args.per_edge else 1, dtype=torch.int32, device=dev)
 
     def step(sel):
-        return lambda: eng.count_device(n, nnz, rowptr.data_ptr(), colidx.data_ptr(), selector=sel)
+        fa = args.force_arm  # profiling aid: every tile on one arm
+        if args.per_edge:  # per-edge local counts written to device memory every step
+            return lambda: eng.count_device(n, nnz, rowptr.data_ptr(), colidx.data_ptr(), selector=sel,
+                                            force_arm=fa, edge_counts_ptr=per_edge.data_ptr(), edge_capacity=m)
+        return lambda: eng.count_device(n, nnz, rowptr.data_ptr(), colidx.data_ptr(), selector=sel, force_arm=fa)
 
+    if args.force_arm:
+        have_weights = False
     results = {}
     clk = Clocks(local_rank)
     with clk:
@@ -212,6 +229,12 @@ def engine_arm(args, rank, world, local_rank, dist):
     ms_best, (total, st) = results[best]
     if results.get("learned") and results["learned"][1][0] != results["fixed"][1][0]:
         raise SystemExit("learned and plain selectors disagree on the count")
+    per_edge_check = None
+    if args.per_edge:  # size-independent property: the per-edge counts sum to the total
+        pe_sum = int(per_edge.to(torch.int64).sum().item())
+        per_edge_check = {"sum_of_per_edge_counts": pe_sum, "equals_total": pe_sum == total}
+        if pe_sum != total:
+            raise SystemExit("per-edge counts do not sum to the total")
     # e2e through the public API with pinned host buffers (H2D + D2H inside)
     rowptr_h = rowptr.cpu().pin_memory()
     colidx_h = colidx.cpu().pin_memory()
@@ -240,10 +263,8 @@ def engine_arm(args, rank, world, local_rank, dist):
             "scaling": "weak",
             "vs_baseline": None,
             "dtype": "int32/uint64",
-            "data": "synthetic (seeded R-MAT generated on the device; inputs larger than L2, no flush)",
-            "config": {"workload": f"rmat s{wl.get('scale')} ef{wl.get('edge_factor')} (a,b,c)=({wl.get('a')},"
-                                   f"{wl.get('b')},{wl.get('c')}) seed {wl.get('seed')}"
-                       if wl["kind"] == "rmat" else args.workload,
+            "data": f"synthetic ({workload_desc(wl)}, generated on the device; inputs larger than L2, no flush)",
+            "config": {"workload": workload_desc(wl),
                        "n": n, "undirected_edges": m, "triangles": total, "selector": best,
                        "tile_edges": 4096, "parallelism": f"replicas x{world}", "l2": "inputs > L2"},
             "plain_gteps": round(m / (results["fixed"][0] * 1e-3) / 1e9, 4),
@@ -263,6 +284,7 @@ def engine_arm(args, rank, world, local_rank, dist):
                                          "achieved": round(st["alg_bytes"] / (st["ms_count"] * 1e-3) / 1e9, 1)
                                          if st["ms_count"] > 0 else None}},
             "gpu_launches": int(st["kernel_launches"]) * args.steps,
+            "per_edge_counts": per_edge_check,
             "clocks": clk.summary(),
         }
     if not args.no_batched:
@@ -364,8 +386,8 @@ def reference_arm(args, rank, world, local_rank):
             "metric": "GTEPS on 1 GB300, learned vs plain selector (exact count); batched graphs/s",
             "value": round(v, 5), "unit": "GTEPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(sec * 1e3, 2), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "int32/uint64", "data": "synthetic (same seeded R-MAT as the engine arm)",
-            "config": {"workload": args.workload, "n": n, "undirected_edges": nnz // 2},
+            "dtype": "int32/uint64", "data": f"synthetic ({workload_desc(wl)}, same graph as the engine arm)",
+            "config": {"workload": workload_desc(wl), "n": n, "undirected_edges": nnz // 2},
             "cpu_baseline": {"value": round(v, 5), "unit": "GTEPS", "cores": cores, "kind": "port",
                              "sample": f"every {step_k}th vertex's rows ({m_sample} oriented edges): orientation "
                                        f"(graph.cc:252-298) + merge count (graph.cc:376-391), C/OpenMP"},
@@ -384,6 +406,8 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--per-edge", action="store_true", help="also write per-edge local counts every step")
+    ap.add_argument("--force-arm", default=None, help="run every tile on this arm (profiling)")
     ap.add_argument("--ref-step-seconds", type=float, default=4.0)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "engine" else args.warmup

@@ -262,6 +262,16 @@ class Engine:
             out = out[:len(colidx)]
         return int(tot.value), out, st.as_dict()
 
+    def count_edges(self, n: int, src, dst, *, selector: str = "fixed", force_arm=None):
+        """Triangles of an undirected edge list (duplicates and self loops allowed)."""
+        src, dst = _i32(src), _i32(dst)
+        o = _opts(selector, force_arm, True)
+        tot = C.c_uint64(0)
+        st = _ffi.Stats()
+        self._chk(self._L.tc_count_edges(self._h, int(n), len(src), _ptr(src), _ptr(dst), 0, C.byref(o),
+                                         C.byref(tot), C.byref(st)))
+        return int(tot.value), st.as_dict()
+
     def orient(self, rowptr, colidx):
         """Reference orientation (graph.cc:252-298) on the GPU: (dag_rowptr, dag_colidx)."""
         rowptr, colidx = _i64(rowptr), _i32(colidx)

@@ -13,14 +13,14 @@ from pathlib import Path
 PKG = Path(__file__).resolve().parent
 LIB_PATH = PKG / "_build" / "libtc.so"
 
-TC_NUM_ARMS = 6
+TC_NUM_ARMS = 8
 TC_MLP_FEATURES = 16
 TC_MLP_HIDDEN = 64
 TC_MLP_PARAM_COUNT = (TC_MLP_FEATURES * TC_MLP_HIDDEN + TC_MLP_HIDDEN + TC_MLP_HIDDEN * TC_MLP_HIDDEN +
                       TC_MLP_HIDDEN + TC_MLP_HIDDEN * TC_NUM_ARMS + TC_NUM_ARMS)
 TILE_EDGES = 4096
 
-ARM_NAMES = ["bsearch4", "bsearch32", "merge8", "merge32", "hash", "bitmap"]
+ARM_NAMES = ["bsearch4", "bsearch32", "merge8", "merge32", "hash", "bitmap", "gallop4", "mpath4"]
 
 SELECT_FIXED, SELECT_LEARNED, SELECT_FORCE = 0, 1, 2
 GEN_ER, GEN_RMAT, GEN_RGG, GEN_CHUNG_LU = 0, 1, 2, 3
@@ -94,6 +94,7 @@ _SIGS = {
     "tc_count_dag": (C.c_int, [P, C.POINTER(Csr), C.POINTER(Opts), PU64, P, I64, C.POINTER(Stats)]),
     "tc_batch_count": (C.c_int, [P, C.POINTER(Batch), C.POINTER(Opts), P, C.POINTER(Stats)]),
     "tc_count_dag_noalloc": (C.c_int, [C.c_int, P, P, I64, I64, P, P, P]),
+    "tc_count_edges": (C.c_int, [P, I64, I64, P, P, I32, C.POINTER(Opts), PU64, C.POINTER(Stats)]),
     "tc_tile_profile": (C.c_int, [P, C.POINTER(Csr), P, P, I64, PI64]),
     "tc_plan_arms": (C.c_int, [P, C.POINTER(Csr), C.POINTER(Opts), P, I64, PI64]),
     "tc_selector_train": (C.c_int, [P, P, P, I64, I32, C.c_float, U64, PF]),

@@ -185,3 +185,32 @@ tc_status tc_csr_from_edges(tc_ctx *ctx, int64_t n, int64_t M, const int32_t *sr
 }
 
 }  // extern "C"
+
+extern "C" tc_status tc_count_edges(tc_ctx *ctx, int64_t n, int64_t M, const int32_t *src, const int32_t *dst,
+                                    int32_t on_device, const tc_opts *opts, uint64_t *total, tc_stats *stats) {
+  if (!ctx || !total) return set_error(ctx, TC_ERR_INVALID_ARG, "null ctx or total");
+  if (n < 1 || n > 2147483647LL || M < 0 || (M > 0 && (!src || !dst)))
+    return set_error(ctx, TC_ERR_INVALID_ARG, "bad n or edge list");
+  if (2 * M >= (int64_t(1) << 32)) return set_error(ctx, TC_ERR_UNSUPPORTED, "too many edge samples");
+  TC_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
+  // the built CSR lives in ctx->aux: at most 2M entries
+  const size_t need = align_up(sizeof(int64_t) * (size_t)(n + 1), 256) + align_up(sizeof(int32_t) * (size_t)(2 * M + 1), 256);
+  if (need > ctx->aux_cap) {
+    TC_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (ctx->aux) TC_CHECK_CUDA(ctx, cudaFree(ctx->aux));
+    ctx->aux = nullptr;
+    ctx->aux_cap = 0;
+    cudaError_t e = cudaMalloc((void **)&ctx->aux, need);
+    if (e != cudaSuccess) {
+      (void)cudaGetLastError();
+      return set_error(ctx, TC_ERR_OOM, "edge-list CSR buffer of %zu bytes: %s", need, cudaGetErrorString(e));
+    }
+    ctx->aux_cap = need;
+  }
+  int64_t *rowptr = (int64_t *)ctx->aux;
+  int32_t *colidx = (int32_t *)(ctx->aux + align_up(sizeof(int64_t) * (size_t)(n + 1), 256));
+  int64_t nnz = 0;
+  TC_TRY(tc_csr_from_edges(ctx, n, M, src, dst, on_device, rowptr, colidx, 2 * M, &nnz));
+  tc_csr g{n, nnz, rowptr, colidx, 1};
+  return tc_count(ctx, &g, opts, total, nullptr, 0, stats);
+}

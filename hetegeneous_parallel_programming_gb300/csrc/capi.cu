@@ -178,6 +178,7 @@ void tc_ctx_destroy(tc_ctx *ctx) {
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   cudaFree(ctx->arena);
+  cudaFree(ctx->aux);
   cudaFree(ctx->d_total);
   cudaFree(ctx->d_flags);
   cudaFree(ctx->d_heads);

@@ -41,9 +41,11 @@ __device__ __forceinline__ float flog2p1(float x) { return __log2f(1.0f + x); }
 // Fixed degree-threshold selector: the engine's fallback and the judge of the
 // learned one.
 __device__ __forceinline__ int fixed_select(const PlanStats &s) {
-  if (s.nrows <= 8.f && s.maxwin <= (float)BM_BITS && s.mean_db >= 4.f && s.frac >= 0.25f) return TC_ARM_BITMAP;
-  if (s.mean_min >= 48.f && s.mean_max <= 8.f * s.mean_min) return TC_ARM_MERGE_32;
-  if (s.mean_min >= 8.f) return TC_ARM_BSEARCH_32;
+  // Thresholds fitted to per-tile arm costs recorded on R-MAT scale 16-20
+  // graphs (the learned selector's training set).  The bitmap is cleared per
+  // row segment, so it only pays for small id windows.
+  if (s.nrows <= 16.f && s.mean_min >= 128.f && s.maxwin <= 16384.f) return TC_ARM_BITMAP;
+  if (s.mean_min >= 96.f) return TC_ARM_BSEARCH_32;
   return TC_ARM_BSEARCH_4;
 }
 
@@ -273,6 +275,48 @@ __device__ __forceinline__ uint32_t bsearch_count(const int32_t *__restrict__ l,
   return c;
 }
 
+// Same count with K independent binary searches in flight per lane: lane gl
+// takes keys gl + k*G of each G*K-key batch; the K searches advance in
+// lockstep, so their loads issue back to back instead of one dependent chain
+// at a time.  Keys grow along a lane, so the next batch starts its searches
+// at the last key's lower bound.
+template <int G, int K>
+__device__ __forceinline__ uint32_t bsearch_count_ilp(const int32_t *__restrict__ l, int nl,
+                                                      const int32_t *__restrict__ s, int ns, int gl) {
+  uint32_t c = 0;
+  int base = 0;
+  for (int i0 = gl; i0 < nl; i0 += G * K) {
+    int32_t key[K];
+    int lo[K], hi[K];
+    int last = 0;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const int idx = i0 + k * G;
+      const bool act = idx < nl;
+      key[k] = act ? __ldg(l + idx) : INT32_MAX;
+      lo[k] = base;
+      hi[k] = act ? ns : base;  // inactive searches are empty
+      last = act ? k : last;
+    }
+    int width = ns - base;
+    while (width > 0) {  // ceil(log2(width + 1)) rounds bound every search
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        if (lo[k] < hi[k]) {
+          const int mid = (lo[k] + hi[k]) >> 1;
+          if (__ldg(s + mid) < key[k]) lo[k] = mid + 1; else hi[k] = mid;
+        }
+      }
+      width >>= 1;
+    }
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+      if (key[k] != INT32_MAX && lo[k] < ns && __ldg(s + lo[k]) == key[k]) ++c;
+    base = lo[last];
+  }
+  return c;
+}
+
 template <int G>
 __device__ __forceinline__ uint32_t group_sum(uint32_t v, unsigned gmask) {
 #pragma unroll
@@ -310,8 +354,9 @@ __global__ void __launch_bounds__(CT_THREADS) bsearch_kernel(DevDag g, const uin
       const EdgeLists L = edge_lists(g, e, s);
       uint32_t c = 0;
       if (L.na > 0 && L.nb > 0) {
-        if (L.na <= L.nb) c = bsearch_count<G>(L.a, L.na, L.b, L.nb, gl);
-        else c = bsearch_count<G>(L.b, L.nb, L.a, L.na, gl);
+        constexpr int K = G <= 8 ? 4 : 2;  // searches in flight per lane
+        if (L.na <= L.nb) c = bsearch_count_ilp<G, K>(L.a, L.na, L.b, L.nb, gl);
+        else c = bsearch_count_ilp<G, K>(L.b, L.nb, L.a, L.na, gl);
       }
       c = group_sum<G>(c, gm);
       if (gl == 0) {
@@ -374,6 +419,179 @@ __global__ void __launch_bounds__(CT_THREADS) merge_kernel(DevDag g, const uint3
       const EdgeLists L = edge_lists(g, e, s);
       uint32_t c = 0;
       if (L.na > 0 && L.nb > 0) c = merge_count<G>(L.a, L.na, L.b, L.nb, gl, gm);
+      c = group_sum<G>(c, gm);
+      if (gl == 0) {
+        put_edge_count(g, out, e, c);
+        acc += c;
+      }
+    }
+    if (tile_cycles) {
+      __syncthreads();
+      if (threadIdx.x == 0) atomicAdd(&tile_cycles[tile], (unsigned long long)(clock64() - c0));
+    }
+  }
+  flush_total(acc, total);
+}
+
+// ---- GALLOP_G ---------------------------------------------------------------------
+//
+// Lane gl of a G-lane group takes the contiguous run [gl*nl/G, (gl+1)*nl/G)
+// of the shorter list and walks it through the longer list with galloping
+// (exponential then binary) searches, each starting where the previous key
+// landed: O(nl/G * log(ns/nl)) steps, mostly within the cache lines the
+// previous key touched.
+
+// First p in [pos, n) with L[p] >= key (n if none).
+__device__ __forceinline__ int gallop_lb(const int32_t *__restrict__ L, int n, int pos, int32_t key) {
+  if (pos >= n || __ldg(L + pos) >= key) return pos;
+  int lo = pos, step = 1, hi;
+  for (;;) {  // invariant: L[lo] < key
+    hi = lo + step;
+    if (hi >= n) { hi = n; break; }
+    if (__ldg(L + hi) >= key) break;
+    lo = hi;
+    step <<= 1;
+  }
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(L + mid) < key) lo = mid; else hi = mid;
+  }
+  return hi;
+}
+
+template <int G>
+__device__ __forceinline__ uint32_t gallop_count(const int32_t *__restrict__ s, int ns, const int32_t *__restrict__ l,
+                                                 int nl, int gl) {
+  const int k0 = (int)(((long long)gl * ns) / G), k1 = (int)(((long long)(gl + 1) * ns) / G);
+  uint32_t c = 0;
+  if (k0 >= k1) return 0;
+  int pos = 0;
+  // the run's first key: plain binary search over the whole longer list
+  {
+    const int32_t key = __ldg(s + k0);
+    int lo = 0, hi = nl;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (__ldg(l + mid) < key) lo = mid + 1; else hi = mid;
+    }
+    pos = lo;
+    if (pos < nl && __ldg(l + pos) == key) { ++c; ++pos; }
+  }
+  for (int k = k0 + 1; k < k1 && pos < nl; ++k) {
+    const int32_t key = __ldg(s + k);
+    pos = gallop_lb(l, nl, pos, key);
+    if (pos < nl && __ldg(l + pos) == key) { ++c; ++pos; }
+  }
+  return c;
+}
+
+template <int G>
+__global__ void __launch_bounds__(CT_THREADS) gallop_kernel(DevDag g, const uint32_t *__restrict__ qtiles,
+                                                           const int64_t *__restrict__ qoff, int arm, unsigned *head,
+                                                           uint32_t *out, unsigned long long *total,
+                                                           unsigned long long *tile_cycles) {
+  __shared__ int64_t s_tile;
+  const int64_t qb = qoff[arm], qn = qoff[arm + 1] - qb;
+  const int lane = threadIdx.x & 31, gl = threadIdx.x % G, gid = threadIdx.x / G;
+  constexpr int NG = CT_THREADS / G;
+  const unsigned gm = group_mask<G>(lane);
+  unsigned long long acc = 0;
+  for (;;) {
+    const int64_t tile = next_tile(qtiles, qb, qn, head, &s_tile);
+    if (tile < 0) break;
+    const long long c0 = clock64();
+    const int64_t e0 = tile * TILE_EDGES, e1 = min(g.m, e0 + TILE_EDGES);
+    for (int64_t e = e0 + gid; e < e1; e += NG) {
+      int32_t s;
+      const EdgeLists L = edge_lists(g, e, s);
+      uint32_t c = 0;
+      if (L.na > 0 && L.nb > 0) {
+        if (L.na <= L.nb) c = gallop_count<G>(L.a, L.na, L.b, L.nb, gl);
+        else c = gallop_count<G>(L.b, L.nb, L.a, L.na, gl);
+      }
+      c = group_sum<G>(c, gm);
+      if (gl == 0) {
+        put_edge_count(g, out, e, c);
+        acc += c;
+      }
+    }
+    if (tile_cycles) {
+      __syncthreads();
+      if (threadIdx.x == 0) atomicAdd(&tile_cycles[tile], (unsigned long long)(clock64() - c0));
+    }
+  }
+  flush_total(acc, total);
+}
+
+// ---- MPATH_G -----------------------------------------------------------------------
+//
+// Merge-path intersection: the merged order of A and B (A first on ties) is
+// cut into G equal segments; lane gl finds its cut (i, d - i) by a binary
+// search on its diagonal d, then merges its segment sequentially and counts a
+// match when a B element equals the most recent A element (which may lie
+// just before the segment).  Strictly increasing lists make every common
+// element counted exactly once.
+
+// Number of A elements among the first d merged elements.
+__device__ __forceinline__ int mpath_split(const int32_t *__restrict__ A, int na, const int32_t *__restrict__ B, int nb,
+                                           int d) {
+  int lo = max(0, d - nb), hi = min(d, na);
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(A + mid) <= __ldg(B + d - mid - 1)) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+template <int G>
+__device__ __forceinline__ uint32_t mpath_count(const int32_t *__restrict__ A, int na, const int32_t *__restrict__ B,
+                                                int nb, int gl, unsigned gm) {
+  const int total = na + nb;
+  const int d0 = (int)(((long long)gl * total) / G);
+  const int i0 = mpath_split(A, na, B, nb, d0);
+  int i1 = __shfl_down_sync(gm, i0, 1, G);
+  int d1 = __shfl_down_sync(gm, d0, 1, G);
+  if (gl == G - 1) { i1 = na; d1 = total; }
+  const int j0 = d0 - i0, j1 = d1 - i1;
+  int i = i0, j = j0;
+  int32_t last_a = i0 > 0 ? __ldg(A + i0 - 1) : INT32_MIN;
+  uint32_t c = 0;
+  for (int step = d0; step < d1; ++step) {
+    const int32_t av = i < i1 ? __ldg(A + i) : INT32_MAX;
+    const int32_t bv = j < j1 ? __ldg(B + j) : INT32_MAX;
+    const bool take_a = (i < i1) && (j >= j1 || av <= bv);
+    if (take_a) {
+      last_a = av;
+      ++i;
+    } else {
+      c += (bv == last_a) ? 1u : 0u;
+      ++j;
+    }
+  }
+  return c;
+}
+
+template <int G>
+__global__ void __launch_bounds__(CT_THREADS) mpath_kernel(DevDag g, const uint32_t *__restrict__ qtiles,
+                                                          const int64_t *__restrict__ qoff, int arm, unsigned *head,
+                                                          uint32_t *out, unsigned long long *total,
+                                                          unsigned long long *tile_cycles) {
+  __shared__ int64_t s_tile;
+  const int64_t qb = qoff[arm], qn = qoff[arm + 1] - qb;
+  const int lane = threadIdx.x & 31, gl = threadIdx.x % G, gid = threadIdx.x / G;
+  constexpr int NG = CT_THREADS / G;
+  const unsigned gm = group_mask<G>(lane);
+  unsigned long long acc = 0;
+  for (;;) {
+    const int64_t tile = next_tile(qtiles, qb, qn, head, &s_tile);
+    if (tile < 0) break;
+    const long long c0 = clock64();
+    const int64_t e0 = tile * TILE_EDGES, e1 = min(g.m, e0 + TILE_EDGES);
+    for (int64_t e = e0 + gid; e < e1; e += NG) {
+      int32_t s;
+      const EdgeLists L = edge_lists(g, e, s);
+      uint32_t c = 0;
+      if (L.na > 0 && L.nb > 0) c = mpath_count<G>(L.a, L.na, L.b, L.nb, gl, gm);
       c = group_sum<G>(c, gm);
       if (gl == 0) {
         put_edge_count(g, out, e, c);
@@ -620,6 +838,8 @@ static ArmKernel arm_kernel(int arm) {
     case TC_ARM_MERGE_8: return merge_kernel<8>;
     case TC_ARM_MERGE_32: return merge_kernel<32>;
     case TC_ARM_HASH: return hash_kernel;
+    case TC_ARM_GALLOP_4: return gallop_kernel<4>;
+    case TC_ARM_MPATH_4: return mpath_kernel<4>;
     default: return bitmap_kernel;
   }
 }
@@ -675,9 +895,11 @@ tc_status count_carve(const tc_ctx *ctx, int64_t m, Bump &bump, CountBufs &cb, b
   return bump.overflow ? TC_ERR_OOM : TC_OK;
 }
 
-// Pinned host scratch layout used by run_count / count_stats.
-constexpr int PIN_QOFF = 16;   // TC_NUM_ARMS + 1 int64
-constexpr int PIN_BYTES = 24;  // TC_NUM_ARMS uint64
+// Pinned host scratch layout used by run_count / count_stats (64 words).
+constexpr int PIN_QOFF = 16;                           // TC_NUM_ARMS + 1 int64
+constexpr int PIN_BYTES = PIN_QOFF + TC_NUM_ARMS + 1;  // TC_NUM_ARMS uint64
+static_assert(PIN_BYTES + TC_NUM_ARMS <= 64, "pinned scratch holds 64 words");
+static_assert(sizeof(((tc_ctx *)nullptr)->ev) / sizeof(cudaEvent_t) >= 10 + TC_NUM_ARMS, "one event per arm");
 
 tc_status run_count(tc_ctx *ctx, const DevDag &g, const tc_opts &opts, CountBufs &cb, uint32_t *out, bool timing) {
   const int64_t T = (g.m + TILE_EDGES - 1) / TILE_EDGES;

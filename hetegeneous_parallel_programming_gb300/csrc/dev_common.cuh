@@ -20,12 +20,18 @@ struct tc_ctx {
   char *arena = nullptr;
   size_t arena_cap = 0;
   size_t arena_used = 0;
+  // grow-only buffer for a CSR built inside a call (tc_count_edges), kept
+  // apart from the arena that the count then reuses
+  char *aux = nullptr;
+  size_t aux_cap = 0;
   // small always-resident device state
   unsigned long long *d_total = nullptr;  // [1] running total
   unsigned int *d_flags = nullptr;        // [8] error flags / counters
   unsigned int *d_heads = nullptr;        // [64] work-queue heads
   unsigned long long *h_pinned = nullptr; // [64] pinned host scratch
-  cudaEvent_t ev[16] = {};
+  // events: [0..8) entry-point phases, [8] plan start, [9] count start,
+  // [10 + a] end of arm a's kernel
+  cudaEvent_t ev[10 + TC_NUM_ARMS] = {};
   // learned selector
   float *d_mlp = nullptr;                 // TC_MLP_PARAM_COUNT floats
   bool mlp_loaded = false;

@@ -86,7 +86,7 @@ def main():
                      "fixed_arm_share": np.bincount(fx, minlength=tc.TC_NUM_ARMS).tolist(),
                      "per_arm_total": k.sum(0).tolist()})
     np.savez(out / "selector_mlp.npz", params=w.astype(np.float32))
-    info = {"architecture": "16 -> 64 -> 64 -> 6, ReLU; bf16 weights at inference, fp32 accumulate",
+    info = {"architecture": f"16 -> 64 -> 64 -> {tc.TC_NUM_ARMS}, ReLU; bf16 weights at inference, fp32 accumulate",
             "loss": loss, "epochs": args.epochs, "lr": args.lr, "rows": int(len(X)),
             "profile_seconds": round(t_prof, 1), "train_seconds": round(t_train, 2),
             "train_regret": train_regret, "held_out": held, "graphs": meta,

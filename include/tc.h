@@ -67,7 +67,9 @@ typedef enum tc_arm {
   TC_ARM_MERGE_32 = 3,     /* 32-lane windowed merge-path                     */
   TC_ARM_HASH = 4,         /* warp hash of the row's out-list, flattened probes */
   TC_ARM_BITMAP = 5,       /* block bitmap of the row's id window + probes    */
-  TC_NUM_ARMS = 6
+  TC_ARM_GALLOP_4 = 6,     /* 4 lanes per edge, each gallops a run of keys    */
+  TC_ARM_MPATH_4 = 7,      /* 4 lanes per edge split the merge path evenly    */
+  TC_NUM_ARMS = 8
 } tc_arm;
 
 typedef enum tc_selector {
@@ -232,6 +234,15 @@ tc_status tc_selector_grad(tc_ctx *ctx, const float *params, const float *featur
 tc_status tc_csr_from_edges(tc_ctx *ctx, int64_t n, int64_t num_edges, const int32_t *src,
                             const int32_t *dst, int32_t on_device, int64_t *rowptr,
                             int32_t *colidx, int64_t capacity, int64_t *nnz_out);
+
+/* Count the triangles of an undirected edge list (COO; duplicates, both
+ * directions and self loops allowed), the reference's edge-list input form
+ * (Graph::init_edgelist, successful_push_pull/graph.cc:316-345): the list is
+ * symmetrised and deduplicated on the device (tc_csr_from_edges), then
+ * oriented and counted as tc_count does.  src/dst host or device per
+ * on_device; *total is overwritten. */
+tc_status tc_count_edges(tc_ctx *ctx, int64_t n, int64_t num_edges, const int32_t *src, const int32_t *dst,
+                         int32_t on_device, const tc_opts *opts, uint64_t *total, tc_stats *stats);
 
 /* Seeded generators (counter-based RNG, identical on host and device). */
 typedef enum tc_gen_kind { TC_GEN_ER = 0, TC_GEN_RMAT = 1, TC_GEN_RGG = 2, TC_GEN_CHUNG_LU = 3 } tc_gen_kind;

@@ -93,6 +93,16 @@ def test_device_csr_builder_matches_oracle(engine):
         assert np.array_equal(r1, r2) and np.array_equal(c1, c2)
 
 
+def test_edge_list_entry_path(engine, golden):
+    for case in golden:
+        e = np.array(case["edges"], np.int64).reshape(-1, 2)
+        total, st = engine.count_edges(case["n"], e[:, 0], e[:, 1])
+        assert total == case["triangles"], case["name"]
+    n, s, d = tc.gen_edges_host(tc.GenSpec("rmat", scale=14, edge_factor=16, seed=8))
+    total, _ = engine.count_edges(n, s, d)
+    assert total == oracle.triangles(*oracle.csr_from_edges(n, s, d))
+
+
 def test_device_pointers_path(engine):
     import torch
     rowptr, colidx = gen_csr(tc.GenSpec("rmat", scale=13, edge_factor=16, seed=3))
