@@ -69,7 +69,7 @@ void orient_sizes(const tc_ctx *ctx, int64_t n, int64_t nnz, bool perm, bool dag
   scr = std::max(scr, scan_scratch_bytes(ctx, G));
   sz.take<char>((int64_t)scr);
   sz.take<int64_t>(n + 1); sz.take<int64_t>(n + 1); sz.take<int64_t>(n + 1);
-  sz.take<int32_t>(n); sz.take<int32_t>(n); sz.take<unsigned>(2);
+  sz.take<int32_t>(n); sz.take<int32_t>(n); sz.take<int32_t>(n); sz.take<unsigned>(3);
   sz.take<int32_t>(mmax); sz.take<int32_t>(mmax);
   if (perm) sz.take<uint32_t>(mmax);
   if (dagcol) sz.take<int32_t>(mmax);
@@ -92,8 +92,9 @@ void orient_carve(const tc_ctx *ctx, int64_t n, int64_t nnz, bool perm, bool dag
   b.nrowptr = bump.take<int64_t>(n + 1);
   b.dnew = bump.take<int64_t>(n + 1);
   b.mid_list = bump.take<int32_t>(n);
+  b.big_list = bump.take<int32_t>(n);
   b.huge_list = bump.take<int32_t>(n);
-  b.seg_counts = bump.take<unsigned>(2);
+  b.seg_counts = bump.take<unsigned>(3);
   b.ncol = bump.take<int32_t>(mmax);
   b.nsrc = bump.take<int32_t>(mmax);
   b.perm = perm ? bump.take<uint32_t>(mmax) : nullptr;
@@ -114,7 +115,9 @@ float elapsed(cudaEvent_t a, cudaEvent_t b) {
 tc_status orient_front(tc_ctx *ctx, const DevCSR &d, const tc_opts &o, OrientBufs &ob, int64_t *m,
                               float *ms_validate, float *ms_a) {
   TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[1], ctx->stream));
-  if (o.validate) TC_TRY(launch_validate(ctx, d, true));
+  // row pointers here; the column checks ride on the kept-count pass
+  if (o.validate) TC_TRY(launch_validate_rowptr(ctx, d));
+  ob.validate = o.validate != 0;
   TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
   TC_TRY(orient_phase_a(ctx, d, ob));
   TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[3], ctx->stream));

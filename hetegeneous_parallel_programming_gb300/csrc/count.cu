@@ -44,8 +44,8 @@ __device__ __forceinline__ int fixed_select(const PlanStats &s) {
   // Thresholds fitted to per-tile arm costs recorded on R-MAT scale 16-20
   // graphs (the learned selector's training set).  The bitmap is cleared per
   // row segment, so it only pays for small id windows.
-  if (s.nrows <= 16.f && s.mean_min >= 128.f && s.maxwin <= 16384.f) return TC_ARM_BITMAP;
-  if (s.mean_min >= 96.f) return TC_ARM_BSEARCH_32;
+  if (s.nrows <= 16.f && s.mean_min >= 64.f && s.maxwin <= 16384.f) return TC_ARM_BITMAP;
+  if (s.mean_min >= 64.f) return TC_ARM_BSEARCH_32;
   return TC_ARM_BSEARCH_4;
 }
 
@@ -354,9 +354,15 @@ __global__ void __launch_bounds__(CT_THREADS) bsearch_kernel(DevDag g, const uin
       const EdgeLists L = edge_lists(g, e, s);
       uint32_t c = 0;
       if (L.na > 0 && L.nb > 0) {
-        constexpr int K = G <= 8 ? 4 : 2;  // searches in flight per lane
-        if (L.na <= L.nb) c = bsearch_count_ilp<G, K>(L.a, L.na, L.b, L.nb, gl);
-        else c = bsearch_count_ilp<G, K>(L.b, L.nb, L.a, L.na, gl);
+        // narrow groups keep 4 searches in flight per lane; a full warp per
+        // edge already has 32 in flight and runs them one at a time
+        if (G <= 8) {
+          if (L.na <= L.nb) c = bsearch_count_ilp<G, 4>(L.a, L.na, L.b, L.nb, gl);
+          else c = bsearch_count_ilp<G, 4>(L.b, L.nb, L.a, L.na, gl);
+        } else {
+          if (L.na <= L.nb) c = bsearch_count<G>(L.a, L.na, L.b, L.nb, gl);
+          else c = bsearch_count<G>(L.b, L.nb, L.a, L.na, gl);
+        }
       }
       c = group_sum<G>(c, gm);
       if (gl == 0) {
@@ -606,6 +612,127 @@ __global__ void __launch_bounds__(CT_THREADS) mpath_kernel(DevDag g, const uint3
   flush_total(acc, total);
 }
 
+// ---- FLAT (warp-level, flattened binary searches) -----------------------------------
+//
+// A warp owns a 512-edge sub-tile and takes 32 edges at a time: lane i loads
+// edge i's lists (the shorter one is the lookup list) and the warp walks the
+// concatenation of the 32 lookup lists, lane p searching element p of it in
+// its edge's longer list, FL_K searches in flight per lane.  Short and long
+// lookups share the lanes evenly; a lane's successive keys in one edge grow,
+// so each search starts at the lane's previous lower bound in that edge.
+
+constexpr int FL_THREADS = 256;
+constexpr int FL_WARPS = FL_THREADS / 32;
+constexpr int FL_K = 4;
+constexpr int FL_SUB = TILE_EDGES / 8;  // edges per warp work item
+
+__global__ void __launch_bounds__(FL_THREADS) flat_kernel(DevDag g, const uint32_t *__restrict__ qtiles,
+                                                         const int64_t *__restrict__ qoff, int arm, unsigned *head,
+                                                         uint32_t *out, unsigned long long *total,
+                                                         unsigned long long *tile_cycles) {
+  __shared__ int32_t s_incl[FL_WARPS][32];
+  __shared__ long long s_lbase[FL_WARPS][32];  // lookup list start minus its first flattened index
+  __shared__ long long s_sbase[FL_WARPS][32];  // search list start
+  __shared__ int32_t s_slen[FL_WARPS][32];
+  __shared__ uint32_t s_hits[FL_WARPS][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t qb = qoff[arm], qn = qoff[arm + 1] - qb;
+  const int64_t items = qn * (TILE_EDGES / FL_SUB);
+  unsigned long long acc = 0;
+  for (;;) {
+    unsigned it = 0;
+    if (lane == 0) it = atomicAdd(head, 1u);
+    it = __shfl_sync(TC_FULL_MASK, it, 0);
+    if ((int64_t)it >= items) break;
+    const int64_t tile = qtiles[qb + it / (TILE_EDGES / FL_SUB)];
+    const int64_t e0 = tile * TILE_EDGES + (int64_t)(it % (TILE_EDGES / FL_SUB)) * FL_SUB;
+    const int64_t e1 = min(g.m, e0 + FL_SUB);
+    const long long c0 = clock64();
+    for (int64_t eb = e0; eb < e1; eb += 32) {
+      const int64_t ei = eb + lane;
+      int nl = 0, ns = 0;
+      long long lb = 0, sb = 0;
+      if (ei < e1) {
+        int32_t s;
+        const EdgeLists L = edge_lists(g, ei, s);
+        if (L.na > 0 && L.nb > 0) {
+          const bool a_short = L.na <= L.nb;
+          nl = a_short ? L.na : L.nb;
+          ns = a_short ? L.nb : L.na;
+          lb = (a_short ? L.a : L.b) - g.col;
+          sb = (a_short ? L.b : L.a) - g.col;
+        }
+      }
+      int incl = nl;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(TC_FULL_MASK, incl, o);
+        if (lane >= o) incl += y;
+      }
+      const int P = __shfl_sync(TC_FULL_MASK, incl, 31);
+      s_incl[w][lane] = incl;
+      s_lbase[w][lane] = lb - (long long)(incl - nl);
+      s_sbase[w][lane] = sb;
+      s_slen[w][lane] = ns;
+      s_hits[w][lane] = 0u;
+      __syncwarp();
+      int cur = 0;          // edge of the lane's current key
+      int lo_edge = -1;     // edge whose lower bound prev_lo is (last finished search)
+      int prev_lo = 0;
+      for (int p0 = lane; p0 < P; p0 += 32 * FL_K) {
+        int32_t key[FL_K];
+        int lo[FL_K], hi[FL_K], ed[FL_K];
+        long long sbase[FL_K];
+        int width = 0;
+#pragma unroll
+        for (int k = 0; k < FL_K; ++k) {
+          const int p = p0 + 32 * k;
+          ed[k] = -1;
+          lo[k] = hi[k] = 0;
+          key[k] = 0;
+          sbase[k] = 0;
+          if (p < P) {
+            while (s_incl[w][cur] <= p) ++cur;
+            ed[k] = cur;
+            key[k] = __ldg(g.col + s_lbase[w][cur] + p);
+            sbase[k] = s_sbase[w][cur];
+            hi[k] = s_slen[w][cur];
+            lo[k] = (cur == lo_edge) ? prev_lo : 0;
+            width = max(width, hi[k] - lo[k]);
+          }
+        }
+        while (width > 0) {
+#pragma unroll
+          for (int k = 0; k < FL_K; ++k) {
+            if (lo[k] < hi[k]) {
+              const int mid = (lo[k] + hi[k]) >> 1;
+              if (__ldg(g.col + sbase[k] + mid) < key[k]) lo[k] = mid + 1; else hi[k] = mid;
+            }
+          }
+          width >>= 1;
+        }
+#pragma unroll
+        for (int k = 0; k < FL_K; ++k) {
+          if (ed[k] >= 0) {
+            if (lo[k] < s_slen[w][ed[k]] && __ldg(g.col + sbase[k] + lo[k]) == key[k]) atomicAdd(&s_hits[w][ed[k]], 1u);
+            prev_lo = lo[k];  // keys grow along the lane: a valid start for its next key in this edge
+            lo_edge = ed[k];
+          }
+        }
+      }
+      __syncwarp();
+      if (ei < e1) {
+        const uint32_t c = s_hits[w][lane];
+        put_edge_count(g, out, ei, c);
+        acc += c;
+      }
+      __syncwarp();
+    }
+    if (tile_cycles && lane == 0) atomicAdd(&tile_cycles[tile], (unsigned long long)(clock64() - c0));
+  }
+  flush_total(acc, total);
+}
+
 // ---- HASH (warp-level, row-staged) ---------------------------------------------------
 //
 // A warp owns a 512-edge sub-tile pulled from the arm's queue.  For every
@@ -840,6 +967,7 @@ static ArmKernel arm_kernel(int arm) {
     case TC_ARM_HASH: return hash_kernel;
     case TC_ARM_GALLOP_4: return gallop_kernel<4>;
     case TC_ARM_MPATH_4: return mpath_kernel<4>;
+    case TC_ARM_FLAT: return flat_kernel;
     default: return bitmap_kernel;
   }
 }
@@ -857,7 +985,8 @@ tc_status init_arm_occupancy(tc_ctx *ctx) {
     TC_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, arm_kernel(a), arm_threads(a), arm_smem(a)));
     ctx->arm_blocks_per_sm[a] = nb > 0 ? nb : 1;
     // independent workers per SM: warps for the warp-level HASH arm, blocks otherwise
-    ctx->arm_units_per_sm[a] = ctx->arm_blocks_per_sm[a] * (a == TC_ARM_HASH ? HT_WARPS : 1);
+    const bool warp_items = a == TC_ARM_HASH || a == TC_ARM_FLAT;
+    ctx->arm_units_per_sm[a] = ctx->arm_blocks_per_sm[a] * (warp_items ? HT_WARPS : 1);
   }
   return TC_OK;
 }
@@ -921,7 +1050,10 @@ tc_status run_count(tc_ctx *ctx, const DevDag &g, const tc_opts &opts, CountBufs
   }
   uint64_t *sk = cb.qkeys0;
   uint32_t *sv = cb.qvals0;
-  if (T > 1) TC_TRY(radix_sort(ctx, cb.qkeys0, cb.qkeys1, cb.qvals0, cb.qvals1, T, 0, 43, cb.sort_scratch, &sk, &sv));
+  constexpr int ARM_BITS = 4;  // queue key = (arm << 40) | inverted work
+  static_assert(TC_NUM_ARMS <= (1 << ARM_BITS), "arm field of the queue key");
+  if (T > 1)
+    TC_TRY(radix_sort(ctx, cb.qkeys0, cb.qkeys1, cb.qvals0, cb.qvals1, T, 0, 40 + ARM_BITS, cb.sort_scratch, &sk, &sv));
   if (T > 0) {
     qoff_kernel<<<1, 32, 0, ctx->stream>>>(sk, T, cb.qoff);
     TC_CHECK_LAUNCH(ctx);

@@ -38,6 +38,7 @@ struct DevDag {
 
 // Validation: sets VF_* bits in ctx->d_flags[0].
 tc_status launch_validate(tc_ctx *ctx, const DevCSR &g, bool require_sorted_simple);
+tc_status launch_validate_rowptr(tc_ctx *ctx, const DevCSR &g);
 
 // Orientation.  Phase A (before the host learns m): degree keys, rank sort,
 // kept counts per row and per block.  Phase B: compaction + relabel sort.
@@ -52,8 +53,8 @@ struct OrientBufs {
   int64_t *orowptr;            // [n+1] original-order DAG row pointers
   int64_t *nrowptr;            // [n+1] relabelled row pointers
   int64_t *dnew;               // [n+1] relabelled row lengths
-  int32_t *mid_list, *huge_list;  // [n] rows for the block sorts
-  unsigned *seg_counts;        // [2]
+  int32_t *mid_list, *big_list, *huge_list;  // [n] rows for the warp / block / global sorts
+  unsigned *seg_counts;        // [3]
   // phase B
   int32_t *ncol, *nsrc;        // [m]
   uint32_t *perm;              // [m] original slot of each relabelled edge (optional)
@@ -64,6 +65,8 @@ struct OrientBufs {
   // id), so every group owns the contiguous rank range of its vertices.
   const int32_t *vgroup = nullptr;
   int group_bits = 0;
+  // check ids, sortedness and self loops inside the kept-count pass
+  bool validate = false;
 };
 void orient_geometry(const tc_ctx *ctx, int64_t nnz, int *G, int64_t *chunk);
 tc_status orient_phase_a(tc_ctx *ctx, const DevCSR &g, OrientBufs &b);

@@ -71,10 +71,15 @@ __global__ void __launch_bounds__(OR_THREADS) validate_col_kernel(const int64_t 
   if ((threadIdx.x & 31) == 0 && f) atomicOr(flags, f);
 }
 
-tc_status launch_validate(tc_ctx *ctx, const DevCSR &g, bool simple) {
+tc_status launch_validate_rowptr(tc_ctx *ctx, const DevCSR &g) {
   validate_rowptr_kernel<<<grid_for(ctx, g.n + 1, 256, 8), 256, 0, ctx->stream>>>(g.rowptr, g.n, g.nnz,
                                                                                   ctx->d_flags);
   TC_CHECK_LAUNCH(ctx);
+  return TC_OK;
+}
+
+tc_status launch_validate(tc_ctx *ctx, const DevCSR &g, bool simple) {
+  TC_TRY(launch_validate_rowptr(ctx, g));
   if (g.nnz > 0) {
     validate_col_kernel<<<grid_for(ctx, g.nnz, ENTRY_TILE, 8), OR_THREADS, 0, ctx->stream>>>(
         g.rowptr, g.col, g.n, g.nnz, simple ? 1 : 0, ctx->d_flags);
@@ -103,18 +108,23 @@ __global__ void rank_kernel(const uint64_t *__restrict__ keys, int64_t n, uint64
 }
 
 // Kept entries per original row (warp-aggregated atomics) and per block chunk.
+// With VALIDATE it also performs validate_col_kernel's checks on the same
+// pass over the adjacency (ids in range, rows strictly ascending, no self
+// loops), so a validated call reads colidx once here instead of twice.
+template <bool VALIDATE>
 __global__ void __launch_bounds__(OR_THREADS) kept_count_kernel(const int64_t *__restrict__ rowptr,
                                                                const int32_t *__restrict__ col, int64_t n,
                                                                int64_t nnz, int64_t chunk,
                                                                const int32_t *__restrict__ rank,
                                                                unsigned long long *__restrict__ kept,
-                                                               int64_t *__restrict__ bcount) {
+                                                               int64_t *__restrict__ bcount, unsigned *flags) {
   __shared__ int rows[ENTRY_TILE];
   __shared__ int scan_tmp[32];
   __shared__ unsigned long long bsum;
   if (threadIdx.x == 0) bsum = 0;
   const int64_t b = (int64_t)blockIdx.x * chunk, e_end = min(nnz, b + chunk);
   unsigned long long mine = 0;
+  unsigned f = 0;
   const int lane = threadIdx.x & 31;
   for (int64_t t0 = b; t0 < e_end; t0 += ENTRY_TILE) {
     const int64_t t1 = min(e_end, t0 + ENTRY_TILE);
@@ -128,6 +138,11 @@ __global__ void __launch_bounds__(OR_THREADS) kept_count_kernel(const int64_t *_
         u = rows[e - t0];
         const int32_t v = col[e];
         keep = u >= 0 && v >= 0 && (int64_t)v < n && rank[v] > rank[u];
+        if (VALIDATE) {
+          if (v < 0 || (int64_t)v >= n) f |= VF_ID_RANGE;
+          else if (u == v) f |= VF_SELF_LOOP;
+          if (u >= 0 && u < n && e > 0 && e > rowptr[u] && col[e - 1] >= v) f |= VF_UNSORTED;
+        }
       }
       const unsigned km = __ballot_sync(TC_FULL_MASK, keep);
       if (keep) {
@@ -140,6 +155,10 @@ __global__ void __launch_bounds__(OR_THREADS) kept_count_kernel(const int64_t *_
   }
   mine = warp_sum(mine);
   if (lane == 0 && mine) atomicAdd(&bsum, mine);
+  if (VALIDATE) {
+    f = __reduce_or_sync(TC_FULL_MASK, f);
+    if (lane == 0 && f) atomicOr(flags, f);
+  }
   __syncthreads();
   if (threadIdx.x == 0) bcount[blockIdx.x] = (int64_t)bsum;
 }
@@ -152,27 +171,34 @@ __global__ void dnew_kernel(const int64_t *__restrict__ kept, const int32_t *__r
   if (blockIdx.x == 0 && threadIdx.x == 0) dnew[n] = 0;
 }
 
-// Rows of the relabelled DAG longer than a warp go to the block sorts: the
-// shared-memory sort up to SEG_SMEM_MAX entries, the in-place global one
-// beyond.  Lists are filled with warp-aggregated atomics (order irrelevant).
+// Rows of the relabelled DAG longer than a warp's registers go to list-driven
+// sorts: up to SEG_WARP_MAX entries one warp in its own shared-memory slice,
+// up to SEG_SMEM_MAX one block in shared memory, beyond that one block in
+// place in global memory.  Lists are filled with warp-aggregated atomics
+// (their order is irrelevant).
+constexpr int SEG_WARP_MAX = 256;
 constexpr int SEG_SMEM_MAX = 4096;
 
 __global__ void classify_rows_kernel(const int64_t *__restrict__ len, int64_t n, int32_t *__restrict__ mid_list,
-                                     int32_t *__restrict__ huge_list, unsigned *counts) {
+                                     int32_t *__restrict__ big_list, int32_t *__restrict__ huge_list,
+                                     unsigned *counts) {
   const int lane = threadIdx.x & 31;
   const unsigned lt = lanemask_lt();
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
     const int64_t r = base + threadIdx.x;
     const int64_t L = r < n ? len[r] : 0;
 #pragma unroll
-    for (int cls = 0; cls < 2; ++cls) {
-      const bool mine = cls == 0 ? (L > 32 && L <= SEG_SMEM_MAX) : (L > SEG_SMEM_MAX);
+    for (int cls = 0; cls < 3; ++cls) {
+      const bool mine = cls == 0   ? (L > 32 && L <= SEG_WARP_MAX)
+                        : cls == 1 ? (L > SEG_WARP_MAX && L <= SEG_SMEM_MAX)
+                                   : (L > SEG_SMEM_MAX);
       const unsigned bal = __ballot_sync(TC_FULL_MASK, mine);
       if (!bal) continue;
       unsigned at = 0;
       if (lane == 0) at = atomicAdd(&counts[cls], (unsigned)__popc(bal));
       at = __shfl_sync(TC_FULL_MASK, at, 0);
-      if (mine) (cls == 0 ? mid_list : huge_list)[at + __popc(bal & lt)] = (int32_t)r;
+      int32_t *list = cls == 0 ? mid_list : cls == 1 ? big_list : huge_list;
+      if (mine) list[at + __popc(bal & lt)] = (int32_t)r;
     }
   }
 }
@@ -193,8 +219,14 @@ tc_status orient_phase_a(tc_ctx *ctx, const DevCSR &g, OrientBufs &b) {
   TC_CHECK_LAUNCH(ctx);
   TC_CHECK_CUDA(ctx, cudaMemsetAsync(b.kept, 0, sizeof(int64_t) * (size_t)(g.n + 1), ctx->stream));
   if (g.nnz > 0) {
-    kept_count_kernel<<<b.G, OR_THREADS, 0, ctx->stream>>>(g.rowptr, g.col, g.n, g.nnz, b.chunk, b.rank,
-                                                           (unsigned long long *)b.kept, b.bcount);
+    if (b.validate)
+      kept_count_kernel<true><<<b.G, OR_THREADS, 0, ctx->stream>>>(g.rowptr, g.col, g.n, g.nnz, b.chunk, b.rank,
+                                                                   (unsigned long long *)b.kept, b.bcount,
+                                                                   ctx->d_flags);
+    else
+      kept_count_kernel<false><<<b.G, OR_THREADS, 0, ctx->stream>>>(g.rowptr, g.col, g.n, g.nnz, b.chunk, b.rank,
+                                                                    (unsigned long long *)b.kept, b.bcount,
+                                                                    ctx->d_flags);
     TC_CHECK_LAUNCH(ctx);
     TC_TRY(exclusive_scan_i64(ctx, b.bcount, b.bcount, b.G, b.sort_scratch, b.d_m));
   } else {
@@ -205,9 +237,9 @@ tc_status orient_phase_a(tc_ctx *ctx, const DevCSR &g, OrientBufs &b) {
   dnew_kernel<<<grid_for(ctx, g.n, 256, 8), 256, 0, ctx->stream>>>(b.kept, b.rank, g.n, b.dnew);
   TC_CHECK_LAUNCH(ctx);
   TC_TRY(exclusive_scan_i64(ctx, b.dnew, b.nrowptr, g.n + 1, b.sort_scratch, nullptr));
-  TC_CHECK_CUDA(ctx, cudaMemsetAsync(b.seg_counts, 0, sizeof(unsigned) * 2, ctx->stream));
-  classify_rows_kernel<<<grid_for(ctx, g.n, 256, 8), 256, 0, ctx->stream>>>(b.dnew, g.n, b.mid_list, b.huge_list,
-                                                                            b.seg_counts);
+  TC_CHECK_CUDA(ctx, cudaMemsetAsync(b.seg_counts, 0, sizeof(unsigned) * 3, ctx->stream));
+  classify_rows_kernel<<<grid_for(ctx, g.n, 256, 8), 256, 0, ctx->stream>>>(b.dnew, g.n, b.mid_list, b.big_list,
+                                                                            b.huge_list, b.seg_counts);
   TC_CHECK_LAUNCH(ctx);
   return TC_OK;
 }
@@ -345,6 +377,55 @@ __global__ void seg_sort_warp_kernel(const int64_t *__restrict__ nrowptr, int64_
   }
 }
 
+// Rows of 33..SEG_WARP_MAX entries: one warp per row sorts in its own slice
+// of shared memory with the same flip network, synchronising with __syncwarp.
+template <bool VALS>
+__global__ void __launch_bounds__(256) seg_sort_warpsmem_kernel(const int64_t *__restrict__ nrowptr,
+                                                               const int32_t *__restrict__ list,
+                                                               const unsigned *count, int32_t *__restrict__ ncol,
+                                                               uint32_t *__restrict__ perm) {
+  __shared__ int32_t skey_all[8][SEG_WARP_MAX];
+  __shared__ uint32_t sval_all[VALS ? 8 : 1][VALS ? SEG_WARP_MAX : 1];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int32_t *key = skey_all[w];
+  uint32_t *val = VALS ? sval_all[w] : nullptr;
+  const unsigned cnt = *count;
+  const unsigned warps = gridDim.x * (blockDim.x >> 5);
+  for (unsigned i = blockIdx.x * (blockDim.x >> 5) + w; i < cnt; i += warps) {
+    const int32_t r = list[i];
+    const int64_t b = nrowptr[r];
+    const int L = (int)(nrowptr[r + 1] - b);
+    for (int k = lane; k < L; k += 32) {
+      key[k] = ncol[b + k];
+      if (VALS) val[k] = perm[b + k];
+    }
+    __syncwarp();
+    int P = 1;
+    while (P < L) P <<= 1;
+    for (int k = 2; k <= P; k <<= 1) {
+      const int h = k >> 1;
+      for (int t = lane; t < P / 2; t += 32) {
+        const int blk = t / h, off = t % h;
+        const int a = blk * k + off, bb = blk * k + k - 1 - off;
+        if (bb < L) cmp_swap<VALS>(key, val, a, bb);
+      }
+      __syncwarp();
+      for (int j = k >> 2; j >= 1; j >>= 1) {
+        for (int t = lane; t < P / 2; t += 32) {
+          const int a = (t / j) * 2 * j + (t % j), bb = a + j;
+          if (bb < L) cmp_swap<VALS>(key, val, a, bb);
+        }
+        __syncwarp();
+      }
+    }
+    for (int k = lane; k < L; k += 32) {
+      ncol[b + k] = key[k];
+      if (VALS) perm[b + k] = val[k];
+    }
+    __syncwarp();
+  }
+}
+
 template <bool VALS>
 __global__ void __launch_bounds__(256) seg_sort_smem_kernel(const int64_t *__restrict__ nrowptr,
                                                            const int32_t *__restrict__ list, const unsigned *count,
@@ -384,6 +465,25 @@ __global__ void __launch_bounds__(1024) seg_sort_global_kernel(const int64_t *__
   }
 }
 
+// Sorts every relabelled row by target rank: rows of <= 32 entries in
+// registers, then the three list-driven classes.
+template <bool VALS>
+static tc_status launch_row_sorts(tc_ctx *ctx, const DevCSR &g, OrientBufs &b) {
+  uint32_t *pv = VALS ? b.perm : nullptr;
+  seg_sort_warp_kernel<VALS><<<grid_for(ctx, g.n * 32, 256, 8), 256, 0, ctx->stream>>>(b.nrowptr, g.n, b.ncol, pv);
+  TC_CHECK_LAUNCH(ctx);
+  seg_sort_warpsmem_kernel<VALS><<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(b.nrowptr, b.mid_list, b.seg_counts,
+                                                                            b.ncol, pv);
+  TC_CHECK_LAUNCH(ctx);
+  seg_sort_smem_kernel<VALS><<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(b.nrowptr, b.big_list, b.seg_counts + 1,
+                                                                        b.ncol, pv);
+  TC_CHECK_LAUNCH(ctx);
+  seg_sort_global_kernel<VALS><<<ctx->num_sms, 1024, 0, ctx->stream>>>(b.nrowptr, b.huge_list, b.seg_counts + 2,
+                                                                       b.ncol, pv);
+  TC_CHECK_LAUNCH(ctx);
+  return TC_OK;
+}
+
 tc_status orient_phase_b(tc_ctx *ctx, const DevCSR &g, OrientBufs &b, int64_t m, bool want_perm, bool want_dag_cols,
                          DevDag *out) {
   const bool relabel = out != nullptr;
@@ -400,28 +500,7 @@ tc_status orient_phase_b(tc_ctx *ctx, const DevCSR &g, OrientBufs &b, int64_t m,
     TC_CHECK_LAUNCH(ctx);
   }
   if (!relabel) return TC_OK;
-  if (m > 1) {
-    const int wgrid = grid_for(ctx, g.n * 32, 256, 8);
-    const int mgrid = ctx->num_sms * 8;
-    if (want_perm) {
-      seg_sort_warp_kernel<true><<<wgrid, 256, 0, ctx->stream>>>(b.nrowptr, g.n, b.ncol, b.perm);
-      TC_CHECK_LAUNCH(ctx);
-      seg_sort_smem_kernel<true><<<mgrid, 256, 0, ctx->stream>>>(b.nrowptr, b.mid_list, b.seg_counts, b.ncol, b.perm);
-      TC_CHECK_LAUNCH(ctx);
-      seg_sort_global_kernel<true><<<ctx->num_sms, 1024, 0, ctx->stream>>>(b.nrowptr, b.huge_list, b.seg_counts + 1,
-                                                                            b.ncol, b.perm);
-      TC_CHECK_LAUNCH(ctx);
-    } else {
-      seg_sort_warp_kernel<false><<<wgrid, 256, 0, ctx->stream>>>(b.nrowptr, g.n, b.ncol, nullptr);
-      TC_CHECK_LAUNCH(ctx);
-      seg_sort_smem_kernel<false><<<mgrid, 256, 0, ctx->stream>>>(b.nrowptr, b.mid_list, b.seg_counts, b.ncol,
-                                                                  nullptr);
-      TC_CHECK_LAUNCH(ctx);
-      seg_sort_global_kernel<false><<<ctx->num_sms, 1024, 0, ctx->stream>>>(b.nrowptr, b.huge_list,
-                                                                             b.seg_counts + 1, b.ncol, nullptr);
-      TC_CHECK_LAUNCH(ctx);
-    }
-  }
+  if (m > 1) TC_TRY(want_perm ? launch_row_sorts<true>(ctx, g, b) : launch_row_sorts<false>(ctx, g, b));
   TC_TRY(launch_expand_src(ctx, b.nrowptr, g.n, m, b.nsrc));
   out->n = g.n;
   out->m = m;

@@ -72,7 +72,9 @@ def main():
     pred = eng.selector_predict(X)
     train_regret = {"learned": regret(Y, pred.argmin(1)), "fixed": regret(Y, np.concatenate(fixed))}
     held = []
-    for scale, seed in [(20, 5), (21, 6), (22, 7)]:
+    # held out: other seeds and larger scales, and the benchmark graph itself
+    # (R-MAT scale 24, seed 0), none of them seen in training
+    for scale, seed in [(20, 5), (21, 6), (22, 7), (24, 0)]:
         r, cidx = rmat_graph(eng, scale, 0.57, 0.19, 0.19, seed=seed)
         f, k = eng.tile_profile(r, cidx)
         learned = eng.plan_arms(r, cidx, selector="learned")

@@ -69,7 +69,8 @@ typedef enum tc_arm {
   TC_ARM_BITMAP = 5,       /* block bitmap of the row's id window + probes    */
   TC_ARM_GALLOP_4 = 6,     /* 4 lanes per edge, each gallops a run of keys    */
   TC_ARM_MPATH_4 = 7,      /* 4 lanes per edge split the merge path evenly    */
-  TC_NUM_ARMS = 8
+  TC_ARM_FLAT = 8,         /* warp walks 32 edges' lookup lists as one run    */
+  TC_NUM_ARMS = 9
 } tc_arm;
 
 typedef enum tc_selector {

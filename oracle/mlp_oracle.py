@@ -1,7 +1,7 @@
 """numpy restatement of the selector MLP — TEST INFRASTRUCTURE ONLY.
 
 Same parameter layout, forward pass and loss as the device kernels
-(16 -> 64 -> 64 -> 8, ReLU; loss = sum of 0.5*(y - t)^2 / (rows*arms)),
+(16 -> 64 -> 64 -> one output per arm, ReLU; loss = sum of 0.5*(y - t)^2 / (rows*arms)),
 with the backward pass derived by hand; tests compare the device gradients
 against these.
 """
@@ -9,7 +9,7 @@ from __future__ import annotations
 
 import numpy as np
 
-F, H, K = 16, 64, 8
+F, H, K = 16, 64, 9
 P = F * H + H + H * H + H + H * K + K
 
 

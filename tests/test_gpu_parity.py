@@ -93,6 +93,37 @@ def test_device_csr_builder_matches_oracle(engine):
         assert np.array_equal(r1, r2) and np.array_equal(c1, c2)
 
 
+def test_long_rows_every_sort_class(engine):
+    """A clique of 4300 vertices, vertex i with i % 5 pendant neighbours: the
+    degree ranks differ from the ids, relabelled rows reach 4299 entries (the
+    in-place global row sort), and the answers are analytic: C(k,3)
+    triangles; edge u->v inside the clique closes one triangle with every
+    clique vertex ranked above v."""
+    k = 4300
+    iu, ju = np.triu_indices(k, 1)
+    pend_owner = np.repeat(np.arange(k), np.arange(k) % 5)
+    pend = k + np.arange(len(pend_owner))
+    src = np.concatenate([iu, pend_owner]).astype(np.int32)
+    dst = np.concatenate([ju, pend]).astype(np.int32)
+    n = k + len(pend)
+    rowptr, colidx = engine.csr_from_edges(n, src, dst)
+    expect = k * (k - 1) * (k - 2) // 6
+    deg = np.diff(rowptr)
+    rank_order = np.lexsort((np.arange(n), deg))
+    rank = np.empty(n, np.int64)
+    rank[rank_order] = np.arange(n)
+    clique_by_rank = np.sort(rank[:k])  # ranks of the clique vertices, ascending
+    above = k - 1 - np.searchsorted(clique_by_rank, rank)  # clique vertices ranked above v
+    drow, dcol = engine.orient(rowptr, colidx)
+    srcs = np.repeat(np.arange(n), np.diff(drow))
+    expect_pe = np.where((srcs < k) & (dcol < k), above[dcol], 0).astype(np.uint32)
+    for arm in [None, 0, 1, 8]:
+        total, pe, st = engine.count(rowptr, colidx, force_arm=arm, edge_counts=True)
+        assert total == expect, arm
+        assert np.array_equal(pe, expect_pe), arm
+    assert int(np.diff(drow).max()) > 4096
+
+
 def test_edge_list_entry_path(engine, golden):
     for case in golden:
         e = np.array(case["edges"], np.int64).reshape(-1, 2)
