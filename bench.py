@@ -225,7 +225,9 @@ def engine_arm(args, rank, world, local_rank, dist):
             ms, out = timed(step(sel), args.steps, args.warmup, eng, torch, dist)
             results[sel] = (ms, out)
             log(f"[rank {rank}] {sel}: {ms:.2f} ms/step, total={out[0]}, {m / ms / 1e6:.3f} GTEPS")
-    best = "learned" if have_weights else "fixed"
+    # the headline is the engine's default selector (fixed thresholds); the
+    # learned selector is reported beside it
+    best = "fixed"
     ms_best, (total, st) = results[best]
     if results.get("learned") and results["learned"][1][0] != results["fixed"][1][0]:
         raise SystemExit("learned and plain selectors disagree on the count")
@@ -270,6 +272,10 @@ def engine_arm(args, rank, world, local_rank, dist):
             "plain_gteps": round(m / (results["fixed"][0] * 1e-3) / 1e9, 4),
             "learned_gteps": round(m / (results["learned"][0] * 1e-3) / 1e9, 4) if have_weights else None,
             "learned_over_plain": round(results["fixed"][0] / results["learned"][0], 4) if have_weights else None,
+            "learned_detail": ({"ms_count": round(results["learned"][1][1]["ms_count"], 3),
+                                "tiles_per_arm": {k: v for k, v in results["learned"][1][1]["tiles_per_arm"].items() if v},
+                                "ms_arm": {k: round(v, 3) for k, v in results["learned"][1][1]["ms_arm"].items()
+                                           if v > 0.05}} if have_weights else None),
             "phases_ms": {k: round(st[k], 3) for k in ("ms_validate", "ms_orient", "ms_plan", "ms_count",
                                                         "ms_total")},
             "tiles_per_arm": st["tiles_per_arm"],

@@ -317,6 +317,44 @@ __device__ __forceinline__ uint32_t bsearch_count_ilp(const int32_t *__restrict_
   return c;
 }
 
+// Warp-wide count with a pivot cache: lane l holds s[l*ns/32] (the whole
+// list when ns <= 32), so the first five levels of every search are
+// register shuffles; the rest is a binary search inside one 1/32 segment.
+// All lanes run the same number of rounds (shuffles need the full warp).
+__device__ __forceinline__ uint32_t pivot_search_count(const int32_t *__restrict__ l, int nl,
+                                                       const int32_t *__restrict__ s, int ns, int lane) {
+  const bool small = ns <= 32;
+  const int32_t piv = small ? (lane < ns ? __ldg(s + lane) : INT32_MAX)
+                            : __ldg(s + (int)(((long long)lane * ns) >> 5));
+  uint32_t c = 0;
+  for (int i0 = 0; i0 < nl; i0 += 32) {  // warp-uniform trip count
+    const int i = i0 + lane;
+    const int32_t key = i < nl ? __ldg(l + i) : INT32_MIN;  // INT32_MIN matches nothing
+    // p = largest pivot index with piv[p] <= key, or -1 when key < piv[0]
+    int p = -1;
+#pragma unroll
+    for (int step = 32; step >= 1; step >>= 1) {  // p reaches every value in [-1, 31]
+      const int32_t pv = __shfl_sync(TC_FULL_MASK, piv, min(p + step, 31));
+      if (p + step <= 31 && pv <= key) p += step;
+    }
+    const int32_t at_p = __shfl_sync(TC_FULL_MASK, piv, p < 0 ? 0 : p);
+    if (i >= nl || p < 0) continue;
+    if (small) {  // the pivots are the list itself
+      c += (at_p == key) ? 1u : 0u;
+      continue;
+    }
+    // s[p*ns/32] <= key < s[(p+1)*ns/32]: the lower bound lies in that segment
+    int lo = (int)(((long long)p * ns) >> 5);
+    int hi = (int)(((long long)(p + 1) * ns) >> 5);
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (__ldg(s + mid) < key) lo = mid + 1; else hi = mid;
+    }
+    if (lo < ns && __ldg(s + lo) == key) ++c;
+  }
+  return c;
+}
+
 template <int G>
 __device__ __forceinline__ uint32_t group_sum(uint32_t v, unsigned gmask) {
 #pragma unroll
@@ -359,6 +397,9 @@ __global__ void __launch_bounds__(CT_THREADS) bsearch_kernel(DevDag g, const uin
         if (G <= 8) {
           if (L.na <= L.nb) c = bsearch_count_ilp<G, 4>(L.a, L.na, L.b, L.nb, gl);
           else c = bsearch_count_ilp<G, 4>(L.b, L.nb, L.a, L.na, gl);
+        } else if (G == 32) {
+          if (L.na <= L.nb) c = pivot_search_count(L.a, L.na, L.b, L.nb, lane);
+          else c = pivot_search_count(L.b, L.nb, L.a, L.na, lane);
         } else {
           if (L.na <= L.nb) c = bsearch_count<G>(L.a, L.na, L.b, L.nb, gl);
           else c = bsearch_count<G>(L.b, L.nb, L.a, L.na, gl);
@@ -886,6 +927,10 @@ __global__ void __launch_bounds__(BM_THREADS) bitmap_kernel(DevDag g, const uint
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   constexpr int NW = BM_THREADS / 32;
   unsigned long long acc = 0;
+  // The bitmap is cleared once; afterwards every segment unsets exactly the
+  // bits it set, so a segment costs its out-degree, not its id window.
+  for (int w = threadIdx.x; w < BM_SMEM_BYTES / 4; w += BM_THREADS) bm[w] = 0u;
+  __syncthreads();
   for (;;) {
     const int64_t tile = next_tile(qtiles, qb, qn, head, &s_tile);
     if (tile < 0) break;
@@ -899,9 +944,6 @@ __global__ void __launch_bounds__(BM_THREADS) bitmap_kernel(DevDag g, const uint
       const int64_t win = (a0 < re) ? (int64_t)g.col[re - 1] - (int64_t)g.col[a0] + 1 : 0;
       if (a0 < re && win <= BM_BITS) {
         const int32_t lo = g.col[a0], hi = g.col[re - 1];
-        const int words = (int)((win + 31) >> 5);
-        for (int w = threadIdx.x; w < words; w += BM_THREADS) bm[w] = 0u;
-        __syncthreads();
         for (int64_t k = a0 + threadIdx.x; k < re; k += BM_THREADS) {
           const uint32_t x = (uint32_t)(g.col[k] - lo);
           atomicOr(&bm[x >> 5], 1u << (x & 31));
@@ -927,14 +969,17 @@ __global__ void __launch_bounds__(BM_THREADS) bitmap_kernel(DevDag g, const uint
           }
         }
         __syncthreads();
+        for (int64_t k = a0 + threadIdx.x; k < re; k += BM_THREADS)  // unset this segment's bits
+          bm[(uint32_t)(g.col[k] - lo) >> 5] = 0u;
+        __syncthreads();
       } else {
         for (int64_t e = sb + warp; e < se; e += NW) {
           int32_t s;
           const EdgeLists L = edge_lists(g, e, s);
           uint32_t c = 0;
           if (L.na > 0 && L.nb > 0) {
-            if (L.na <= L.nb) c = bsearch_count<32>(L.a, L.na, L.b, L.nb, lane);
-            else c = bsearch_count<32>(L.b, L.nb, L.a, L.na, lane);
+            if (L.na <= L.nb) c = pivot_search_count(L.a, L.na, L.b, L.nb, lane);
+            else c = pivot_search_count(L.b, L.nb, L.a, L.na, lane);
           }
           c = warp_sum(c);
           if (lane == 0) {
