@@ -216,7 +216,7 @@ def engine_arm(args, rank, world, local_rank, dist):
                                             force_arm=fa, edge_counts_ptr=per_edge.data_ptr(), edge_capacity=m)
         return lambda: eng.count_device(n, nnz, rowptr.data_ptr(), colidx.data_ptr(), selector=sel, force_arm=fa)
 
-    if args.force_arm:
+    if args.force_arm is not None:
         have_weights = False
     results = {}
     clk = Clocks(local_rank)
@@ -416,6 +416,8 @@ def main():
     ap.add_argument("--force-arm", default=None, help="run every tile on this arm (profiling)")
     ap.add_argument("--ref-step-seconds", type=float, default=4.0)
     args = ap.parse_args()
+    if args.force_arm is not None and args.force_arm.isdigit():
+        args.force_arm = int(args.force_arm)
     args.warmup = max(args.warmup, 3) if args.impl == "engine" else args.warmup
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -124,7 +124,7 @@ tc_status tc_batch_count(tc_ctx *ctx, const tc_batch *b, const tc_opts *opts_in,
   sz.take<int32_t>(nnz);
   sz.take<int32_t>(n);
   orient_sizes(ctx, n, nnz, false, false, sz);
-  sz.used += count_scratch_bytes(ctx, nnz);
+  sz.used += count_scratch_bytes(ctx, n, nnz);
   sz.take<uint32_t>(nnz);
   sz.take<unsigned long long>(G);
   TC_TRY(arena_reserve(ctx, sz.used));
@@ -152,7 +152,7 @@ tc_status tc_batch_count(tc_ctx *ctx, const tc_batch *b, const tc_opts *opts_in,
   ob.vgroup = vgroup;
   ob.group_bits = gbits;
   CountBufs cb;
-  if (count_carve(ctx, nnz, bump, cb, false) != TC_OK) return set_error(ctx, TC_ERR_OOM, "arena overflow");
+  if (count_carve(ctx, n, nnz, bump, cb, false) != TC_OK) return set_error(ctx, TC_ERR_OOM, "arena overflow");
   uint32_t *cnt = bump.take<uint32_t>(nnz);
   unsigned long long *d_tot = bump.take<unsigned long long>(G);
   if (bump.overflow) return set_error(ctx, TC_ERR_OOM, "arena overflow");
@@ -248,7 +248,7 @@ tc_status tc_plan_arms(tc_ctx *ctx, const tc_csr *g, const tc_opts *opts_in, int
   Sizer sz;
   if (!g->on_device) { sz.take<int64_t>(g->n + 1); sz.take<int32_t>(g->nnz); }
   orient_sizes(ctx, g->n, g->nnz, false, false, sz);
-  sz.used += count_scratch_bytes(ctx, g->nnz);
+  sz.used += count_scratch_bytes(ctx, g->n, g->nnz);
   TC_TRY(arena_reserve(ctx, sz.used));
   Bump bump{ctx->arena, ctx->arena_cap};
   uint64_t h2d = 0;
@@ -257,7 +257,7 @@ tc_status tc_plan_arms(tc_ctx *ctx, const tc_csr *g, const tc_opts *opts_in, int
   OrientBufs ob;
   orient_carve(ctx, d.n, d.nnz, false, false, bump, ob);
   CountBufs cb;
-  if (count_carve(ctx, d.nnz, bump, cb, false) != TC_OK || bump.overflow) return set_error(ctx, TC_ERR_OOM, "arena");
+  if (count_carve(ctx, d.n, d.nnz, bump, cb, false) != TC_OK || bump.overflow) return set_error(ctx, TC_ERR_OOM, "arena");
   int64_t m = 0;
   float a, bb;
   TC_TRY(orient_front(ctx, d, o, ob, &m, &a, &bb));
@@ -290,7 +290,7 @@ tc_status tc_tile_profile(tc_ctx *ctx, const tc_csr *g, float *features, float *
   Sizer sz;
   if (!g->on_device) { sz.take<int64_t>(g->n + 1); sz.take<int32_t>(g->nnz); }
   orient_sizes(ctx, g->n, g->nnz, false, false, sz);
-  sz.used += count_scratch_bytes(ctx, g->nnz);
+  sz.used += count_scratch_bytes(ctx, g->n, g->nnz);
   TC_TRY(arena_reserve(ctx, sz.used));
   Bump bump{ctx->arena, ctx->arena_cap};
   uint64_t h2d = 0;
@@ -299,7 +299,7 @@ tc_status tc_tile_profile(tc_ctx *ctx, const tc_csr *g, float *features, float *
   OrientBufs ob;
   orient_carve(ctx, d.n, d.nnz, false, false, bump, ob);
   CountBufs cb;
-  if (count_carve(ctx, d.nnz, bump, cb, true) != TC_OK || bump.overflow) return set_error(ctx, TC_ERR_OOM, "arena");
+  if (count_carve(ctx, d.n, d.nnz, bump, cb, true) != TC_OK || bump.overflow) return set_error(ctx, TC_ERR_OOM, "arena");
   int64_t m = 0;
   float a, bb;
   TC_TRY(orient_front(ctx, d, o, ob, &m, &a, &bb));

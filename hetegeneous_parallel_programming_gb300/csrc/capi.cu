@@ -223,7 +223,7 @@ tc_status tc_count(tc_ctx *ctx, const tc_csr *g, const tc_opts *opts_in, uint64_
   Sizer sz;
   if (!g->on_device) { sz.take<int64_t>(g->n + 1); sz.take<int32_t>(g->nnz); }
   orient_sizes(ctx, g->n, g->nnz, want_edges, false, sz);
-  sz.used += count_scratch_bytes(ctx, g->nnz);
+  sz.used += count_scratch_bytes(ctx, g->n, g->nnz);
   if (want_edges && !g->on_device) sz.take<uint32_t>(g->nnz);
   TC_TRY(arena_reserve(ctx, sz.used));
   Bump bump{ctx->arena, ctx->arena_cap};
@@ -234,7 +234,7 @@ tc_status tc_count(tc_ctx *ctx, const tc_csr *g, const tc_opts *opts_in, uint64_
   OrientBufs ob;
   orient_carve(ctx, d.n, d.nnz, want_edges, false, bump, ob);
   CountBufs cb;
-  if (count_carve(ctx, d.nnz, bump, cb, o.record_tile_costs != 0) != TC_OK || bump.overflow)
+  if (count_carve(ctx, d.n, d.nnz, bump, cb, o.record_tile_costs != 0) != TC_OK || bump.overflow)
     return set_error(ctx, TC_ERR_OOM, "arena overflow");
   uint32_t *d_out = nullptr;
   if (want_edges) d_out = g->on_device ? edge_counts : bump.take<uint32_t>(d.nnz);
@@ -293,7 +293,7 @@ tc_status tc_count_dag(tc_ctx *ctx, const tc_csr *dag_in, const tc_opts *opts_in
   Sizer sz;
   if (!dag_in->on_device) { sz.take<int64_t>(dag_in->n + 1); sz.take<int32_t>(m); }
   sz.take<int32_t>(m);
-  sz.used += count_scratch_bytes(ctx, m);
+  sz.used += count_scratch_bytes(ctx, dag_in->n, m);
   if (want_edges && !dag_in->on_device) sz.take<uint32_t>(m);
   TC_TRY(arena_reserve(ctx, sz.used));
   Bump bump{ctx->arena, ctx->arena_cap};
@@ -302,7 +302,7 @@ tc_status tc_count_dag(tc_ctx *ctx, const tc_csr *dag_in, const tc_opts *opts_in
   TC_TRY(stage_csr(ctx, dag_in, bump, d, &st.h2d_bytes));
   int32_t *src = bump.take<int32_t>(m);
   CountBufs cb;
-  if (count_carve(ctx, m, bump, cb, o.record_tile_costs != 0) != TC_OK || bump.overflow)
+  if (count_carve(ctx, dag_in->n, m, bump, cb, o.record_tile_costs != 0) != TC_OK || bump.overflow)
     return set_error(ctx, TC_ERR_OOM, "arena overflow");
   uint32_t *d_out = nullptr;
   if (want_edges) d_out = dag_in->on_device ? edge_counts : bump.take<uint32_t>(m);

@@ -31,7 +31,9 @@ constexpr int PLAN_THREADS = 256;
 // ---- plan: features + selection ------------------------------------------------
 
 struct PlanStats {
-  float mean_da, mean_db, mean_min, mean_max, lr, alr;
+  float mean_da, mean_db, mean_min, mean_max;
+  float lr;   // mean target rank as a fraction of n
+  float alr;  // mean |log2 ratio| of the two list lengths
   float nrows, maxdr, maxwin, frac;
   float bins[6];
 };
@@ -102,7 +104,7 @@ __global__ void __launch_bounds__(PLAN_THREADS) plan_kernel(DevDag g, int64_t T,
   const int64_t t = (int64_t)blockIdx.x * (PLAN_THREADS / 32) + (threadIdx.x >> 5);
   if (t >= T) return;
   const int64_t e0 = t * TILE_EDGES, e1 = min(g.m, e0 + TILE_EDGES);
-  float sda = 0, sdb = 0, smin = 0, smax = 0, slr = 0, salr = 0;
+  float sda = 0, sdb = 0, smin = 0, smax = 0, salr = 0, srank = 0;
   float bins[6] = {0, 0, 0, 0, 0, 0};
   unsigned long long work = 0, alg = 0;
   int nrows = 0;
@@ -119,8 +121,8 @@ __global__ void __launch_bounds__(PLAN_THREADS) plan_kernel(DevDag g, int64_t T,
     smin += mn;
     smax += mx;
     const float lr = flog2p1(da) - flog2p1(db);
-    slr += lr;
     salr += fabsf(lr);
+    srank += (float)s / (float)g.n;  // high ranks: hub lists, the hot (cache-resident) ones
     const int bin = mn < 2.f ? 0 : mn < 8.f ? 1 : mn < 32.f ? 2 : mn < 128.f ? 3 : mn < 512.f ? 4 : 5;
 #pragma unroll
     for (int k = 0; k < 6; ++k) bins[k] += (bin == k) ? 1.f : 0.f;
@@ -134,7 +136,7 @@ __global__ void __launch_bounds__(PLAN_THREADS) plan_kernel(DevDag g, int64_t T,
     }
   }
   sda = warp_sum(sda); sdb = warp_sum(sdb); smin = warp_sum(smin); smax = warp_sum(smax);
-  slr = warp_sum(slr); salr = warp_sum(salr);
+  salr = warp_sum(salr); srank = warp_sum(srank);
 #pragma unroll
   for (int k = 0; k < 6; ++k) bins[k] = warp_sum(bins[k]);
   work = warp_sum(work);
@@ -148,12 +150,12 @@ __global__ void __launch_bounds__(PLAN_THREADS) plan_kernel(DevDag g, int64_t T,
   const float ne = (float)(e1 - e0);
   PlanStats st;
   st.mean_da = sda / ne; st.mean_db = sdb / ne; st.mean_min = smin / ne; st.mean_max = smax / ne;
-  st.lr = slr / ne; st.alr = salr / ne;
+  st.lr = srank / ne; st.alr = salr / ne;
   st.nrows = (float)nrows; st.maxdr = (float)maxdr; st.maxwin = (float)maxwin; st.frac = ne / (float)TILE_EDGES;
   float f[TC_MLP_FEATURES];
   f[0] = flog2p1(st.mean_da) / 16.f;
   f[1] = flog2p1(st.mean_db) / 16.f;
-  f[2] = st.lr / 16.f;
+  f[2] = st.lr;  // mean target rank / n (restrict mode: relabelled ranks)
   f[3] = st.alr / 16.f;
   f[4] = flog2p1(st.mean_min) / 16.f;
   f[5] = flog2p1(st.mean_max) / 16.f;
@@ -162,7 +164,7 @@ __global__ void __launch_bounds__(PLAN_THREADS) plan_kernel(DevDag g, int64_t T,
 #pragma unroll
   for (int k = 0; k < 6; ++k) f[8 + k] = bins[k] / ne;
   f[14] = flog2p1(st.maxwin) / 24.f;
-  f[15] = st.frac;
+  f[15] = flog2p1((float)g.m) / 32.f;  // graph size: how much of it the L2 can hold
   int arm;
   if (selector == TC_SELECT_FORCE) arm = force_arm;
   else if (selector == TC_SELECT_LEARNED) arm = mlp_select(s_w, f, lane);
@@ -998,6 +1000,200 @@ __global__ void __launch_bounds__(BM_THREADS) bitmap_kernel(DevDag g, const uint
   flush_total(acc, total);
 }
 
+// ---- PULL (edges grouped by target) ---------------------------------------------------
+//
+// The edges of PULL tiles are grouped by target v with a counting sort
+// (in-edge histogram, exclusive scan, scatter of edge ids; tiles of other arms
+// are skipped whole, so the grouping costs nothing when no tile chose PULL).
+// A warp takes 512 grouped entries; for each run of equal v it hashes N+(v)
+// once into its shared-memory table and probes, for every in-edge u->v of the
+// run, the part of N+(u) that can close a triangle (the row after v in
+// relabelled order, trimmed to values <= max N+(v)), flattened over 32 edges
+// at a time.  Hub targets have thousands of in-edges, so one table serves
+// them all and each edge costs its (short) row suffix, not a search per key.
+// The order inside a group depends on atomics; counts do not.
+
+constexpr int PL_THREADS = 128;
+constexpr int PL_WARPS = PL_THREADS / 32;
+constexpr int PL_SLOTS = 2048;  // per warp: targets with up to 1024 out-neighbours
+constexpr int PL_ITEM = 512;
+constexpr int PL_GROUP_THREADS = 256;
+
+// in-edge histogram of the PULL tiles' targets: cnt[v] += 1 (cnt is zeroed, n+1 long)
+__global__ void __launch_bounds__(PL_GROUP_THREADS) pull_hist_kernel(const int32_t *__restrict__ col,
+                                                                    const int32_t *__restrict__ arm, int64_t m,
+                                                                    unsigned long long *__restrict__ cnt) {
+  const int64_t T = (m + TILE_EDGES - 1) / TILE_EDGES;
+  for (int64_t t = blockIdx.x; t < T; t += gridDim.x) {
+    if (arm[t] != TC_ARM_PULL) continue;
+    const int64_t e1 = min(m, (t + 1) * TILE_EDGES);
+    for (int64_t e = t * TILE_EDGES + threadIdx.x; e < e1; e += PL_GROUP_THREADS)
+      atomicAdd(cnt + __ldg(col + e), 1ull);
+  }
+}
+
+// pos[v] starts at the exclusive scan of the histogram; each edge takes the
+// next slot of its target's group
+__global__ void __launch_bounds__(PL_GROUP_THREADS) pull_scatter_kernel(const int32_t *__restrict__ col,
+                                                                       const int32_t *__restrict__ arm, int64_t m,
+                                                                       unsigned long long *__restrict__ pos,
+                                                                       uint32_t *__restrict__ eids) {
+  const int64_t T = (m + TILE_EDGES - 1) / TILE_EDGES;
+  for (int64_t t = blockIdx.x; t < T; t += gridDim.x) {
+    if (arm[t] != TC_ARM_PULL) continue;
+    const int64_t e1 = min(m, (t + 1) * TILE_EDGES);
+    for (int64_t e = t * TILE_EDGES + threadIdx.x; e < e1; e += PL_GROUP_THREADS)
+      eids[atomicAdd(pos + __ldg(col + e), 1ull)] = (uint32_t)e;
+  }
+}
+
+// `eids` holds the grouped edge ids; `npull` points at their number.
+__global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint32_t *__restrict__ eids,
+                                                         const unsigned long long *__restrict__ npull,
+                                                         unsigned *head, uint32_t *out, unsigned long long *total,
+                                                         unsigned long long *tile_cycles) {
+  __shared__ int32_t tab[PL_WARPS][PL_SLOTS];
+  __shared__ int32_t s_incl[PL_WARPS][32];
+  __shared__ long long s_base[PL_WARPS][32];
+  __shared__ uint32_t s_hits[PL_WARPS][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int32_t *T = tab[w];
+  const int64_t np = (int64_t)*npull;
+  const int64_t items = (np + PL_ITEM - 1) / PL_ITEM;
+  unsigned long long acc = 0;
+  for (;;) {
+    unsigned it = 0;
+    if (lane == 0) it = atomicAdd(head, 1u);
+    it = __shfl_sync(TC_FULL_MASK, it, 0);
+    if ((int64_t)it >= items) break;
+    const int64_t p0 = (int64_t)it * PL_ITEM, p1 = min(np, p0 + PL_ITEM);
+    for (int64_t k = p0; k < p1;) {
+      const long long tr0 = clock64();  // profiling: the run's search and table build are its edges' cost too
+      const int32_t v = __ldg(g.col + eids[k]);
+      // end of the run of target v inside this item
+      int64_t k2 = k + 1;
+      for (;;) {
+        const int64_t j = k2 + lane;
+        const bool diff = j >= p1 || __ldg(g.col + eids[j]) != v;
+        const unsigned bal = __ballot_sync(TC_FULL_MASK, diff);
+        if (bal) { k2 += __ffs(bal) - 1; break; }
+        k2 += 32;
+      }
+      const int64_t bb = g.rowptr[v];
+      const int nb = (int)(g.rowptr[v + 1] - bb);
+      if (nb > PL_SLOTS / 2) {  // long target list: warp pivot search per edge
+        long long tq = tr0;
+        for (int64_t q = k; q < k2; ++q) {
+          const int64_t e = eids[q];
+          int32_t s;
+          const EdgeLists L = edge_lists(g, e, s);
+          uint32_t c = 0;
+          if (L.na > 0 && L.nb > 0) {
+            if (L.na <= L.nb) c = pivot_search_count(L.a, L.na, L.b, L.nb, lane);
+            else c = pivot_search_count(L.b, L.nb, L.a, L.na, lane);
+          }
+          c = warp_sum(c);
+          if (lane == 0) {
+            put_edge_count(g, out, e, c);
+            acc += c;
+            if (tile_cycles) {
+              const long long now = clock64();
+              atomicAdd(&tile_cycles[e / TILE_EDGES], (unsigned long long)(now - tq));
+              tq = now;
+            }
+          }
+        }
+        k = k2;
+        continue;
+      }
+      int bits = 5;
+      while ((1 << bits) < 2 * nb) ++bits;
+      const uint32_t mask = (1u << bits) - 1u;
+      int32_t bmax = 0;
+      if (nb > 0) {
+        for (int q = lane; q < (1 << bits); q += 32) T[q] = HT_EMPTY;
+        __syncwarp();
+        for (int q = lane; q < nb; q += 32) {
+          const int32_t x = __ldg(g.col + bb + q);
+          uint32_t sl = hslot(x, bits);
+          while (atomicCAS(&T[sl], HT_EMPTY, x) != HT_EMPTY) sl = (sl + 1) & mask;
+        }
+        bmax = __ldg(g.col + bb + nb - 1);
+        __syncwarp();
+      }
+      const unsigned long long build_share = (unsigned long long)(clock64() - tr0) / (unsigned long long)(k2 - k);
+      for (int64_t qb = k; qb < k2; qb += 32) {
+        const long long t0 = clock64();
+        const int64_t q = qb + lane;
+        int64_t e = -1;
+        int na = 0;
+        long long abase = 0;
+        if (q < k2) {
+          e = eids[q];
+          if (nb > 0) {
+            const int32_t r = g.src[e];
+            const int64_t rb = g.rowptr[r], re = g.rowptr[r + 1];
+            const int64_t a0 = g.restrict_after ? e + 1 : rb;
+            // keep only the entries <= max N+(v): the rest cannot match
+            int lo = 0, hi = (int)(re - a0);
+            while (lo < hi) {
+              const int mid = (lo + hi) >> 1;
+              if (__ldg(g.col + a0 + mid) <= bmax) lo = mid + 1; else hi = mid;
+            }
+            na = lo;
+            abase = a0;
+          }
+        }
+        int incl = na;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(TC_FULL_MASK, incl, o);
+          if (lane >= o) incl += y;
+        }
+        const int P = __shfl_sync(TC_FULL_MASK, incl, 31);
+        s_incl[w][lane] = incl;
+        s_base[w][lane] = abase - (long long)(incl - na);
+        s_hits[w][lane] = 0u;
+        __syncwarp();
+        int i = 0;
+        int cur_end = s_incl[w][0];
+        long long cur_base = s_base[w][0];
+        for (int p = lane; p < P; p += 32) {
+          if (p >= cur_end) {
+            do { ++i; } while (s_incl[w][i] <= p);
+            cur_end = s_incl[w][i];
+            cur_base = s_base[w][i];
+          }
+          const int32_t x = __ldg(g.col + cur_base + p);
+          uint32_t sl = hslot(x, bits);
+          for (;;) {
+            const int32_t t = T[sl];
+            if (t == x) { atomicAdd(&s_hits[w][i], 1u); break; }
+            if (t == HT_EMPTY) break;
+            sl = (sl + 1) & mask;
+          }
+        }
+        __syncwarp();
+        if (e >= 0) {
+          const uint32_t c = s_hits[w][lane];
+          put_edge_count(g, out, e, c);
+          acc += c;
+          if (tile_cycles) {  // share of this batch's time, by the edge's probe count
+            const unsigned long long dt = (unsigned long long)(clock64() - t0);
+            const unsigned long long part = dt * (unsigned long long)(na + 1) /
+                                            (unsigned long long)(P + min((int64_t)32, k2 - qb));
+            atomicAdd(&tile_cycles[e / TILE_EDGES], part + build_share);
+          }
+        }
+        __syncwarp();
+      }
+      k = k2;
+      __syncwarp();
+    }
+  }
+  flush_total(acc, total);
+}
+
 // ---- host side ---------------------------------------------------------------------
 
 typedef void (*ArmKernel)(DevDag, const uint32_t *, const int64_t *, int, unsigned *, uint32_t *,
@@ -1016,8 +1212,11 @@ static ArmKernel arm_kernel(int arm) {
     default: return bitmap_kernel;
   }
 }
+static const void *arm_func(int arm) {
+  return arm == TC_ARM_PULL ? (const void *)pull_kernel : (const void *)arm_kernel(arm);
+}
 static int arm_threads(int arm) {
-  return arm == TC_ARM_BITMAP ? BM_THREADS : arm == TC_ARM_HASH ? HT_THREADS : CT_THREADS;
+  return arm == TC_ARM_BITMAP ? BM_THREADS : arm == TC_ARM_HASH ? HT_THREADS : arm == TC_ARM_PULL ? PL_THREADS : CT_THREADS;
 }
 static int arm_smem(int arm) { return arm == TC_ARM_BITMAP ? BM_SMEM_BYTES : 0; }
 
@@ -1027,16 +1226,20 @@ tc_status init_arm_occupancy(tc_ctx *ctx) {
                                           (int)(TC_MLP_PARAM_COUNT * sizeof(float))));
   for (int a = 0; a < TC_NUM_ARMS; ++a) {
     int nb = 0;
-    TC_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, arm_kernel(a), arm_threads(a), arm_smem(a)));
+    TC_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, arm_func(a), arm_threads(a), arm_smem(a)));
     ctx->arm_blocks_per_sm[a] = nb > 0 ? nb : 1;
-    // independent workers per SM: warps for the warp-level HASH arm, blocks otherwise
-    const bool warp_items = a == TC_ARM_HASH || a == TC_ARM_FLAT;
-    ctx->arm_units_per_sm[a] = ctx->arm_blocks_per_sm[a] * (warp_items ? HT_WARPS : 1);
+    // independent workers per SM: warps for the warp-level arms, blocks otherwise
+    const bool warp_items = a == TC_ARM_HASH || a == TC_ARM_FLAT || a == TC_ARM_PULL;
+    ctx->arm_units_per_sm[a] = ctx->arm_blocks_per_sm[a] * (warp_items ? arm_threads(a) / 32 : 1);
   }
   return TC_OK;
 }
 
-size_t count_scratch_bytes(const tc_ctx *ctx, int64_t m) {
+static size_t count_sort_scratch_bytes(const tc_ctx *ctx, int64_t n, int64_t T) {
+  return std::max(radix_sort_scratch_bytes(ctx, T > 0 ? T : 1), scan_scratch_bytes(ctx, n + 1));
+}
+
+size_t count_scratch_bytes(const tc_ctx *ctx, int64_t n, int64_t m) {
   const int64_t T = (m + TILE_EDGES - 1) / TILE_EDGES;
   Sizer sz;
   sz.take<float>(T * TC_MLP_FEATURES);
@@ -1049,10 +1252,12 @@ size_t count_scratch_bytes(const tc_ctx *ctx, int64_t m) {
   sz.take<unsigned long long>(T);
   sz.take<unsigned long long>(T);
   sz.take<unsigned long long>(TC_NUM_ARMS);
-  return sz.used + radix_sort_scratch_bytes(ctx, T > 0 ? T : 1) + 256;
+  sz.take<int64_t>(n + 1);
+  sz.take<uint32_t>(m);
+  return sz.used + count_sort_scratch_bytes(ctx, n, T) + 256;
 }
 
-tc_status count_carve(const tc_ctx *ctx, int64_t m, Bump &bump, CountBufs &cb, bool want_cycles) {
+tc_status count_carve(const tc_ctx *ctx, int64_t n, int64_t m, Bump &bump, CountBufs &cb, bool want_cycles) {
   const int64_t T = (m + TILE_EDGES - 1) / TILE_EDGES;
   cb.features = bump.take<float>(T * TC_MLP_FEATURES);
   cb.qkeys0 = bump.take<uint64_t>(T);
@@ -1065,7 +1270,9 @@ tc_status count_carve(const tc_ctx *ctx, int64_t m, Bump &bump, CountBufs &cb, b
   cb.tile_cycles = want_cycles ? cyc : nullptr;
   cb.tile_bytes = bump.take<unsigned long long>(T);
   cb.arm_bytes = bump.take<unsigned long long>(TC_NUM_ARMS);
-  cb.sort_scratch = bump.take<char>((int64_t)radix_sort_scratch_bytes(ctx, T > 0 ? T : 1));
+  cb.pull_pos = bump.take<int64_t>(n + 1);
+  cb.pull_eids = bump.take<uint32_t>(m);
+  cb.sort_scratch = bump.take<char>((int64_t)count_sort_scratch_bytes(ctx, n, T));
   return bump.overflow ? TC_ERR_OOM : TC_OK;
 }
 
@@ -1074,6 +1281,27 @@ constexpr int PIN_QOFF = 16;                           // TC_NUM_ARMS + 1 int64
 constexpr int PIN_BYTES = PIN_QOFF + TC_NUM_ARMS + 1;  // TC_NUM_ARMS uint64
 static_assert(PIN_BYTES + TC_NUM_ARMS <= 64, "pinned scratch holds 64 words");
 static_assert(sizeof(((tc_ctx *)nullptr)->ev) / sizeof(cudaEvent_t) >= 10 + TC_NUM_ARMS, "one event per arm");
+
+// PULL arm: group the PULL tiles' edges by target, then count.  Launched with
+// a grid for every tile (each block skips tiles of other arms) since the
+// number of PULL tiles is known only on the device.
+static tc_status run_pull(tc_ctx *ctx, const DevDag &g, CountBufs &cb, uint32_t *out, int64_t T) {
+  unsigned long long *pos = reinterpret_cast<unsigned long long *>(cb.pull_pos);
+  TC_CHECK_CUDA(ctx, cudaMemsetAsync(cb.pull_pos, 0, sizeof(int64_t) * (g.n + 1), ctx->stream));
+  const int gblocks = (int)std::min<int64_t>(T, (int64_t)ctx->num_sms * 8);
+  pull_hist_kernel<<<gblocks, PL_GROUP_THREADS, 0, ctx->stream>>>(g.col, cb.arm, g.m, pos);
+  TC_CHECK_LAUNCH(ctx);
+  TC_TRY(exclusive_scan_i64(ctx, cb.pull_pos, cb.pull_pos, g.n + 1, cb.sort_scratch, nullptr));
+  pull_scatter_kernel<<<gblocks, PL_GROUP_THREADS, 0, ctx->stream>>>(g.col, cb.arm, g.m, pos, cb.pull_eids);
+  TC_CHECK_LAUNCH(ctx);
+  // after the scatter pos[v] is the end of v's group; pos[n] (no edge targets
+  // n) still holds the number of grouped edges
+  const int grid = ctx->num_sms * ctx->arm_blocks_per_sm[TC_ARM_PULL];
+  pull_kernel<<<grid, PL_THREADS, 0, ctx->stream>>>(g, cb.pull_eids, pos + g.n, ctx->d_heads + TC_ARM_PULL, out,
+                                                    ctx->d_total, cb.tile_cycles);
+  TC_CHECK_LAUNCH(ctx);
+  return TC_OK;
+}
 
 tc_status run_count(tc_ctx *ctx, const DevDag &g, const tc_opts &opts, CountBufs &cb, uint32_t *out, bool timing) {
   const int64_t T = (g.m + TILE_EDGES - 1) / TILE_EDGES;
@@ -1110,7 +1338,9 @@ tc_status run_count(tc_ctx *ctx, const DevDag &g, const tc_opts &opts, CountBufs
     TC_CHECK_CUDA(ctx, cudaMemsetAsync(cb.tile_cycles, 0, sizeof(unsigned long long) * T, ctx->stream));
   if (timing) TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[9], ctx->stream));
   for (int a = 0; a < TC_NUM_ARMS; ++a) {
-    if (T > 0) {
+    if (T > 0 && a == TC_ARM_PULL) {
+      TC_TRY(run_pull(ctx, g, cb, out, T));
+    } else if (T > 0) {
       const int grid = ctx->num_sms * ctx->arm_blocks_per_sm[a];
       arm_kernel(a)<<<grid, arm_threads(a), arm_smem(a), ctx->stream>>>(g, sv, cb.qoff, a, ctx->d_heads + a, out,
                                                                         ctx->d_total, cb.tile_cycles);

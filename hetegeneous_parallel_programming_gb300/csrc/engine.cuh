@@ -87,10 +87,12 @@ struct CountBufs {
   unsigned long long *tile_cycles;  // [T] (optional)
   unsigned long long *tile_bytes;   // [T] algorithmic bytes per tile
   unsigned long long *arm_bytes;    // [TC_NUM_ARMS]
+  int64_t *pull_pos;      // [n+1] PULL grouping: in-edge counts, then group offsets
+  uint32_t *pull_eids;    // [m] PULL grouping: edge ids grouped by target
   void *sort_scratch;
 };
-size_t count_scratch_bytes(const tc_ctx *ctx, int64_t m);
-tc_status count_carve(const tc_ctx *ctx, int64_t m, Bump &bump, CountBufs &cb, bool want_cycles);
+size_t count_scratch_bytes(const tc_ctx *ctx, int64_t n, int64_t m);
+tc_status count_carve(const tc_ctx *ctx, int64_t n, int64_t m, Bump &bump, CountBufs &cb, bool want_cycles);
 // Enqueues plan, queue build and every arm kernel on the ctx stream (no host
 // sync, so it can be captured into a CUDA graph); adds the count into
 // ctx->d_total (which the caller zeroes) and writes per-edge counts to

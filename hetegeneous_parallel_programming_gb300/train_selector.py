@@ -3,9 +3,15 @@
 Training data: per-tile features and per-arm SM-cycle costs that the plain
 engine records (tc_tile_profile: every tile run with every arm) on R-MAT
 graphs of scale 16-20 with 32 seeds, (a, b, c) drawn from [0.45, 0.6] x
-[0.1, 0.25] x [0.1, 0.25] (d = 1 - a - b - c).  Training is the library's own
+[0.1, 0.25] x [0.1, 0.25] (d = 1 - a - b - c).  Each graph is profiled twice:
+alone, where its whole DAG sits in the 129 MB L2, and as part of one disjoint
+union of all 32 graphs (about 330M adjacency entries), where the lists come
+from HBM as they do for a scale-24 graph.  The union is an ordinary graph;
+degree ordering inside each component is the same as in the graph alone, so
+the tiles do the same work in the two regimes and only their costs differ
+(the m feature tells the regimes apart).  Training is the library's own
 device forward/backward/Adam kernels (tc_selector_train).  Held-out graphs
-(other seeds, scales 20-22, the default (0.57, 0.19, 0.19)) measure regret:
+(other seeds, scales 20-24, the default (0.57, 0.19, 0.19)) measure regret:
 the summed cost of the chosen arm per tile over the summed cost of the
 per-tile best arm, for the fixed-threshold selector and for the MLP.
 
@@ -30,6 +36,15 @@ def rmat_graph(eng: tc.Engine, scale: int, a: float, b: float, c: float, seed: i
     return eng.csr_from_edges(n, s, d)
 
 
+def disjoint_union(graphs):
+    """One CSR holding every (rowptr, colidx) as a separate component."""
+    voff = np.cumsum([0] + [len(r) - 1 for r, _ in graphs])
+    eoff = np.cumsum([0] + [len(c) for _, c in graphs])
+    rowptr = np.concatenate([r[:-1] + eoff[i] for i, (r, _) in enumerate(graphs)] + [eoff[-1:]]).astype(np.int64)
+    colidx = np.concatenate([c + np.int32(voff[i]) for i, (_, c) in enumerate(graphs)]).astype(np.int32)
+    return rowptr, colidx
+
+
 def regret(costs: np.ndarray, chosen: np.ndarray) -> float:
     """Summed cost of the chosen arms over the summed per-tile best cost."""
     best = costs.min(axis=1).sum()
@@ -42,12 +57,14 @@ def main():
     ap.add_argument("--seeds", type=int, default=32)
     ap.add_argument("--epochs", type=int, default=80)
     ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--no-union", action="store_true", help="profile each graph alone only")
+    ap.add_argument("--save-heldout", action="store_true", help="also write the held-out graphs' tile profiles")
     args = ap.parse_args()
     out = Path(args.out)
     out.mkdir(parents=True, exist_ok=True)
     eng = tc.Engine(0)
     rng = np.random.default_rng(1234)
-    feats, costs, meta, fixed = [], [], [], []
+    feats, costs, meta, fixed, graphs = [], [], [], [], []
     t0 = time.time()
     for i in range(args.seeds):
         scale = 16 + i % 5
@@ -62,6 +79,18 @@ def main():
         costs.append(k)
         fixed.append(eng.plan_arms(r, cidx, selector="fixed"))
         meta.append({"scale": scale, "a": a, "b": b, "c": c, "seed": 1000 + i, "tiles": len(f)})
+        if not args.no_union:
+            graphs.append((r, cidx))
+    union = None
+    if graphs:
+        ur, uc = disjoint_union(graphs)
+        graphs.clear()
+        f, k = eng.tile_profile(ur, uc)
+        feats.append(f)
+        costs.append(k)
+        fixed.append(eng.plan_arms(ur, uc, selector="fixed"))
+        union = {"n": int(len(ur) - 1), "nnz": int(len(uc)), "tiles": len(f)}
+        del ur, uc
     X = np.concatenate(feats)
     Y = np.concatenate(costs)
     t_prof = time.time() - t0
@@ -72,6 +101,7 @@ def main():
     pred = eng.selector_predict(X)
     train_regret = {"learned": regret(Y, pred.argmin(1)), "fixed": regret(Y, np.concatenate(fixed))}
     held = []
+    held_sets = {}
     # held out: other seeds and larger scales, and the benchmark graph itself
     # (R-MAT scale 24, seed 0), none of them seen in training
     for scale, seed in [(20, 5), (21, 6), (22, 7), (24, 0)]:
@@ -79,6 +109,9 @@ def main():
         f, k = eng.tile_profile(r, cidx)
         learned = eng.plan_arms(r, cidx, selector="learned")
         fx = eng.plan_arms(r, cidx, selector="fixed")
+        if args.save_heldout:
+            held_sets[f"s{scale}_features"] = f
+            held_sets[f"s{scale}_costs"] = k
         held.append({"scale": scale, "seed": seed, "tiles": len(f),
                      "regret_learned": regret(k, learned), "regret_fixed": regret(k, fx),
                      "cost_fixed_over_learned": float(k[np.arange(len(k)), fx].sum() /
@@ -91,10 +124,12 @@ def main():
     info = {"architecture": f"16 -> 64 -> 64 -> {tc.TC_NUM_ARMS}, ReLU; bf16 weights at inference, fp32 accumulate",
             "loss": loss, "epochs": args.epochs, "lr": args.lr, "rows": int(len(X)),
             "profile_seconds": round(t_prof, 1), "train_seconds": round(t_train, 2),
-            "train_regret": train_regret, "held_out": held, "graphs": meta,
+            "train_regret": train_regret, "held_out": held, "graphs": meta, "union": union,
             "arms": tc.ARM_NAMES}
     (out / "selector_mlp.json").write_text(json.dumps(info, indent=1))
     np.savez_compressed(out / "selector_training_set.npz", features=X, costs=Y)
+    if held_sets:
+        np.savez_compressed(out / "selector_heldout_set.npz", **held_sets)
     print(json.dumps({k: info[k] for k in ("loss", "rows", "train_regret", "held_out")}, indent=1))
     eng.close()
 

@@ -70,7 +70,9 @@ typedef enum tc_arm {
   TC_ARM_GALLOP_4 = 6,     /* 4 lanes per edge, each gallops a run of keys    */
   TC_ARM_MPATH_4 = 7,      /* 4 lanes per edge split the merge path evenly    */
   TC_ARM_FLAT = 8,         /* warp walks 32 edges' lookup lists as one run    */
-  TC_NUM_ARMS = 9
+  TC_ARM_PULL = 9,         /* edges grouped by target: hash N+(v) once, probe
+                              every in-edge's row suffix against it           */
+  TC_NUM_ARMS = 10
 } tc_arm;
 
 typedef enum tc_selector {

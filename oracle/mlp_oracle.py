@@ -9,7 +9,7 @@ from __future__ import annotations
 
 import numpy as np
 
-F, H, K = 16, 64, 9
+F, H, K = 16, 64, 10
 P = F * H + H + H * H + H + H * K + K
 
 

@@ -42,7 +42,7 @@ def test_count_dag_matches_reference_solver(engine, golden):
     for case in golden:
         rowptr, colidx = csr_of(case)
         orow, ocol = oracle.orient(rowptr, colidx)
-        for arm in [None, 0, 3, 5]:
+        for arm in [None, 0, 3, 5, 9]:
             total, per_edge, _ = engine.count_dag(orow, ocol, force_arm=arm, edge_counts=True)
             ref, ref_pe = oracle.count(orow, ocol, per_edge=True)
             assert total == ref == case["triangles"]
@@ -117,7 +117,7 @@ def test_long_rows_every_sort_class(engine):
     drow, dcol = engine.orient(rowptr, colidx)
     srcs = np.repeat(np.arange(n), np.diff(drow))
     expect_pe = np.where((srcs < k) & (dcol < k), above[dcol], 0).astype(np.uint32)
-    for arm in [None, 0, 1, 8]:
+    for arm in [None, 0, 1, 8, 9]:
         total, pe, st = engine.count(rowptr, colidx, force_arm=arm, edge_counts=True)
         assert total == expect, arm
         assert np.array_equal(pe, expect_pe), arm
@@ -169,7 +169,7 @@ def test_batch_matches_per_graph(engine):
         base += len(c)
     rowptr, colidx = np.concatenate(rows), np.concatenate(cols)
     ref = oracle.batch_count(vtx_off, rowptr, colidx)
-    for arm in [None, 0, 2, 4, 5]:
+    for arm in [None, 0, 2, 4, 5, 9]:
         totals, st = engine.batch_count(vtx_off, rowptr, colidx, force_arm=arm)
         assert np.array_equal(totals, ref), arm
     # replay of the captured graph gives the same answer
