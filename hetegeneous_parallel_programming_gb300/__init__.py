@@ -346,12 +346,13 @@ class Engine:
         self._chk(self._L.tc_plan_arms(self._h, C.byref(g), C.byref(o), _ptr(arms), cap, C.byref(t)))
         return arms[:t.value].copy()
 
-    def train_selector(self, features, costs, *, epochs: int = 60, lr: float = 2e-3, seed: int = 0) -> float:
+    def train_selector(self, features, costs, *, epochs: int = 60, lr: float = 2e-3, weight_decay: float = 0.0,
+                       seed: int = 0) -> float:
         features = np.ascontiguousarray(features, np.float32)
         costs = np.ascontiguousarray(costs, np.float32)
         loss = C.c_float(0)
         self._chk(self._L.tc_selector_train(self._h, _ptr(features), _ptr(costs), len(features), int(epochs),
-                                            float(lr), int(seed), C.byref(loss)))
+                                            float(lr), float(weight_decay), int(seed), C.byref(loss)))
         return float(loss.value)
 
     def set_selector_weights(self, params) -> None:

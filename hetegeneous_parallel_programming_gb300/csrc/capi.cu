@@ -69,6 +69,7 @@ void orient_sizes(const tc_ctx *ctx, int64_t n, int64_t nnz, bool perm, bool dag
   scr = std::max(scr, scan_scratch_bytes(ctx, G));
   sz.take<char>((int64_t)scr);
   sz.take<int64_t>(n + 1); sz.take<int64_t>(n + 1); sz.take<int64_t>(n + 1);
+  sz.take<int32_t>(n);
   sz.take<int32_t>(n); sz.take<int32_t>(n); sz.take<int32_t>(n); sz.take<unsigned>(3);
   sz.take<int32_t>(mmax); sz.take<int32_t>(mmax);
   if (perm) sz.take<uint32_t>(mmax);
@@ -91,6 +92,7 @@ void orient_carve(const tc_ctx *ctx, int64_t n, int64_t nnz, bool perm, bool dag
   b.orowptr = bump.take<int64_t>(n + 1);
   b.nrowptr = bump.take<int64_t>(n + 1);
   b.dnew = bump.take<int64_t>(n + 1);
+  b.indeg = bump.take<int32_t>(n);
   b.mid_list = bump.take<int32_t>(n);
   b.big_list = bump.take<int32_t>(n);
   b.huge_list = bump.take<int32_t>(n);
@@ -293,6 +295,7 @@ tc_status tc_count_dag(tc_ctx *ctx, const tc_csr *dag_in, const tc_opts *opts_in
   Sizer sz;
   if (!dag_in->on_device) { sz.take<int64_t>(dag_in->n + 1); sz.take<int32_t>(m); }
   sz.take<int32_t>(m);
+  sz.take<int32_t>(dag_in->n);
   sz.used += count_scratch_bytes(ctx, dag_in->n, m);
   if (want_edges && !dag_in->on_device) sz.take<uint32_t>(m);
   TC_TRY(arena_reserve(ctx, sz.used));
@@ -301,6 +304,7 @@ tc_status tc_count_dag(tc_ctx *ctx, const tc_csr *dag_in, const tc_opts *opts_in
   DevCSR d;
   TC_TRY(stage_csr(ctx, dag_in, bump, d, &st.h2d_bytes));
   int32_t *src = bump.take<int32_t>(m);
+  int32_t *indeg = bump.take<int32_t>(dag_in->n);
   CountBufs cb;
   if (count_carve(ctx, dag_in->n, m, bump, cb, o.record_tile_costs != 0) != TC_OK || bump.overflow)
     return set_error(ctx, TC_ERR_OOM, "arena overflow");
@@ -318,6 +322,7 @@ tc_status tc_count_dag(tc_ctx *ctx, const tc_csr *dag_in, const tc_opts *opts_in
   if (flags) return set_error(ctx, TC_ERR_INVALID_GRAPH, "%s", flag_text(flags));
   TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[4], ctx->stream));
   TC_TRY(launch_expand_src(ctx, d.rowptr, d.n, m, src));
+  TC_TRY(launch_indeg(ctx, d.col, d.n, m, indeg));
   TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[5], ctx->stream));
   DevDag dag;
   dag.n = d.n;
@@ -326,6 +331,7 @@ tc_status tc_count_dag(tc_ctx *ctx, const tc_csr *dag_in, const tc_opts *opts_in
   dag.col = d.col;
   dag.src = src;
   dag.perm = nullptr;
+  dag.indeg = indeg;
   dag.restrict_after = 0;
   TC_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->d_total, 0, sizeof(unsigned long long), ctx->stream));
   TC_TRY(run_count(ctx, dag, o, cb, d_out, true));

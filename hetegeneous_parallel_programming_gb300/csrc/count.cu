@@ -32,7 +32,7 @@ constexpr int PLAN_THREADS = 256;
 
 struct PlanStats {
   float mean_da, mean_db, mean_min, mean_max;
-  float lr;   // mean target rank as a fraction of n
+  float mean_in;  // mean DAG in-degree of the edges' targets
   float alr;  // mean |log2 ratio| of the two list lengths
   float nrows, maxdr, maxwin, frac;
   float bins[6];
@@ -46,6 +46,10 @@ __device__ __forceinline__ int fixed_select(const PlanStats &s) {
   // Thresholds fitted to per-tile arm costs recorded on R-MAT scale 16-20
   // graphs (the learned selector's training set).  The bitmap is cleared per
   // row segment, so it only pays for small id windows.
+  // PULL when many edges share each target list (its table build is spread
+  // over them) and the lists are long enough for searches to cost more than
+  // one shared-memory test per row-suffix entry.
+  if (s.mean_in >= 256.f && s.mean_db >= 32.f && s.mean_da >= 8.f) return TC_ARM_PULL;
   if (s.nrows <= 16.f && s.mean_min >= 64.f && s.maxwin <= 16384.f) return TC_ARM_BITMAP;
   if (s.mean_min >= 64.f) return TC_ARM_BSEARCH_32;
   return TC_ARM_BSEARCH_4;
@@ -104,7 +108,7 @@ __global__ void __launch_bounds__(PLAN_THREADS) plan_kernel(DevDag g, int64_t T,
   const int64_t t = (int64_t)blockIdx.x * (PLAN_THREADS / 32) + (threadIdx.x >> 5);
   if (t >= T) return;
   const int64_t e0 = t * TILE_EDGES, e1 = min(g.m, e0 + TILE_EDGES);
-  float sda = 0, sdb = 0, smin = 0, smax = 0, salr = 0, srank = 0;
+  float sda = 0, sdb = 0, smin = 0, smax = 0, salr = 0, sin = 0;
   float bins[6] = {0, 0, 0, 0, 0, 0};
   unsigned long long work = 0, alg = 0;
   int nrows = 0;
@@ -122,7 +126,7 @@ __global__ void __launch_bounds__(PLAN_THREADS) plan_kernel(DevDag g, int64_t T,
     smax += mx;
     const float lr = flog2p1(da) - flog2p1(db);
     salr += fabsf(lr);
-    srank += (float)s / (float)g.n;  // high ranks: hub lists, the hot (cache-resident) ones
+    if (g.indeg) sin += (float)g.indeg[s];  // how many edges share this target's list
     const int bin = mn < 2.f ? 0 : mn < 8.f ? 1 : mn < 32.f ? 2 : mn < 128.f ? 3 : mn < 512.f ? 4 : 5;
 #pragma unroll
     for (int k = 0; k < 6; ++k) bins[k] += (bin == k) ? 1.f : 0.f;
@@ -136,7 +140,7 @@ __global__ void __launch_bounds__(PLAN_THREADS) plan_kernel(DevDag g, int64_t T,
     }
   }
   sda = warp_sum(sda); sdb = warp_sum(sdb); smin = warp_sum(smin); smax = warp_sum(smax);
-  salr = warp_sum(salr); srank = warp_sum(srank);
+  salr = warp_sum(salr); sin = warp_sum(sin);
 #pragma unroll
   for (int k = 0; k < 6; ++k) bins[k] = warp_sum(bins[k]);
   work = warp_sum(work);
@@ -150,12 +154,12 @@ __global__ void __launch_bounds__(PLAN_THREADS) plan_kernel(DevDag g, int64_t T,
   const float ne = (float)(e1 - e0);
   PlanStats st;
   st.mean_da = sda / ne; st.mean_db = sdb / ne; st.mean_min = smin / ne; st.mean_max = smax / ne;
-  st.lr = srank / ne; st.alr = salr / ne;
+  st.mean_in = sin / ne; st.alr = salr / ne;
   st.nrows = (float)nrows; st.maxdr = (float)maxdr; st.maxwin = (float)maxwin; st.frac = ne / (float)TILE_EDGES;
   float f[TC_MLP_FEATURES];
   f[0] = flog2p1(st.mean_da) / 16.f;
   f[1] = flog2p1(st.mean_db) / 16.f;
-  f[2] = st.lr;  // mean target rank / n (restrict mode: relabelled ranks)
+  f[2] = flog2p1(st.mean_in) / 24.f;
   f[3] = st.alr / 16.f;
   f[4] = flog2p1(st.mean_min) / 16.f;
   f[5] = flog2p1(st.mean_max) / 16.f;
@@ -1005,18 +1009,19 @@ __global__ void __launch_bounds__(BM_THREADS) bitmap_kernel(DevDag g, const uint
 // The edges of PULL tiles are grouped by target v with a counting sort
 // (in-edge histogram, exclusive scan, scatter of edge ids; tiles of other arms
 // are skipped whole, so the grouping costs nothing when no tile chose PULL).
-// A warp takes 512 grouped entries; for each run of equal v it hashes N+(v)
-// once into its shared-memory table and probes, for every in-edge u->v of the
-// run, the part of N+(u) that can close a triangle (the row after v in
-// relabelled order, trimmed to values <= max N+(v)), flattened over 32 edges
-// at a time.  Hub targets have thousands of in-edges, so one table serves
-// them all and each edge costs its (short) row suffix, not a search per key.
-// The order inside a group depends on atomics; counts do not.
+// A warp takes 512 grouped entries; for each run of equal v it loads N+(v)
+// once into its shared-memory bitmap or hash table and probes, for every
+// in-edge u->v of the run, the part of N+(u) that can close a triangle (the
+// row after v in relabelled order), flattened over 32 edges at a time.  Hub
+// targets have thousands of in-edges, so one table serves them all and each
+// edge costs its row suffix at one shared-memory test per entry, not a
+// search per key.  The order inside a group depends on atomics; counts do not.
 
 constexpr int PL_THREADS = 128;
 constexpr int PL_WARPS = PL_THREADS / 32;
-constexpr int PL_SLOTS = 2048;  // per warp: targets with up to 1024 out-neighbours
+constexpr int PL_WORDS = 2048;  // per warp: a 65536-id bitmap or a 2048-slot hash table
 constexpr int PL_ITEM = 512;
+constexpr int PL_UNROLL = 4;
 constexpr int PL_GROUP_THREADS = 256;
 
 // in-edge histogram of the PULL tiles' targets: cnt[v] += 1 (cnt is zeroed, n+1 long)
@@ -1048,16 +1053,41 @@ __global__ void __launch_bounds__(PL_GROUP_THREADS) pull_scatter_kernel(const in
 }
 
 // `eids` holds the grouped edge ids; `npull` points at their number.
+//
+// Each warp owns PL_WORDS words of shared memory, all zero between runs.  A
+// run of target v uses them as a bitmap over v's id window (min..max of
+// N+(v)) when that window has at most PL_WORDS*32 ids, else as a hash table of
+// 2*d+(v) slots holding x+1 (0 = empty) when d+(v) <= PL_WORDS/2, else the
+// run's edges fall back to the warp pivot search.  After the run the warp
+// zeroes what it wrote.
+__device__ __forceinline__ uint32_t pull_probe(const uint32_t *tb, bool bitmap, int32_t base, uint32_t span,
+                                               int bits, int32_t x) {
+  if (bitmap) {
+    const uint32_t d = (uint32_t)(x - base);
+    return d < span ? (tb[d >> 5] >> (d & 31)) & 1u : 0u;
+  }
+  const uint32_t mask = (1u << bits) - 1u, want = (uint32_t)x + 1u;
+  uint32_t sl = hslot(x, bits);
+  for (;;) {
+    const uint32_t t = tb[sl];
+    if (t == want) return 1u;
+    if (t == 0u) return 0u;
+    sl = (sl + 1) & mask;
+  }
+}
+
 __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint32_t *__restrict__ eids,
                                                          const unsigned long long *__restrict__ npull,
                                                          unsigned *head, uint32_t *out, unsigned long long *total,
                                                          unsigned long long *tile_cycles) {
-  __shared__ int32_t tab[PL_WARPS][PL_SLOTS];
+  __shared__ uint32_t tab[PL_WARPS][PL_WORDS];
   __shared__ int32_t s_incl[PL_WARPS][32];
   __shared__ long long s_base[PL_WARPS][32];
   __shared__ uint32_t s_hits[PL_WARPS][32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  int32_t *T = tab[w];
+  uint32_t *tb = tab[w];
+  for (int q = lane; q < PL_WORDS; q += 32) tb[q] = 0u;
+  __syncwarp();
   const int64_t np = (int64_t)*npull;
   const int64_t items = (np + PL_ITEM - 1) / PL_ITEM;
   unsigned long long acc = 0;
@@ -1081,7 +1111,10 @@ __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint32
       }
       const int64_t bb = g.rowptr[v];
       const int nb = (int)(g.rowptr[v + 1] - bb);
-      if (nb > PL_SLOTS / 2) {  // long target list: warp pivot search per edge
+      const int32_t bmin = nb > 0 ? __ldg(g.col + bb) : 0;
+      const uint32_t span = nb > 0 ? (uint32_t)(__ldg(g.col + bb + nb - 1) - bmin) + 1u : 0u;
+      const bool bitmap = span <= (uint32_t)PL_WORDS * 32u;
+      if (!bitmap && nb > PL_WORDS / 2) {  // wide window and long list: warp pivot search per edge
         long long tq = tr0;
         for (int64_t q = k; q < k2; ++q) {
           const int64_t e = eids[q];
@@ -1107,20 +1140,22 @@ __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint32
         continue;
       }
       int bits = 5;
-      while ((1 << bits) < 2 * nb) ++bits;
-      const uint32_t mask = (1u << bits) - 1u;
-      int32_t bmax = 0;
-      if (nb > 0) {
-        for (int q = lane; q < (1 << bits); q += 32) T[q] = HT_EMPTY;
-        __syncwarp();
+      if (!bitmap)
+        while ((1 << bits) < 2 * nb) ++bits;
+      if (bitmap) {
+        for (int q = lane; q < nb; q += 32) {
+          const uint32_t d = (uint32_t)(__ldg(g.col + bb + q) - bmin);
+          if (d < span) atomicOr(&tb[d >> 5], 1u << (d & 31));  // false only for an unsorted list
+        }
+      } else {
+        const uint32_t mask = (1u << bits) - 1u;
         for (int q = lane; q < nb; q += 32) {
           const int32_t x = __ldg(g.col + bb + q);
           uint32_t sl = hslot(x, bits);
-          while (atomicCAS(&T[sl], HT_EMPTY, x) != HT_EMPTY) sl = (sl + 1) & mask;
+          while (atomicCAS(&tb[sl], 0u, (uint32_t)x + 1u) != 0u) sl = (sl + 1) & mask;
         }
-        bmax = __ldg(g.col + bb + nb - 1);
-        __syncwarp();
       }
+      __syncwarp();
       const unsigned long long build_share = (unsigned long long)(clock64() - tr0) / (unsigned long long)(k2 - k);
       for (int64_t qb = k; qb < k2; qb += 32) {
         const long long t0 = clock64();
@@ -1132,15 +1167,9 @@ __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint32
           e = eids[q];
           if (nb > 0) {
             const int32_t r = g.src[e];
-            const int64_t rb = g.rowptr[r], re = g.rowptr[r + 1];
-            const int64_t a0 = g.restrict_after ? e + 1 : rb;
-            // keep only the entries <= max N+(v): the rest cannot match
-            int lo = 0, hi = (int)(re - a0);
-            while (lo < hi) {
-              const int mid = (lo + hi) >> 1;
-              if (__ldg(g.col + a0 + mid) <= bmax) lo = mid + 1; else hi = mid;
-            }
-            na = lo;
+            const int64_t re = g.rowptr[r + 1];
+            const int64_t a0 = g.restrict_after ? e + 1 : g.rowptr[r];
+            na = (int)(re - a0);
             abase = a0;
           }
         }
@@ -1155,24 +1184,36 @@ __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint32
         s_base[w][lane] = abase - (long long)(incl - na);
         s_hits[w][lane] = 0u;
         __syncwarp();
-        int i = 0;
-        int cur_end = s_incl[w][0];
-        long long cur_base = s_base[w][0];
-        for (int p = lane; p < P; p += 32) {
-          if (p >= cur_end) {
-            do { ++i; } while (s_incl[w][i] <= p);
-            cur_end = s_incl[w][i];
-            cur_base = s_base[w][i];
+        // flattened probes, PL_UNROLL loads in flight per lane; hits count in
+        // a register while the lane stays on one edge
+        int i = 0, cur = -1;
+        uint32_t cnt = 0;
+        for (int pb = 0; pb < P; pb += 32 * PL_UNROLL) {
+          int32_t x[PL_UNROLL];
+          int ie[PL_UNROLL];
+#pragma unroll
+          for (int u = 0; u < PL_UNROLL; ++u) {
+            const int p = pb + 32 * u + lane;
+            ie[u] = -1;
+            x[u] = 0;
+            if (p < P) {
+              while (s_incl[w][i] <= p) ++i;
+              ie[u] = i;
+              x[u] = __ldg(g.col + s_base[w][i] + p);
+            }
           }
-          const int32_t x = __ldg(g.col + cur_base + p);
-          uint32_t sl = hslot(x, bits);
-          for (;;) {
-            const int32_t t = T[sl];
-            if (t == x) { atomicAdd(&s_hits[w][i], 1u); break; }
-            if (t == HT_EMPTY) break;
-            sl = (sl + 1) & mask;
+#pragma unroll
+          for (int u = 0; u < PL_UNROLL; ++u) {
+            if (ie[u] < 0) continue;
+            if (ie[u] != cur) {
+              if (cnt) atomicAdd(&s_hits[w][cur], cnt);
+              cur = ie[u];
+              cnt = 0;
+            }
+            cnt += pull_probe(tb, bitmap, bmin, span, bits, x[u]);
           }
         }
+        if (cnt) atomicAdd(&s_hits[w][cur], cnt);
         __syncwarp();
         if (e >= 0) {
           const uint32_t c = s_hits[w][lane];
@@ -1187,8 +1228,17 @@ __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint32
         }
         __syncwarp();
       }
-      k = k2;
+      // back to all zero
+      if (bitmap) {
+        for (int q = lane; q < nb; q += 32) {
+          const uint32_t d = (uint32_t)(__ldg(g.col + bb + q) - bmin);
+          if (d < span) tb[d >> 5] = 0u;
+        }
+      } else {
+        for (int q = lane; q < (1 << bits); q += 32) tb[q] = 0u;
+      }
       __syncwarp();
+      k = k2;
     }
   }
   flush_total(acc, total);

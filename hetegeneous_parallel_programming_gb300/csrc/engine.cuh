@@ -33,12 +33,15 @@ struct DevDag {
   const int32_t *col = nullptr;      // [m]
   const int32_t *src = nullptr;      // [m] row of each edge
   const uint32_t *perm = nullptr;    // [m] output slot of each edge (null: identity)
+  const int32_t *indeg = nullptr;    // [n] in-degree of each vertex in the DAG
   int restrict_after = 0;
 };
 
 // Validation: sets VF_* bits in ctx->d_flags[0].
 tc_status launch_validate(tc_ctx *ctx, const DevCSR &g, bool require_sorted_simple);
 tc_status launch_validate_rowptr(tc_ctx *ctx, const DevCSR &g);
+// in-degree of every vertex of a caller-oriented DAG (histogram of col)
+tc_status launch_indeg(tc_ctx *ctx, const int32_t *col, int64_t n, int64_t m, int32_t *indeg);
 
 // Orientation.  Phase A (before the host learns m): degree keys, rank sort,
 // kept counts per row and per block.  Phase B: compaction + relabel sort.
@@ -53,6 +56,7 @@ struct OrientBufs {
   int64_t *orowptr;            // [n+1] original-order DAG row pointers
   int64_t *nrowptr;            // [n+1] relabelled row pointers
   int64_t *dnew;               // [n+1] relabelled row lengths
+  int32_t *indeg;              // [n] DAG in-degree by relabelled id
   int32_t *mid_list, *big_list, *huge_list;  // [n] rows for the warp / block / global sorts
   unsigned *seg_counts;        // [3]
   // phase B

@@ -146,7 +146,7 @@ __global__ void mlp_reduce_kernel(const float *__restrict__ part, int nblk, cons
 }
 
 __global__ void mlp_adam_kernel(float *__restrict__ w, const float *__restrict__ g, float *__restrict__ m1,
-                                float *__restrict__ m2, float lr, float bc1, float bc2) {
+                                float *__restrict__ m2, float lr, float wd, float bc1, float bc2) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= P) return;
   const float gp = g[p];
@@ -154,7 +154,7 @@ __global__ void mlp_adam_kernel(float *__restrict__ w, const float *__restrict__
   const float v = 0.999f * m2[p] + 0.001f * gp * gp;
   m1[p] = a;
   m2[p] = v;
-  w[p] -= lr * (a / bc1) / (sqrtf(v / bc2) + 1e-8f);
+  w[p] -= lr * ((a / bc1) / (sqrtf(v / bc2) + 1e-8f) + wd * w[p]);  // decoupled weight decay (AdamW)
 }
 
 // Inference for host-supplied rows, with the plan kernel's bf16 rounding.
@@ -280,8 +280,8 @@ tc_status tc_selector_grad(tc_ctx *ctx, const float *params, const float *featur
 }
 
 tc_status tc_selector_train(tc_ctx *ctx, const float *features, const float *costs, int64_t rows, int32_t epochs,
-                            float lr, uint64_t seed, float *loss_out) {
-  if (!ctx || !features || !costs || rows < 1 || epochs < 1 || !(lr > 0))
+                            float lr, float weight_decay, uint64_t seed, float *loss_out) {
+  if (!ctx || !features || !costs || rows < 1 || epochs < 1 || !(lr > 0) || !(weight_decay >= 0))
     return set_error(ctx, TC_ERR_INVALID_ARG, "bad argument");
   TC_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
   TC_CHECK_CUDA(ctx, cudaFuncSetAttribute(mlp_fwd_bwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -327,7 +327,7 @@ tc_status tc_selector_train(tc_ctx *ctx, const float *features, const float *cos
       mlp_reduce_kernel<<<(P + 255) / 256, 256, 0, ctx->stream>>>(part, blk, lp, dg, dl);
       ++step;
       const float bc1 = 1.f - std::pow(0.9f, (float)step), bc2 = 1.f - std::pow(0.999f, (float)step);
-      mlp_adam_kernel<<<(P + 255) / 256, 256, 0, ctx->stream>>>(ctx->d_mlp, dg, m1, m2, lr, bc1, bc2);
+      mlp_adam_kernel<<<(P + 255) / 256, 256, 0, ctx->stream>>>(ctx->d_mlp, dg, m1, m2, lr, weight_decay, bc1, bc2);
     }
     TC_CHECK_CUDA(ctx, cudaGetLastError());
   }

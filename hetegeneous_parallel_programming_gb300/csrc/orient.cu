@@ -164,10 +164,17 @@ __global__ void __launch_bounds__(OR_THREADS) kept_count_kernel(const int64_t *_
 }
 
 
-__global__ void dnew_kernel(const int64_t *__restrict__ kept, const int32_t *__restrict__ rank, int64_t n,
-                            int64_t *__restrict__ dnew) {
-  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x)
-    dnew[rank[u]] = kept[u];
+// Relabelled out-degree and DAG in-degree (symmetric degree minus kept
+// out-degree) of every vertex.
+__global__ void dnew_kernel(const int64_t *__restrict__ kept, const int32_t *__restrict__ rank,
+                            const int64_t *__restrict__ rowptr, int64_t n, int64_t *__restrict__ dnew,
+                            int32_t *__restrict__ indeg) {
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t r = rank[u];
+    const int64_t k = kept[u];
+    dnew[r] = k;
+    indeg[r] = (int32_t)(rowptr[u + 1] - rowptr[u] - k);
+  }
   if (blockIdx.x == 0 && threadIdx.x == 0) dnew[n] = 0;
 }
 
@@ -234,7 +241,8 @@ tc_status orient_phase_a(tc_ctx *ctx, const DevCSR &g, OrientBufs &b) {
   }
   // original-order DAG rowptr, relabelled rowptr, and the row classes
   TC_TRY(exclusive_scan_i64(ctx, b.kept, b.orowptr, g.n + 1, b.sort_scratch, nullptr));
-  dnew_kernel<<<grid_for(ctx, g.n, 256, 8), 256, 0, ctx->stream>>>(b.kept, b.rank, g.n, b.dnew);
+  dnew_kernel<<<grid_for(ctx, g.n, 256, 8), 256, 0, ctx->stream>>>(b.kept, b.rank, g.rowptr, g.n, b.dnew,
+                                                                    b.indeg);
   TC_CHECK_LAUNCH(ctx);
   TC_TRY(exclusive_scan_i64(ctx, b.dnew, b.nrowptr, g.n + 1, b.sort_scratch, nullptr));
   TC_CHECK_CUDA(ctx, cudaMemsetAsync(b.seg_counts, 0, sizeof(unsigned) * 3, ctx->stream));
@@ -508,6 +516,7 @@ tc_status orient_phase_b(tc_ctx *ctx, const DevCSR &g, OrientBufs &b, int64_t m,
   out->col = b.ncol;
   out->src = b.nsrc;
   out->perm = want_perm ? b.perm : nullptr;
+  out->indeg = b.indeg;
   out->restrict_after = 1;
   return TC_OK;
 }
@@ -525,6 +534,21 @@ __global__ void __launch_bounds__(OR_THREADS) expand_src_kernel(const int64_t *_
     for (int k = threadIdx.x; k < t1 - t0; k += OR_THREADS) src[t0 + k] = rows[k];
     __syncthreads();
   }
+}
+
+__global__ void indeg_kernel(const int32_t *__restrict__ col, int64_t n, int64_t m, int32_t *__restrict__ indeg) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < m; e += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t v = col[e];
+    if (v >= 0 && v < n) atomicAdd(indeg + v, 1);
+  }
+}
+
+tc_status launch_indeg(tc_ctx *ctx, const int32_t *col, int64_t n, int64_t m, int32_t *indeg) {
+  TC_CHECK_CUDA(ctx, cudaMemsetAsync(indeg, 0, sizeof(int32_t) * (size_t)n, ctx->stream));
+  if (m <= 0) return TC_OK;
+  indeg_kernel<<<grid_for(ctx, m, ENTRY_TILE, 8), OR_THREADS, 0, ctx->stream>>>(col, n, m, indeg);
+  TC_CHECK_LAUNCH(ctx);
+  return TC_OK;
 }
 
 tc_status launch_expand_src(tc_ctx *ctx, const int64_t *rowptr, int64_t n, int64_t m, int32_t *src) {

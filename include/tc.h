@@ -212,10 +212,12 @@ tc_status tc_plan_arms(tc_ctx *ctx, const tc_csr *g, const tc_opts *opts, int32_
 
 /* Train the MLP cost model on the device (forward/backward/Adam kernels of
  * this library) from host arrays of features and costs; the trained weights
- * stay loaded in the ctx.  loss_out (optional) receives the final loss. */
+ * stay loaded in the ctx.  weight_decay is decoupled (AdamW: every step also
+ * scales the weights by 1 - lr * weight_decay).  loss_out (optional)
+ * receives the final loss. */
 tc_status tc_selector_train(tc_ctx *ctx, const float *features, const float *costs,
-                            int64_t tiles, int32_t epochs, float lr, uint64_t seed,
-                            float *loss_out);
+                            int64_t tiles, int32_t epochs, float lr, float weight_decay,
+                            uint64_t seed, float *loss_out);
 /* Weights as a flat float blob (TC_MLP_PARAM_COUNT floats). */
 #define TC_MLP_PARAM_COUNT (TC_MLP_FEATURES * TC_MLP_HIDDEN + TC_MLP_HIDDEN + \
                             TC_MLP_HIDDEN * TC_MLP_HIDDEN + TC_MLP_HIDDEN +   \
