@@ -1009,7 +1009,7 @@ __global__ void __launch_bounds__(BM_THREADS) bitmap_kernel(DevDag g, const uint
 // The edges of PULL tiles are grouped by target v with a counting sort
 // (in-edge histogram, exclusive scan, scatter of edge ids; tiles of other arms
 // are skipped whole, so the grouping costs nothing when no tile chose PULL).
-// A warp takes 512 grouped entries; for each run of equal v it loads N+(v)
+// A warp takes 2048 grouped entries; for each run of equal v it loads N+(v)
 // once into its shared-memory bitmap or hash table and probes, for every
 // in-edge u->v of the run, the part of N+(u) that can close a triangle (the
 // row after v in relabelled order), flattened over 32 edges at a time.  Hub
@@ -1020,8 +1020,9 @@ __global__ void __launch_bounds__(BM_THREADS) bitmap_kernel(DevDag g, const uint
 constexpr int PL_THREADS = 128;
 constexpr int PL_WARPS = PL_THREADS / 32;
 constexpr int PL_WORDS = 2048;  // per warp: a 65536-id bitmap or a 2048-slot hash table
-constexpr int PL_ITEM = 512;
+constexpr int PL_ITEM = 2048;
 constexpr int PL_UNROLL = 4;
+constexpr int PL_SHORT = 16;  // row suffixes up to this long are probed by one lane
 constexpr int PL_GROUP_THREADS = 256;
 
 // in-edge histogram of the PULL tiles' targets: cnt[v] += 1 (cnt is zeroed, n+1 long)
@@ -1059,20 +1060,98 @@ __global__ void __launch_bounds__(PL_GROUP_THREADS) pull_scatter_kernel(const in
 // N+(v)) when that window has at most PL_WORDS*32 ids, else as a hash table of
 // 2*d+(v) slots holding x+1 (0 = empty) when d+(v) <= PL_WORDS/2, else the
 // run's edges fall back to the warp pivot search.  After the run the warp
-// zeroes what it wrote.
-__device__ __forceinline__ uint32_t pull_probe(const uint32_t *tb, bool bitmap, int32_t base, uint32_t span,
-                                               int bits, int32_t x) {
-  if (bitmap) {
+// zeroes what it wrote.  Probing is edge by edge: a row suffix of at most
+// PL_SHORT entries is read by its own lane, a longer one by the whole warp
+// with PL_UNROLL coalesced loads in flight per lane.
+template <bool BITMAP>
+__device__ __forceinline__ uint32_t pull_test(const uint32_t *tb, int32_t base, uint32_t span, int bits, int32_t x) {
+  if (BITMAP) {
     const uint32_t d = (uint32_t)(x - base);
     return d < span ? (tb[d >> 5] >> (d & 31)) & 1u : 0u;
   }
   const uint32_t mask = (1u << bits) - 1u, want = (uint32_t)x + 1u;
   uint32_t sl = hslot(x, bits);
-  for (;;) {
+  for (;;) {  // ends: the table is at most half full
     const uint32_t t = tb[sl];
     if (t == want) return 1u;
     if (t == 0u) return 0u;
     sl = (sl + 1) & mask;
+  }
+}
+
+// Grouped entries [k, k2) (one target) against the warp's table.  The next
+// batch's edge ids and rows are loaded while the current batch probes.
+template <bool BITMAP>
+__device__ __forceinline__ void pull_run(const DevDag &g, const uint32_t *__restrict__ eids, int64_t k, int64_t k2,
+                                         bool have_b, const uint32_t *tb, int32_t base, uint32_t span, int bits,
+                                         int lane, uint32_t *out, unsigned long long &acc,
+                                         unsigned long long *tile_cycles, unsigned long long build_share) {
+  int64_t e_n = -1;
+  int32_t r_n = 0;
+  if (k + lane < k2) {
+    e_n = eids[k + lane];
+    if (have_b) r_n = g.src[e_n];
+  }
+  for (int64_t qb = k; qb < k2; qb += 32) {
+    const long long t0 = clock64();
+    const int64_t e = e_n;
+    const int32_t r = r_n;
+    e_n = -1;
+    if (qb + 32 + lane < k2) {  // prefetch for the next batch
+      e_n = eids[qb + 32 + lane];
+      if (have_b) r_n = g.src[e_n];
+    }
+    int64_t a0 = 0;
+    int na = 0;
+    if (e >= 0 && have_b) {
+      const int64_t re = g.rowptr[r + 1];
+      a0 = g.restrict_after ? e + 1 : g.rowptr[r];
+      na = (int)(re - a0);
+    }
+    uint32_t c = 0;
+    if (na <= PL_SHORT) {  // short suffix: this lane alone
+      const int32_t *a = g.col + a0;
+      for (int j0 = 0; j0 < na; j0 += 4) {
+        int32_t x[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) x[u] = j0 + u < na ? __ldg(a + j0 + u) : 0;
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (j0 + u < na) c += pull_test<BITMAP>(tb, base, span, bits, x[u]);
+      }
+    }
+    unsigned longm = __ballot_sync(TC_FULL_MASK, na > PL_SHORT);
+    while (longm) {  // long suffixes: the whole warp, one edge at a time
+      const int l = __ffs(longm) - 1;
+      longm &= longm - 1;
+      const long long b = __shfl_sync(TC_FULL_MASK, (long long)a0, l);
+      const int nl = __shfl_sync(TC_FULL_MASK, na, l);
+      uint32_t h = 0;
+      for (int j0 = 0; j0 < nl; j0 += 32 * PL_UNROLL) {
+        int32_t x[PL_UNROLL];
+#pragma unroll
+        for (int u = 0; u < PL_UNROLL; ++u) {
+          const int j = j0 + 32 * u + lane;
+          x[u] = j < nl ? __ldg(g.col + b + j) : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < PL_UNROLL; ++u)
+          if (j0 + 32 * u + lane < nl) h += pull_test<BITMAP>(tb, base, span, bits, x[u]);
+      }
+      h = __reduce_add_sync(TC_FULL_MASK, h);
+      if (lane == l) c = h;
+    }
+    if (e >= 0) {
+      put_edge_count(g, out, e, c);
+      acc += c;
+    }
+    if (tile_cycles) {  // share of this batch's time by the edge's probe count, plus the build share
+      const unsigned tot = __reduce_add_sync(TC_FULL_MASK, (unsigned)(e >= 0 ? na + 1 : 0));
+      if (e >= 0) {
+        const unsigned long long dt = (unsigned long long)(clock64() - t0);
+        atomicAdd(&tile_cycles[e / TILE_EDGES], dt * (unsigned long long)(na + 1) / tot + build_share);
+      }
+    }
   }
 }
 
@@ -1081,9 +1160,6 @@ __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint32
                                                          unsigned *head, uint32_t *out, unsigned long long *total,
                                                          unsigned long long *tile_cycles) {
   __shared__ uint32_t tab[PL_WARPS][PL_WORDS];
-  __shared__ int32_t s_incl[PL_WARPS][32];
-  __shared__ long long s_base[PL_WARPS][32];
-  __shared__ uint32_t s_hits[PL_WARPS][32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   uint32_t *tb = tab[w];
   for (int q = lane; q < PL_WORDS; q += 32) tb[q] = 0u;
@@ -1142,100 +1218,45 @@ __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint32
       int bits = 5;
       if (!bitmap)
         while ((1 << bits) < 2 * nb) ++bits;
-      if (bitmap) {
-        for (int q = lane; q < nb; q += 32) {
-          const uint32_t d = (uint32_t)(__ldg(g.col + bb + q) - bmin);
-          if (d < span) atomicOr(&tb[d >> 5], 1u << (d & 31));  // false only for an unsorted list
+      // build: PL_UNROLL list loads in flight per lane
+      for (int q0 = 0; q0 < nb; q0 += 32 * PL_UNROLL) {
+        int32_t x[PL_UNROLL];
+#pragma unroll
+        for (int u = 0; u < PL_UNROLL; ++u) {
+          const int q = q0 + 32 * u + lane;
+          x[u] = q < nb ? __ldg(g.col + bb + q) : 0;
         }
-      } else {
-        const uint32_t mask = (1u << bits) - 1u;
-        for (int q = lane; q < nb; q += 32) {
-          const int32_t x = __ldg(g.col + bb + q);
-          uint32_t sl = hslot(x, bits);
-          while (atomicCAS(&tb[sl], 0u, (uint32_t)x + 1u) != 0u) sl = (sl + 1) & mask;
+#pragma unroll
+        for (int u = 0; u < PL_UNROLL; ++u) {
+          if (q0 + 32 * u + lane >= nb) continue;
+          if (bitmap) {
+            const uint32_t d = (uint32_t)(x[u] - bmin);
+            if (d < span) atomicOr(&tb[d >> 5], 1u << (d & 31));  // false only for an unsorted list
+          } else {
+            const uint32_t mask = (1u << bits) - 1u;
+            uint32_t sl = hslot(x[u], bits);
+            while (atomicCAS(&tb[sl], 0u, (uint32_t)x[u] + 1u) != 0u) sl = (sl + 1) & mask;
+          }
         }
       }
       __syncwarp();
-      const unsigned long long build_share = (unsigned long long)(clock64() - tr0) / (unsigned long long)(k2 - k);
-      for (int64_t qb = k; qb < k2; qb += 32) {
-        const long long t0 = clock64();
-        const int64_t q = qb + lane;
-        int64_t e = -1;
-        int na = 0;
-        long long abase = 0;
-        if (q < k2) {
-          e = eids[q];
-          if (nb > 0) {
-            const int32_t r = g.src[e];
-            const int64_t re = g.rowptr[r + 1];
-            const int64_t a0 = g.restrict_after ? e + 1 : g.rowptr[r];
-            na = (int)(re - a0);
-            abase = a0;
-          }
-        }
-        int incl = na;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const int y = __shfl_up_sync(TC_FULL_MASK, incl, o);
-          if (lane >= o) incl += y;
-        }
-        const int P = __shfl_sync(TC_FULL_MASK, incl, 31);
-        s_incl[w][lane] = incl;
-        s_base[w][lane] = abase - (long long)(incl - na);
-        s_hits[w][lane] = 0u;
-        __syncwarp();
-        // flattened probes, PL_UNROLL loads in flight per lane; hits count in
-        // a register while the lane stays on one edge
-        int i = 0, cur = -1;
-        uint32_t cnt = 0;
-        for (int pb = 0; pb < P; pb += 32 * PL_UNROLL) {
-          int32_t x[PL_UNROLL];
-          int ie[PL_UNROLL];
-#pragma unroll
-          for (int u = 0; u < PL_UNROLL; ++u) {
-            const int p = pb + 32 * u + lane;
-            ie[u] = -1;
-            x[u] = 0;
-            if (p < P) {
-              while (s_incl[w][i] <= p) ++i;
-              ie[u] = i;
-              x[u] = __ldg(g.col + s_base[w][i] + p);
-            }
-          }
-#pragma unroll
-          for (int u = 0; u < PL_UNROLL; ++u) {
-            if (ie[u] < 0) continue;
-            if (ie[u] != cur) {
-              if (cnt) atomicAdd(&s_hits[w][cur], cnt);
-              cur = ie[u];
-              cnt = 0;
-            }
-            cnt += pull_probe(tb, bitmap, bmin, span, bits, x[u]);
-          }
-        }
-        if (cnt) atomicAdd(&s_hits[w][cur], cnt);
-        __syncwarp();
-        if (e >= 0) {
-          const uint32_t c = s_hits[w][lane];
-          put_edge_count(g, out, e, c);
-          acc += c;
-          if (tile_cycles) {  // share of this batch's time, by the edge's probe count
-            const unsigned long long dt = (unsigned long long)(clock64() - t0);
-            const unsigned long long part = dt * (unsigned long long)(na + 1) /
-                                            (unsigned long long)(P + min((int64_t)32, k2 - qb));
-            atomicAdd(&tile_cycles[e / TILE_EDGES], part + build_share);
-          }
-        }
-        __syncwarp();
-      }
-      // back to all zero
-      if (bitmap) {
+      const unsigned long long build_share =
+          tile_cycles ? (unsigned long long)(clock64() - tr0) / (unsigned long long)(k2 - k) : 0ull;
+      if (bitmap)
+        pull_run<true>(g, eids, k, k2, nb > 0, tb, bmin, span, bits, lane, out, acc, tile_cycles, build_share);
+      else
+        pull_run<false>(g, eids, k, k2, nb > 0, tb, bmin, span, bits, lane, out, acc, tile_cycles, build_share);
+      __syncwarp();
+      // back to all zero: the touched word range, or the list's own words
+      // when the window is much wider than the list
+      const int words = bitmap ? (int)((span + 31u) >> 5) : (1 << bits);
+      if (!bitmap || words <= 8 * nb) {
+        for (int q = lane; q < words; q += 32) tb[q] = 0u;
+      } else {
         for (int q = lane; q < nb; q += 32) {
           const uint32_t d = (uint32_t)(__ldg(g.col + bb + q) - bmin);
           if (d < span) tb[d >> 5] = 0u;
         }
-      } else {
-        for (int q = lane; q < (1 << bits); q += 32) tb[q] = 0u;
       }
       __syncwarp();
       k = k2;
