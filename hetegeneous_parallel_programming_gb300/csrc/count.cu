@@ -1006,10 +1006,11 @@ __global__ void __launch_bounds__(BM_THREADS) bitmap_kernel(DevDag g, const uint
 
 // ---- PULL (edges grouped by target) ---------------------------------------------------
 //
-// The edges of PULL tiles are grouped by target v with a counting sort
-// (in-edge histogram, exclusive scan, scatter of edge ids; tiles of other arms
-// are skipped whole, so the grouping costs nothing when no tile chose PULL).
-// A warp takes 2048 grouped entries; for each run of equal v it loads N+(v)
+// The edges of PULL tiles are grouped by target v with a counting sort per
+// source block (in-edge histogram, exclusive scan, scatter of edge and row
+// ids; tiles of other arms are skipped whole, so the grouping costs little
+// when no tile chose PULL).
+// A warp takes up to 2048 grouped entries; for each run of equal v it loads N+(v)
 // once into its shared-memory bitmap or hash table and probes, for every
 // in-edge u->v of the run, the part of N+(u) that can close a triangle (the
 // row after v in relabelled order), flattened over 32 edges at a time.  Hub
@@ -1020,77 +1021,163 @@ __global__ void __launch_bounds__(BM_THREADS) bitmap_kernel(DevDag g, const uint
 constexpr int PL_THREADS = 128;
 constexpr int PL_WARPS = PL_THREADS / 32;
 constexpr int PL_WORDS = 2048;  // per warp: a 65536-id bitmap or a 2048-slot hash table
-constexpr int PL_ITEM = 2048;
+constexpr int PL_ITEM = 2048;      // largest work chunk (grouped entries)
+constexpr int PL_ITEM_MIN = 256;   // smallest, near the end of the work
 constexpr int PL_UNROLL = 4;
+constexpr int PL_VUNROLL = 2;      // 16-byte row-suffix loads in flight per lane
 constexpr int PL_SHORT = 16;  // row suffixes up to this long are probed by one lane
 constexpr int PL_GROUP_THREADS = 256;
 
-// in-edge histogram of the PULL tiles' targets: cnt[v] += 1 (cnt is zeroed, n+1 long)
+// Edges whose target list fits the bitmap window (hub targets: most edges,
+// many in-edges each) are grouped per source block (a range of tiles, so a
+// range of rows): the blocks' groups are concatenated in block order, and the
+// PULL kernel's warps, which take work in order, then probe the rows of about
+// one block at a time, a slice of the DAG small enough to stay in L2.  Edges
+// whose target needs the hash table (wide id window, few in-edges) follow in
+// one group over all blocks, so their runs are not split block by block.
+constexpr int64_t PL_BLOCK_TILES = 2560;  // 10.5M edges, 42 MB of adjacency
+constexpr int PL_MAX_BLOCKS = 64;
+
+// wide[v] = 1 when N+(v) spans more ids than the bitmap window holds
+__global__ void pull_wide_kernel(const int64_t *__restrict__ rowptr, const int32_t *__restrict__ col, int64_t n,
+                                 uint8_t *__restrict__ wide) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = rowptr[v], e = rowptr[v + 1];
+    wide[v] = (e > b && (uint32_t)(col[e - 1] - col[b]) + 1u > (uint32_t)PL_WORDS * 32u) ? 1 : 0;
+  }
+}
+
+// in-edge histogram of the targets (with wide[v] == want) of the PULL tiles in
+// [t0, t1): cnt[v] += 1
 __global__ void __launch_bounds__(PL_GROUP_THREADS) pull_hist_kernel(const int32_t *__restrict__ col,
-                                                                    const int32_t *__restrict__ arm, int64_t m,
+                                                                    const int32_t *__restrict__ arm,
+                                                                    const uint8_t *__restrict__ wide, int want,
+                                                                    int64_t m, int64_t t0, int64_t t1,
                                                                     unsigned long long *__restrict__ cnt) {
-  const int64_t T = (m + TILE_EDGES - 1) / TILE_EDGES;
-  for (int64_t t = blockIdx.x; t < T; t += gridDim.x) {
+  for (int64_t t = t0 + blockIdx.x; t < t1; t += gridDim.x) {
     if (arm[t] != TC_ARM_PULL) continue;
     const int64_t e1 = min(m, (t + 1) * TILE_EDGES);
-    for (int64_t e = t * TILE_EDGES + threadIdx.x; e < e1; e += PL_GROUP_THREADS)
-      atomicAdd(cnt + __ldg(col + e), 1ull);
+    for (int64_t e = t * TILE_EDGES + threadIdx.x; e < e1; e += PL_GROUP_THREADS) {
+      const int32_t v = __ldg(col + e);
+      if (wide[v] == want) atomicAdd(cnt + v, 1ull);
+    }
   }
 }
 
-// pos[v] starts at the exclusive scan of the histogram; each edge takes the
-// next slot of its target's group
+// pos[v] starts at the exclusive scan of the block's histogram; each edge
+// takes the next slot of its target's group, after the *base earlier blocks'
+// edges, and records its row
 __global__ void __launch_bounds__(PL_GROUP_THREADS) pull_scatter_kernel(const int32_t *__restrict__ col,
-                                                                       const int32_t *__restrict__ arm, int64_t m,
+                                                                       const int32_t *__restrict__ src,
+                                                                       const int32_t *__restrict__ arm,
+                                                                       const uint8_t *__restrict__ wide, int want,
+                                                                       int64_t m, int64_t t0, int64_t t1,
                                                                        unsigned long long *__restrict__ pos,
-                                                                       uint32_t *__restrict__ eids) {
-  const int64_t T = (m + TILE_EDGES - 1) / TILE_EDGES;
-  for (int64_t t = blockIdx.x; t < T; t += gridDim.x) {
+                                                                       const long long *__restrict__ base,
+                                                                       uint32_t *__restrict__ eids,
+                                                                       int32_t *__restrict__ rids) {
+  const long long b0 = *base;
+  for (int64_t t = t0 + blockIdx.x; t < t1; t += gridDim.x) {
     if (arm[t] != TC_ARM_PULL) continue;
     const int64_t e1 = min(m, (t + 1) * TILE_EDGES);
-    for (int64_t e = t * TILE_EDGES + threadIdx.x; e < e1; e += PL_GROUP_THREADS)
-      eids[atomicAdd(pos + __ldg(col + e), 1ull)] = (uint32_t)e;
+    for (int64_t e = t * TILE_EDGES + threadIdx.x; e < e1; e += PL_GROUP_THREADS) {
+      const int32_t v = __ldg(col + e);
+      if (wide[v] != want) continue;
+      const long long slot = b0 + (long long)atomicAdd(pos + v, 1ull);
+      eids[slot] = (uint32_t)e;
+      rids[slot] = __ldg(src + e);
+    }
   }
 }
 
-// `eids` holds the grouped edge ids; `npull` points at their number.
+// base[b + 1] = base[b] + edges grouped in block b (pos[n], which no edge targets)
+__global__ void pull_base_kernel(const unsigned long long *__restrict__ count, long long *__restrict__ base, int b) {
+  base[b + 1] = base[b] + (long long)*count;
+}
+
+// `eids`/`rids` hold the grouped edge ids and their rows; `npull` points at
+// their number.
 //
-// Each warp owns PL_WORDS words of shared memory, all zero between runs.  A
-// run of target v uses them as a bitmap over v's id window (min..max of
-// N+(v)) when that window has at most PL_WORDS*32 ids, else as a hash table of
-// 2*d+(v) slots holding x+1 (0 = empty) when d+(v) <= PL_WORDS/2, else the
-// run's edges fall back to the warp pivot search.  After the run the warp
-// zeroes what it wrote.  Probing is edge by edge: a row suffix of at most
-// PL_SHORT entries is read by its own lane, a longer one by the whole warp
-// with PL_UNROLL coalesced loads in flight per lane.
+// Each warp owns PL_WORDS words of shared memory, all zero between runs, and
+// a guard word after them that is never written.  A run of target v uses the
+// words as a bitmap over v's id window (min..max of N+(v)) when that window
+// has at most PL_WORDS*32 ids, else as a hash table of 4-slot buckets holding
+// x+1 (0 = empty; at most two entries per bucket on average) when
+// d+(v) <= PL_WORDS/2, else the run's edges fall back to the warp pivot
+// search.  Bucket slots fill in order and an entry moves on to the next
+// bucket only when all four are taken, so one 16-byte read answers a probe
+// unless that bucket is full.  After the run the warp zeroes what it wrote.  A
+// bitmap test needs no bounds check: ids outside the window land on zero
+// words or, past the table, on the guard word.  Probing is edge by edge: a
+// row suffix of at most PL_SHORT entries is read by its own lane, a longer
+// one by the whole warp with 16-byte loads (four entries per lane per load).
+constexpr int PL_ROW = PL_WORDS + 4;  // words per warp: table + guard, 16-byte rows
+
 template <bool BITMAP>
-__device__ __forceinline__ uint32_t pull_test(const uint32_t *tb, int32_t base, uint32_t span, int bits, int32_t x) {
+__device__ __forceinline__ uint32_t pull_test(const uint32_t *tb, int32_t base, int bits, int32_t x) {
   if (BITMAP) {
     const uint32_t d = (uint32_t)(x - base);
-    return d < span ? (tb[d >> 5] >> (d & 31)) & 1u : 0u;
+    return (tb[min(d >> 5, (uint32_t)PL_WORDS)] >> (d & 31)) & 1u;
   }
   const uint32_t mask = (1u << bits) - 1u, want = (uint32_t)x + 1u;
-  uint32_t sl = hslot(x, bits);
+  const uint4 *B = reinterpret_cast<const uint4 *>(tb);
+  uint32_t b = hslot(x, bits);
   for (;;) {  // ends: the table is at most half full
-    const uint32_t t = tb[sl];
-    if (t == want) return 1u;
-    if (t == 0u) return 0u;
-    sl = (sl + 1) & mask;
+    const uint4 q = B[b];
+    if (q.x == want || q.y == want || q.z == want || q.w == want) return 1u;
+    if (q.w == 0u) return 0u;  // bucket never overflowed
+    b = (b + 1) & mask;
   }
+}
+
+template <bool BITMAP>
+__device__ __forceinline__ uint32_t pull_test4(const uint32_t *tb, int32_t base, int bits, int4 q) {
+  return pull_test<BITMAP>(tb, base, bits, q.x) + pull_test<BITMAP>(tb, base, bits, q.y) +
+         pull_test<BITMAP>(tb, base, bits, q.z) + pull_test<BITMAP>(tb, base, bits, q.w);
+}
+
+// Hits of the whole list A[0, nl) (warp-wide; every lane returns its part).
+// The unaligned head, the first 16-byte loads and the tail are all issued
+// before the first test, so a list of up to 32*4*PL_VUNROLL entries costs one
+// memory round trip.
+template <bool BITMAP>
+__device__ __forceinline__ uint32_t pull_list(const int32_t *__restrict__ A, int nl, const uint32_t *tb,
+                                              int32_t base, int bits, int lane) {
+  const int head = min(nl, (int)((4u - (uint32_t)((reinterpret_cast<uintptr_t>(A) >> 2) & 3u)) & 3u));
+  const int4 *V = reinterpret_cast<const int4 *>(A + head);  // 16-byte aligned
+  const int rest = nl - head, nv = rest >> 2, tail = rest & 3;
+  const int32_t xh = lane < head ? __ldg(A + lane) : 0;
+  const int32_t xt = lane < tail ? __ldg(A + head + 4 * nv + lane) : 0;
+  uint32_t h = 0;
+  for (int v0 = 0; v0 < nv; v0 += 32 * PL_VUNROLL) {
+    int4 q[PL_VUNROLL];
+#pragma unroll
+    for (int u = 0; u < PL_VUNROLL; ++u) {
+      const int j = v0 + 32 * u + lane;
+      q[u] = j < nv ? __ldg(V + j) : make_int4(0, 0, 0, 0);
+    }
+#pragma unroll
+    for (int u = 0; u < PL_VUNROLL; ++u)
+      if (v0 + 32 * u + lane < nv) h += pull_test4<BITMAP>(tb, base, bits, q[u]);
+  }
+  if (lane < head) h += pull_test<BITMAP>(tb, base, bits, xh);
+  if (lane < tail) h += pull_test<BITMAP>(tb, base, bits, xt);
+  return h;
 }
 
 // Grouped entries [k, k2) (one target) against the warp's table.  The next
 // batch's edge ids and rows are loaded while the current batch probes.
 template <bool BITMAP>
-__device__ __forceinline__ void pull_run(const DevDag &g, const uint32_t *__restrict__ eids, int64_t k, int64_t k2,
-                                         bool have_b, const uint32_t *tb, int32_t base, uint32_t span, int bits,
+__device__ __forceinline__ void pull_run(const DevDag &g, const uint32_t *__restrict__ eids,
+                                         const int32_t *__restrict__ rids, int64_t k, int64_t k2,
+                                         bool have_b, const uint32_t *tb, int32_t base, int bits,
                                          int lane, uint32_t *out, unsigned long long &acc,
                                          unsigned long long *tile_cycles, unsigned long long build_share) {
   int64_t e_n = -1;
   int32_t r_n = 0;
   if (k + lane < k2) {
     e_n = eids[k + lane];
-    if (have_b) r_n = g.src[e_n];
+    r_n = rids[k + lane];
   }
   for (int64_t qb = k; qb < k2; qb += 32) {
     const long long t0 = clock64();
@@ -1099,7 +1186,7 @@ __device__ __forceinline__ void pull_run(const DevDag &g, const uint32_t *__rest
     e_n = -1;
     if (qb + 32 + lane < k2) {  // prefetch for the next batch
       e_n = eids[qb + 32 + lane];
-      if (have_b) r_n = g.src[e_n];
+      r_n = rids[qb + 32 + lane];
     }
     int64_t a0 = 0;
     int na = 0;
@@ -1117,7 +1204,7 @@ __device__ __forceinline__ void pull_run(const DevDag &g, const uint32_t *__rest
         for (int u = 0; u < 4; ++u) x[u] = j0 + u < na ? __ldg(a + j0 + u) : 0;
 #pragma unroll
         for (int u = 0; u < 4; ++u)
-          if (j0 + u < na) c += pull_test<BITMAP>(tb, base, span, bits, x[u]);
+          if (j0 + u < na) c += pull_test<BITMAP>(tb, base, bits, x[u]);
       }
     }
     unsigned longm = __ballot_sync(TC_FULL_MASK, na > PL_SHORT);
@@ -1126,19 +1213,7 @@ __device__ __forceinline__ void pull_run(const DevDag &g, const uint32_t *__rest
       longm &= longm - 1;
       const long long b = __shfl_sync(TC_FULL_MASK, (long long)a0, l);
       const int nl = __shfl_sync(TC_FULL_MASK, na, l);
-      uint32_t h = 0;
-      for (int j0 = 0; j0 < nl; j0 += 32 * PL_UNROLL) {
-        int32_t x[PL_UNROLL];
-#pragma unroll
-        for (int u = 0; u < PL_UNROLL; ++u) {
-          const int j = j0 + 32 * u + lane;
-          x[u] = j < nl ? __ldg(g.col + b + j) : 0;
-        }
-#pragma unroll
-        for (int u = 0; u < PL_UNROLL; ++u)
-          if (j0 + 32 * u + lane < nl) h += pull_test<BITMAP>(tb, base, span, bits, x[u]);
-      }
-      h = __reduce_add_sync(TC_FULL_MASK, h);
+      const uint32_t h = __reduce_add_sync(TC_FULL_MASK, pull_list<BITMAP>(g.col + b, nl, tb, base, bits, lane));
       if (lane == l) c = h;
     }
     if (e >= 0) {
@@ -1155,28 +1230,43 @@ __device__ __forceinline__ void pull_run(const DevDag &g, const uint32_t *__rest
   }
 }
 
+// Work is taken in chunks of grouped entries that shrink from PL_ITEM to
+// PL_ITEM_MIN as the remaining work falls, so the last chunks end together.
+__device__ __forceinline__ unsigned pull_next_chunk(unsigned *head, int64_t np, int64_t warps, int64_t *end) {
+  const int64_t seen = (int64_t)*(volatile unsigned *)head;
+  const int64_t left = np - seen;
+  int64_t chunk = left / warps;
+  chunk = chunk >= PL_ITEM ? PL_ITEM : chunk <= PL_ITEM_MIN ? PL_ITEM_MIN : chunk;
+  const unsigned start = atomicAdd(head, (unsigned)chunk);
+  *end = min(np, (int64_t)start + chunk);
+  return start;
+}
+
 __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint32_t *__restrict__ eids,
-                                                         const unsigned long long *__restrict__ npull,
+                                                         const int32_t *__restrict__ rids,
+                                                         const long long *__restrict__ npull,
                                                          unsigned *head, uint32_t *out, unsigned long long *total,
                                                          unsigned long long *tile_cycles) {
-  __shared__ uint32_t tab[PL_WARPS][PL_WORDS];
+  __shared__ __align__(16) uint32_t tab[PL_WARPS][PL_ROW];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   uint32_t *tb = tab[w];
-  for (int q = lane; q < PL_WORDS; q += 32) tb[q] = 0u;
+  for (int q = lane; q < PL_ROW; q += 32) tb[q] = 0u;
   __syncwarp();
   const int64_t np = (int64_t)*npull;
-  const int64_t items = (np + PL_ITEM - 1) / PL_ITEM;
+  const int64_t warps = (int64_t)gridDim.x * PL_WARPS;
   unsigned long long acc = 0;
   for (;;) {
     unsigned it = 0;
-    if (lane == 0) it = atomicAdd(head, 1u);
+    int64_t p1 = 0;
+    if (lane == 0) it = pull_next_chunk(head, np, warps, &p1);
     it = __shfl_sync(TC_FULL_MASK, it, 0);
-    if ((int64_t)it >= items) break;
-    const int64_t p0 = (int64_t)it * PL_ITEM, p1 = min(np, p0 + PL_ITEM);
+    p1 = __shfl_sync(TC_FULL_MASK, (long long)p1, 0);
+    if ((int64_t)it >= np) break;
+    const int64_t p0 = (int64_t)it;
     for (int64_t k = p0; k < p1;) {
       const long long tr0 = clock64();  // profiling: the run's search and table build are its edges' cost too
       const int32_t v = __ldg(g.col + eids[k]);
-      // end of the run of target v inside this item
+      // end of the run of target v inside this chunk
       int64_t k2 = k + 1;
       for (;;) {
         const int64_t j = k2 + lane;
@@ -1215,9 +1305,9 @@ __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint32
         k = k2;
         continue;
       }
-      int bits = 5;
+      int bits = 3;  // hash mode: log2 of the bucket count, one bucket per entry up to 512 entries
       if (!bitmap)
-        while ((1 << bits) < 2 * nb) ++bits;
+        while ((1 << bits) < nb && (4 << bits) < PL_WORDS) ++bits;
       // build: PL_UNROLL list loads in flight per lane
       for (int q0 = 0; q0 < nb; q0 += 32 * PL_UNROLL) {
         int32_t x[PL_UNROLL];
@@ -1232,10 +1322,16 @@ __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint32
           if (bitmap) {
             const uint32_t d = (uint32_t)(x[u] - bmin);
             if (d < span) atomicOr(&tb[d >> 5], 1u << (d & 31));  // false only for an unsorted list
-          } else {
+          } else {  // first free slot of the first bucket with room
             const uint32_t mask = (1u << bits) - 1u;
-            uint32_t sl = hslot(x[u], bits);
-            while (atomicCAS(&tb[sl], 0u, (uint32_t)x[u] + 1u) != 0u) sl = (sl + 1) & mask;
+            uint32_t b = hslot(x[u], bits);
+            for (;;) {
+              uint32_t *bk = tb + 4 * b;
+              if (atomicCAS(bk, 0u, (uint32_t)x[u] + 1u) == 0u || atomicCAS(bk + 1, 0u, (uint32_t)x[u] + 1u) == 0u ||
+                  atomicCAS(bk + 2, 0u, (uint32_t)x[u] + 1u) == 0u || atomicCAS(bk + 3, 0u, (uint32_t)x[u] + 1u) == 0u)
+                break;
+              b = (b + 1) & mask;
+            }
           }
         }
       }
@@ -1243,15 +1339,16 @@ __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint32
       const unsigned long long build_share =
           tile_cycles ? (unsigned long long)(clock64() - tr0) / (unsigned long long)(k2 - k) : 0ull;
       if (bitmap)
-        pull_run<true>(g, eids, k, k2, nb > 0, tb, bmin, span, bits, lane, out, acc, tile_cycles, build_share);
+        pull_run<true>(g, eids, rids, k, k2, nb > 0, tb, bmin, bits, lane, out, acc, tile_cycles, build_share);
       else
-        pull_run<false>(g, eids, k, k2, nb > 0, tb, bmin, span, bits, lane, out, acc, tile_cycles, build_share);
+        pull_run<false>(g, eids, rids, k, k2, nb > 0, tb, bmin, bits, lane, out, acc, tile_cycles, build_share);
       __syncwarp();
-      // back to all zero: the touched word range, or the list's own words
-      // when the window is much wider than the list
-      const int words = bitmap ? (int)((span + 31u) >> 5) : (1 << bits);
-      if (!bitmap || words <= 8 * nb) {
-        for (int q = lane; q < words; q += 32) tb[q] = 0u;
+      // back to all zero: the touched word range with 16-byte stores, or the
+      // list's own words when the window is much wider than the list
+      const int words = bitmap ? (int)((span + 31u) >> 5) : (4 << bits);
+      if (!bitmap || words <= 16 * nb) {
+        uint4 *t4 = reinterpret_cast<uint4 *>(tb);
+        for (int q = lane; q < (words + 3) >> 2; q += 32) t4[q] = make_uint4(0u, 0u, 0u, 0u);
       } else {
         for (int q = lane; q < nb; q += 32) {
           const uint32_t d = (uint32_t)(__ldg(g.col + bb + q) - bmin);
@@ -1325,6 +1422,9 @@ size_t count_scratch_bytes(const tc_ctx *ctx, int64_t n, int64_t m) {
   sz.take<unsigned long long>(TC_NUM_ARMS);
   sz.take<int64_t>(n + 1);
   sz.take<uint32_t>(m);
+  sz.take<int32_t>(m);
+  sz.take<long long>(PL_MAX_BLOCKS + 2);
+  sz.take<uint8_t>(n);
   return sz.used + count_sort_scratch_bytes(ctx, n, T) + 256;
 }
 
@@ -1343,6 +1443,9 @@ tc_status count_carve(const tc_ctx *ctx, int64_t n, int64_t m, Bump &bump, Count
   cb.arm_bytes = bump.take<unsigned long long>(TC_NUM_ARMS);
   cb.pull_pos = bump.take<int64_t>(n + 1);
   cb.pull_eids = bump.take<uint32_t>(m);
+  cb.pull_rids = bump.take<int32_t>(m);
+  cb.pull_base = bump.take<long long>(PL_MAX_BLOCKS + 2);
+  cb.pull_wide = bump.take<uint8_t>(n);
   cb.sort_scratch = bump.take<char>((int64_t)count_sort_scratch_bytes(ctx, n, T));
   return bump.overflow ? TC_ERR_OOM : TC_OK;
 }
@@ -1353,23 +1456,41 @@ constexpr int PIN_BYTES = PIN_QOFF + TC_NUM_ARMS + 1;  // TC_NUM_ARMS uint64
 static_assert(PIN_BYTES + TC_NUM_ARMS <= 64, "pinned scratch holds 64 words");
 static_assert(sizeof(((tc_ctx *)nullptr)->ev) / sizeof(cudaEvent_t) >= 10 + TC_NUM_ARMS, "one event per arm");
 
-// PULL arm: group the PULL tiles' edges by target, then count.  Launched with
-// a grid for every tile (each block skips tiles of other arms) since the
-// number of PULL tiles is known only on the device.
-static tc_status run_pull(tc_ctx *ctx, const DevDag &g, CountBufs &cb, uint32_t *out, int64_t T) {
+// PULL arm: group the PULL tiles' edges by (source block, target), then
+// count.  The grouping kernels run over every tile of a block (each skips
+// tiles of other arms) since the number of PULL tiles is known only on the
+// device.
+static tc_status pull_group_round(tc_ctx *ctx, const DevDag &g, CountBufs &cb, int64_t t0, int64_t t1, int want,
+                                  int b) {
   unsigned long long *pos = reinterpret_cast<unsigned long long *>(cb.pull_pos);
+  const int gblocks = (int)std::min<int64_t>(t1 - t0, (int64_t)ctx->num_sms * 8);
   TC_CHECK_CUDA(ctx, cudaMemsetAsync(cb.pull_pos, 0, sizeof(int64_t) * (g.n + 1), ctx->stream));
-  const int gblocks = (int)std::min<int64_t>(T, (int64_t)ctx->num_sms * 8);
-  pull_hist_kernel<<<gblocks, PL_GROUP_THREADS, 0, ctx->stream>>>(g.col, cb.arm, g.m, pos);
+  pull_hist_kernel<<<gblocks, PL_GROUP_THREADS, 0, ctx->stream>>>(g.col, cb.arm, cb.pull_wide, want, g.m, t0, t1,
+                                                                  pos);
   TC_CHECK_LAUNCH(ctx);
   TC_TRY(exclusive_scan_i64(ctx, cb.pull_pos, cb.pull_pos, g.n + 1, cb.sort_scratch, nullptr));
-  pull_scatter_kernel<<<gblocks, PL_GROUP_THREADS, 0, ctx->stream>>>(g.col, cb.arm, g.m, pos, cb.pull_eids);
+  pull_scatter_kernel<<<gblocks, PL_GROUP_THREADS, 0, ctx->stream>>>(g.col, g.src, cb.arm, cb.pull_wide, want, g.m,
+                                                                     t0, t1, pos, cb.pull_base + b, cb.pull_eids,
+                                                                     cb.pull_rids);
   TC_CHECK_LAUNCH(ctx);
-  // after the scatter pos[v] is the end of v's group; pos[n] (no edge targets
-  // n) still holds the number of grouped edges
+  // pos[n] (no edge targets n) still holds the round's number of grouped edges
+  pull_base_kernel<<<1, 1, 0, ctx->stream>>>(pos + g.n, cb.pull_base, b);
+  TC_CHECK_LAUNCH(ctx);
+  return TC_OK;
+}
+
+static tc_status run_pull(tc_ctx *ctx, const DevDag &g, CountBufs &cb, uint32_t *out, int64_t T) {
+  const int64_t per_block = std::max<int64_t>(PL_BLOCK_TILES, (T + PL_MAX_BLOCKS - 1) / PL_MAX_BLOCKS);
+  const int nblocks = (int)((T + per_block - 1) / per_block);
+  pull_wide_kernel<<<grid_for(ctx, g.n, 256, 8), 256, 0, ctx->stream>>>(g.rowptr, g.col, g.n, cb.pull_wide);
+  TC_CHECK_LAUNCH(ctx);
+  TC_CHECK_CUDA(ctx, cudaMemsetAsync(cb.pull_base, 0, sizeof(long long), ctx->stream));
+  for (int b = 0; b < nblocks; ++b)  // bitmap targets, block by block
+    TC_TRY(pull_group_round(ctx, g, cb, b * per_block, std::min(T, (b + 1) * per_block), 0, b));
+  TC_TRY(pull_group_round(ctx, g, cb, 0, T, 1, nblocks));  // hash targets, all blocks at once
   const int grid = ctx->num_sms * ctx->arm_blocks_per_sm[TC_ARM_PULL];
-  pull_kernel<<<grid, PL_THREADS, 0, ctx->stream>>>(g, cb.pull_eids, pos + g.n, ctx->d_heads + TC_ARM_PULL, out,
-                                                    ctx->d_total, cb.tile_cycles);
+  pull_kernel<<<grid, PL_THREADS, 0, ctx->stream>>>(g, cb.pull_eids, cb.pull_rids, cb.pull_base + nblocks + 1,
+                                                    ctx->d_heads + TC_ARM_PULL, out, ctx->d_total, cb.tile_cycles);
   TC_CHECK_LAUNCH(ctx);
   return TC_OK;
 }

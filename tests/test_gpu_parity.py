@@ -70,6 +70,18 @@ def test_seeded_graphs_bit_exact(engine, spec):
     assert total == ref_total
 
 
+def test_pull_source_blocks_bit_exact(engine):
+    """R-MAT scale 20 has more oriented edges than one PULL source block
+    (2560 tiles of 4096 edges), so its grouped edges span several blocks."""
+    rowptr, colidx = gen_csr(tc.GenSpec("rmat", scale=20, edge_factor=16, seed=4))
+    ref_total, ref_pe, _, ocol = oracle.triangles(rowptr, colidx, per_edge=True)
+    assert len(ocol) > 2560 * tc.TILE_EDGES
+    for sel, arm in [("fixed", None), ("force", 9)]:
+        total, per_edge, st = engine.count(rowptr, colidx, selector=sel, force_arm=arm, edge_counts=True)
+        assert total == ref_total, (sel, arm)
+        assert np.array_equal(per_edge, ref_pe), (sel, arm)
+
+
 def test_device_generators_match_host(engine):
     import torch
     for spec in [tc.GenSpec("er", n=100000, avg_degree=8, seed=11),
