@@ -44,7 +44,8 @@ __global__ void __launch_bounds__(BT_THREADS) globalize_kernel(const int64_t *__
   const int64_t tiles = (nnz + ENTRY_TILE - 1) / ENTRY_TILE;
   for (int64_t t = blockIdx.x; t < tiles; t += gridDim.x) {
     const int64_t t0 = t * ENTRY_TILE, t1 = min(nnz, t0 + ENTRY_TILE);
-    expand_rows<ENTRY_TILE>(rowptr, n, t0, t1, rows, scan_tmp);
+    int64_t hint = -1;  // tiles of one block are not contiguous here
+    expand_rows<ENTRY_TILE>(rowptr, n, t0, t1, rows, scan_tmp, hint);
     for (int k = threadIdx.x; k < t1 - t0; k += BT_THREADS) {
       const int u = rows[k];
       const int32_t v = col[t0 + k];

@@ -157,13 +157,26 @@ __device__ __forceinline__ int64_t row_of_entry(const int64_t *__restrict__ rowp
 }
 
 // Row of every entry of the tile [t0, t_end) of a CSR, into rows[0..t_end-t0)
-// (shared, TILE slots).  All threads of the block call it; ends synchronised.
+// (shared, TILE slots).  All threads of the block call it with the same
+// `hint`: -1, or the row of entry t0 - 1 (the previous tile's last entry),
+// which it updates to the row of entry t_end - 1.  With a hint one warp finds
+// the tile's first row among the next 32 rows instead of a binary search over
+// rowptr.  Ends synchronised.
 template <int TILE>
 __device__ void expand_rows(const int64_t *__restrict__ rowptr, int64_t n, int64_t t0, int64_t t_end,
-                            int *rows, int *scan_tmp) {
+                            int *rows, int *scan_tmp, int64_t &hint) {
   __shared__ int64_t s_first;
   for (int i = threadIdx.x; i < TILE; i += blockDim.x) rows[i] = -1;
-  if (threadIdx.x == 0) s_first = row_of_entry(rowptr, n, t0);
+  if (threadIdx.x < 32) {
+    int64_t r = -1;
+    if (hint >= 0) {  // first r >= hint with rowptr[r + 1] > t0
+      const int64_t rr = hint + threadIdx.x;
+      const unsigned bal = __ballot_sync(TC_FULL_MASK, rr < n && rowptr[rr + 1] > t0);
+      if (bal) r = hint + __ffs(bal) - 1;
+    }
+    if (r < 0) r = row_of_entry(rowptr, n, t0);
+    if (threadIdx.x == 0) s_first = r;
+  }
   __syncthreads();
   const int64_t r0 = s_first;
   if (threadIdx.x == 0) rows[0] = (int)r0;
@@ -208,6 +221,7 @@ __device__ void expand_rows(const int64_t *__restrict__ rowptr, int64_t n, int64
     rows[base + k] = carry;
   }
   __syncthreads();
+  hint = rows[t_end - t0 - 1];
 }
 
 // ---- host-side launch helpers shared by the .cu files --------------------------

@@ -16,7 +16,7 @@ constexpr int OR_PER = ENTRY_TILE / OR_THREADS;  // 8 entries per thread per til
 
 void orient_geometry(const tc_ctx *ctx, int64_t nnz, int *G, int64_t *chunk) {
   int64_t tiles = (nnz + ENTRY_TILE - 1) / ENTRY_TILE;
-  int64_t g = (int64_t)ctx->num_sms * 4;
+  int64_t g = (int64_t)ctx->num_sms * 6;  // resident at once: 6 blocks of 256 per SM
   if (g > tiles) g = tiles;
   if (g < 1) g = 1;
   *chunk = ((tiles + g - 1) / g) * ENTRY_TILE;
@@ -52,7 +52,8 @@ __global__ void __launch_bounds__(OR_THREADS) validate_col_kernel(const int64_t 
   const int64_t tiles = (nnz + ENTRY_TILE - 1) / ENTRY_TILE;
   for (int64_t t = blockIdx.x; t < tiles; t += gridDim.x) {
     const int64_t t0 = t * ENTRY_TILE, t1 = min(nnz, t0 + ENTRY_TILE);
-    if (simple) expand_rows<ENTRY_TILE>(rowptr, n, t0, t1, rows, scan_tmp);
+    int64_t hint = -1;  // tiles of one block are not contiguous here
+    if (simple) expand_rows<ENTRY_TILE>(rowptr, n, t0, t1, rows, scan_tmp, hint);
 #pragma unroll
     for (int k = 0; k < OR_PER; ++k) {
       const int64_t e = t0 + k * OR_THREADS + threadIdx.x;
@@ -112,7 +113,7 @@ __global__ void rank_kernel(const uint64_t *__restrict__ keys, int64_t n, uint64
 // pass over the adjacency (ids in range, rows strictly ascending, no self
 // loops), so a validated call reads colidx once here instead of twice.
 template <bool VALIDATE>
-__global__ void __launch_bounds__(OR_THREADS) kept_count_kernel(const int64_t *__restrict__ rowptr,
+__global__ void __launch_bounds__(OR_THREADS, 6) kept_count_kernel(const int64_t *__restrict__ rowptr,
                                                                const int32_t *__restrict__ col, int64_t n,
                                                                int64_t nnz, int64_t chunk,
                                                                const int32_t *__restrict__ rank,
@@ -126,9 +127,19 @@ __global__ void __launch_bounds__(OR_THREADS) kept_count_kernel(const int64_t *_
   unsigned long long mine = 0;
   unsigned f = 0;
   const int lane = threadIdx.x & 31;
+  int64_t hint = -1;
   for (int64_t t0 = b; t0 < e_end; t0 += ENTRY_TILE) {
     const int64_t t1 = min(e_end, t0 + ENTRY_TILE);
-    expand_rows<ENTRY_TILE>(rowptr, n, t0, t1, rows, scan_tmp);
+    expand_rows<ENTRY_TILE>(rowptr, n, t0, t1, rows, scan_tmp, hint);
+    // all loads of the tile first, then the rank gathers, then the counts
+    int32_t vv[OR_PER], rv[OR_PER];
+#pragma unroll
+    for (int k = 0; k < OR_PER; ++k) {
+      const int64_t e = t0 + k * OR_THREADS + threadIdx.x;
+      vv[k] = e < t1 ? col[e] : -1;
+    }
+#pragma unroll
+    for (int k = 0; k < OR_PER; ++k) rv[k] = vv[k] >= 0 && (int64_t)vv[k] < n ? rank[vv[k]] : -1;
 #pragma unroll
     for (int k = 0; k < OR_PER; ++k) {
       const int64_t e = t0 + k * OR_THREADS + threadIdx.x;
@@ -136,8 +147,8 @@ __global__ void __launch_bounds__(OR_THREADS) kept_count_kernel(const int64_t *_
       int u = -1;
       if (e < t1) {
         u = rows[e - t0];
-        const int32_t v = col[e];
-        keep = u >= 0 && v >= 0 && (int64_t)v < n && rank[v] > rank[u];
+        const int32_t v = vv[k];
+        keep = u >= 0 && rv[k] >= 0 && rv[k] > rank[u];
         if (VALIDATE) {
           if (v < 0 || (int64_t)v >= n) f |= VF_ID_RANGE;
           else if (u == v) f |= VF_SELF_LOOP;
@@ -258,54 +269,78 @@ tc_status orient_phase_a(tc_ctx *ctx, const DevCSR &g, OrientBufs &b) {
 // slot nrowptr[rank u] + (kpos - orowptr[u]) with value rank v; rows are then
 // sorted by value.
 template <bool VALS, bool DAGCOL, bool RELABEL>
-__global__ void __launch_bounds__(OR_THREADS) place_kernel(const int64_t *__restrict__ rowptr,
+__global__ void __launch_bounds__(OR_THREADS, 6) place_kernel(const int64_t *__restrict__ rowptr,
                                                           const int32_t *__restrict__ col, int64_t n, int64_t nnz,
                                                           int64_t chunk, const int32_t *__restrict__ rank,
                                                           const int64_t *__restrict__ boff,
                                                           const int64_t *__restrict__ orowptr,
                                                           const int64_t *__restrict__ nrowptr,
-                                                          int32_t *__restrict__ ncol, uint32_t *__restrict__ perm,
+                                                          int32_t *__restrict__ ncol, int32_t *__restrict__ nsrc,
+                                                          uint32_t *__restrict__ perm,
                                                           int32_t *__restrict__ dag_col) {
   __shared__ int rows[ENTRY_TILE];
   __shared__ int scan_tmp[32];
-  __shared__ long long stmp[33];
+  __shared__ long long s_wbase[OR_THREADS / 32 + 1];
+  constexpr int NW = OR_THREADS / 32;
   const int64_t b = (int64_t)blockIdx.x * chunk, e_end = min(nnz, b + chunk);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned lt = lanemask_lt();
   long long carry = boff[blockIdx.x];
+  int64_t hint = -1;
   for (int64_t t0 = b; t0 < e_end; t0 += ENTRY_TILE) {
     const int64_t t1 = min(e_end, t0 + ENTRY_TILE);
-    expand_rows<ENTRY_TILE>(rowptr, n, t0, t1, rows, scan_tmp);
-    int32_t vv[OR_PER];
-    unsigned keepm = 0;
-    const int first = threadIdx.x * OR_PER;
+    expand_rows<ENTRY_TILE>(rowptr, n, t0, t1, rows, scan_tmp, hint);
+    // warp w owns entries [w*32*OR_PER, (w+1)*32*OR_PER) of the tile, lane-
+    // strided so every load is coalesced; entry order = (k, lane) order
+    const int wbase = warp * 32 * OR_PER;
+    int32_t vv[OR_PER], rv[OR_PER], uu[OR_PER];
 #pragma unroll
     for (int k = 0; k < OR_PER; ++k) {
-      const int64_t e = t0 + first + k;
-      vv[k] = -1;
-      if (e < t1) {
-        const int u = rows[first + k];
-        const int32_t v = col[e];
-        if (u >= 0 && v >= 0 && (int64_t)v < n && rank[v] > rank[u]) {
-          keepm |= 1u << k;
-          vv[k] = v;
-        }
-      }
+      const int i = wbase + k * 32 + lane;
+      const bool in = t0 + i < t1;
+      vv[k] = in ? col[t0 + i] : -1;
+      uu[k] = in ? rows[i] : -1;
     }
-    long long tot;
-    long long pos = carry + block_exclusive_scan<long long>((long long)__popc(keepm), stmp, &tot);
+#pragma unroll
+    for (int k = 0; k < OR_PER; ++k) rv[k] = vv[k] >= 0 && (int64_t)vv[k] < n ? rank[vv[k]] : -1;
+    unsigned bal[OR_PER];
+    int cnt = 0;
 #pragma unroll
     for (int k = 0; k < OR_PER; ++k) {
-      if (keepm & (1u << k)) {
-        const int u = rows[first + k];
+      const bool keep = uu[k] >= 0 && rv[k] >= 0 && rv[k] > rank[uu[k]];
+      bal[k] = __ballot_sync(TC_FULL_MASK, keep);
+      cnt += __popc(bal[k]);
+    }
+    if (lane == 0) s_wbase[warp] = cnt;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      long long acc = 0;
+      for (int w = 0; w < NW; ++w) {
+        const long long c = s_wbase[w];
+        s_wbase[w] = acc;
+        acc += c;
+      }
+      s_wbase[NW] = acc;
+    }
+    __syncthreads();
+    long long pos = carry + s_wbase[warp];
+#pragma unroll
+    for (int k = 0; k < OR_PER; ++k) {
+      if ((bal[k] >> lane) & 1u) {
+        const long long p = pos + __popc(bal[k] & lt);
+        const int u = uu[k];
         if (RELABEL) {
-          const long long dst = nrowptr[rank[u]] + (pos - orowptr[u]);
-          ncol[dst] = rank[vv[k]];
-          if (VALS) perm[dst] = (uint32_t)pos;
+          const int32_t ru = rank[u];
+          const long long dst = nrowptr[ru] + (p - orowptr[u]);
+          ncol[dst] = rv[k];
+          nsrc[dst] = ru;
+          if (VALS) perm[dst] = (uint32_t)p;
         }
-        if (DAGCOL) dag_col[pos] = vv[k];
-        ++pos;
+        if (DAGCOL) dag_col[p] = vv[k];
       }
+      pos += __popc(bal[k]);
     }
-    carry += tot;
+    carry += s_wbase[NW];
     __syncthreads();
   }
 }
@@ -498,7 +533,7 @@ tc_status orient_phase_b(tc_ctx *ctx, const DevCSR &g, OrientBufs &b, int64_t m,
   if (g.nnz > 0 && m > 0) {
 #define TC_PLACE(V, D, R)                                                                                        \
   place_kernel<V, D, R><<<b.G, OR_THREADS, 0, ctx->stream>>>(g.rowptr, g.col, g.n, g.nnz, b.chunk, b.rank, b.bcount, \
-                                                             b.orowptr, b.nrowptr, b.ncol, b.perm, b.dag_col)
+                                                             b.orowptr, b.nrowptr, b.ncol, b.nsrc, b.perm, b.dag_col)
     if (!relabel) TC_PLACE(false, true, false);
     else if (want_perm && want_dag_cols) TC_PLACE(true, true, true);
     else if (want_perm) TC_PLACE(true, false, true);
@@ -508,8 +543,9 @@ tc_status orient_phase_b(tc_ctx *ctx, const DevCSR &g, OrientBufs &b, int64_t m,
     TC_CHECK_LAUNCH(ctx);
   }
   if (!relabel) return TC_OK;
+  // place_kernel wrote every entry's row into nsrc; the row sorts keep
+  // entries inside their rows
   if (m > 1) TC_TRY(want_perm ? launch_row_sorts<true>(ctx, g, b) : launch_row_sorts<false>(ctx, g, b));
-  TC_TRY(launch_expand_src(ctx, b.nrowptr, g.n, m, b.nsrc));
   out->n = g.n;
   out->m = m;
   out->rowptr = b.nrowptr;
@@ -530,7 +566,8 @@ __global__ void __launch_bounds__(OR_THREADS) expand_src_kernel(const int64_t *_
   const int64_t tiles = (m + ENTRY_TILE - 1) / ENTRY_TILE;
   for (int64_t t = blockIdx.x; t < tiles; t += gridDim.x) {
     const int64_t t0 = t * ENTRY_TILE, t1 = min(m, t0 + ENTRY_TILE);
-    expand_rows<ENTRY_TILE>(rowptr, n, t0, t1, rows, scan_tmp);
+    int64_t hint = -1;  // tiles of one block are not contiguous here
+    expand_rows<ENTRY_TILE>(rowptr, n, t0, t1, rows, scan_tmp, hint);
     for (int k = threadIdx.x; k < t1 - t0; k += OR_THREADS) src[t0 + k] = rows[k];
     __syncthreads();
   }
