@@ -1028,71 +1028,61 @@ constexpr int PL_VUNROLL = 2;      // 16-byte row-suffix loads in flight per lan
 constexpr int PL_SHORT = 16;  // row suffixes up to this long are probed by one lane
 constexpr int PL_GROUP_THREADS = 256;
 
-// Edges whose target list fits the bitmap window (hub targets: most edges,
-// many in-edges each) are grouped per source block (a range of tiles, so a
-// range of rows): the blocks' groups are concatenated in block order, and the
-// PULL kernel's warps, which take work in order, then probe the rows of about
-// one block at a time, a slice of the DAG small enough to stay in L2.  Edges
-// whose target needs the hash table (wide id window, few in-edges) follow in
-// one group over all blocks, so their runs are not split block by block.
-constexpr int64_t PL_BLOCK_TILES = 2560;  // 10.5M edges, 42 MB of adjacency
+// One counting sort groups the PULL tiles' edges.  A target among the top
+// PL_HUB ids (ids are degree ranks) always fits the bitmap window, since all
+// of N+(v) lies in (v, n); those targets, the hubs that most edges point to,
+// are grouped per source block (a range of tiles, so a range of rows): key
+// block * PL_HUB + (v - hub0).  The blocks' groups come first, in block
+// order, and the PULL kernel's warps, which take work in order, then probe
+// the rows of about one block at a time, a slice of the DAG small enough to
+// stay in L2.  Every other target (few in-edges; its list may need the hash
+// table) is grouped over all blocks at once, key B * PL_HUB + v, so its runs
+// are not split block by block.
+constexpr int64_t PL_HUB = (int64_t)PL_WORDS * 32;  // 65536
+constexpr int64_t PL_BLOCK_TILES = 2560;            // 10.5M edges, 42 MB of adjacency
 constexpr int PL_MAX_BLOCKS = 64;
 
-// wide[v] = 1 when N+(v) spans more ids than the bitmap window holds
-__global__ void pull_wide_kernel(const int64_t *__restrict__ rowptr, const int32_t *__restrict__ col, int64_t n,
-                                 uint8_t *__restrict__ wide) {
-  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t b = rowptr[v], e = rowptr[v + 1];
-    wide[v] = (e > b && (uint32_t)(col[e - 1] - col[b]) + 1u > (uint32_t)PL_WORDS * 32u) ? 1 : 0;
+struct PullKeys {
+  int64_t hub0;         // first hub id: n - min(n, PL_HUB)
+  int64_t block_edges;  // edges per source block
+  int64_t global0;      // first key of the non-hub part: blocks * PL_HUB
+  __device__ __forceinline__ int64_t key(int64_t e, int32_t v) const {
+    return v >= hub0 ? (e / block_edges) * PL_HUB + (v - hub0) : global0 + v;
   }
-}
+};
 
-// in-edge histogram of the targets (with wide[v] == want) of the PULL tiles in
-// [t0, t1): cnt[v] += 1
+// key histogram of the PULL tiles' edges: cnt[key] += 1
 __global__ void __launch_bounds__(PL_GROUP_THREADS) pull_hist_kernel(const int32_t *__restrict__ col,
-                                                                    const int32_t *__restrict__ arm,
-                                                                    const uint8_t *__restrict__ wide, int want,
-                                                                    int64_t m, int64_t t0, int64_t t1,
-                                                                    unsigned long long *__restrict__ cnt) {
-  for (int64_t t = t0 + blockIdx.x; t < t1; t += gridDim.x) {
+                                                                    const int32_t *__restrict__ arm, int64_t m,
+                                                                    PullKeys pk, unsigned long long *__restrict__ cnt) {
+  const int64_t T = (m + TILE_EDGES - 1) / TILE_EDGES;
+  for (int64_t t = blockIdx.x; t < T; t += gridDim.x) {
     if (arm[t] != TC_ARM_PULL) continue;
     const int64_t e1 = min(m, (t + 1) * TILE_EDGES);
-    for (int64_t e = t * TILE_EDGES + threadIdx.x; e < e1; e += PL_GROUP_THREADS) {
-      const int32_t v = __ldg(col + e);
-      if (wide[v] == want) atomicAdd(cnt + v, 1ull);
-    }
+    for (int64_t e = t * TILE_EDGES + threadIdx.x; e < e1; e += PL_GROUP_THREADS)
+      atomicAdd(cnt + pk.key(e, __ldg(col + e)), 1ull);
   }
 }
 
-// pos[v] starts at the exclusive scan of the block's histogram; each edge
-// takes the next slot of its target's group, after the *base earlier blocks'
-// edges, and records its row
+// pos[key] starts at the exclusive scan of the histogram; each edge takes the
+// next slot of its key's group and records its row
 __global__ void __launch_bounds__(PL_GROUP_THREADS) pull_scatter_kernel(const int32_t *__restrict__ col,
                                                                        const int32_t *__restrict__ src,
-                                                                       const int32_t *__restrict__ arm,
-                                                                       const uint8_t *__restrict__ wide, int want,
-                                                                       int64_t m, int64_t t0, int64_t t1,
+                                                                       const int32_t *__restrict__ arm, int64_t m,
+                                                                       PullKeys pk,
                                                                        unsigned long long *__restrict__ pos,
-                                                                       const long long *__restrict__ base,
                                                                        uint32_t *__restrict__ eids,
                                                                        int32_t *__restrict__ rids) {
-  const long long b0 = *base;
-  for (int64_t t = t0 + blockIdx.x; t < t1; t += gridDim.x) {
+  const int64_t T = (m + TILE_EDGES - 1) / TILE_EDGES;
+  for (int64_t t = blockIdx.x; t < T; t += gridDim.x) {
     if (arm[t] != TC_ARM_PULL) continue;
     const int64_t e1 = min(m, (t + 1) * TILE_EDGES);
     for (int64_t e = t * TILE_EDGES + threadIdx.x; e < e1; e += PL_GROUP_THREADS) {
-      const int32_t v = __ldg(col + e);
-      if (wide[v] != want) continue;
-      const long long slot = b0 + (long long)atomicAdd(pos + v, 1ull);
+      const long long slot = (long long)atomicAdd(pos + pk.key(e, __ldg(col + e)), 1ull);
       eids[slot] = (uint32_t)e;
       rids[slot] = __ldg(src + e);
     }
   }
-}
-
-// base[b + 1] = base[b] + edges grouped in block b (pos[n], which no edge targets)
-__global__ void pull_base_kernel(const unsigned long long *__restrict__ count, long long *__restrict__ base, int b) {
-  base[b + 1] = base[b] + (long long)*count;
 }
 
 // `eids`/`rids` hold the grouped edge ids and their rows; `npull` points at
@@ -1244,7 +1234,7 @@ __device__ __forceinline__ unsigned pull_next_chunk(unsigned *head, int64_t np, 
 
 __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint32_t *__restrict__ eids,
                                                          const int32_t *__restrict__ rids,
-                                                         const long long *__restrict__ npull,
+                                                         const unsigned long long *__restrict__ npull,
                                                          unsigned *head, uint32_t *out, unsigned long long *total,
                                                          unsigned long long *tile_cycles) {
   __shared__ __align__(16) uint32_t tab[PL_WARPS][PL_ROW];
@@ -1403,8 +1393,10 @@ tc_status init_arm_occupancy(tc_ctx *ctx) {
   return TC_OK;
 }
 
+static int64_t pull_key_count(int64_t n, int64_t T, PullKeys *pk);
+
 static size_t count_sort_scratch_bytes(const tc_ctx *ctx, int64_t n, int64_t T) {
-  return std::max(radix_sort_scratch_bytes(ctx, T > 0 ? T : 1), scan_scratch_bytes(ctx, n + 1));
+  return std::max(radix_sort_scratch_bytes(ctx, T > 0 ? T : 1), scan_scratch_bytes(ctx, pull_key_count(n, T, nullptr) + 1));
 }
 
 size_t count_scratch_bytes(const tc_ctx *ctx, int64_t n, int64_t m) {
@@ -1420,11 +1412,9 @@ size_t count_scratch_bytes(const tc_ctx *ctx, int64_t n, int64_t m) {
   sz.take<unsigned long long>(T);
   sz.take<unsigned long long>(T);
   sz.take<unsigned long long>(TC_NUM_ARMS);
-  sz.take<int64_t>(n + 1);
+  sz.take<int64_t>(pull_key_count(n, T, nullptr) + 1);
   sz.take<uint32_t>(m);
   sz.take<int32_t>(m);
-  sz.take<long long>(PL_MAX_BLOCKS + 2);
-  sz.take<uint8_t>(n);
   return sz.used + count_sort_scratch_bytes(ctx, n, T) + 256;
 }
 
@@ -1441,11 +1431,9 @@ tc_status count_carve(const tc_ctx *ctx, int64_t n, int64_t m, Bump &bump, Count
   cb.tile_cycles = want_cycles ? cyc : nullptr;
   cb.tile_bytes = bump.take<unsigned long long>(T);
   cb.arm_bytes = bump.take<unsigned long long>(TC_NUM_ARMS);
-  cb.pull_pos = bump.take<int64_t>(n + 1);
+  cb.pull_pos = bump.take<int64_t>(pull_key_count(n, T, nullptr) + 1);
   cb.pull_eids = bump.take<uint32_t>(m);
   cb.pull_rids = bump.take<int32_t>(m);
-  cb.pull_base = bump.take<long long>(PL_MAX_BLOCKS + 2);
-  cb.pull_wide = bump.take<uint8_t>(n);
   cb.sort_scratch = bump.take<char>((int64_t)count_sort_scratch_bytes(ctx, n, T));
   return bump.overflow ? TC_ERR_OOM : TC_OK;
 }
@@ -1456,40 +1444,36 @@ constexpr int PIN_BYTES = PIN_QOFF + TC_NUM_ARMS + 1;  // TC_NUM_ARMS uint64
 static_assert(PIN_BYTES + TC_NUM_ARMS <= 64, "pinned scratch holds 64 words");
 static_assert(sizeof(((tc_ctx *)nullptr)->ev) / sizeof(cudaEvent_t) >= 10 + TC_NUM_ARMS, "one event per arm");
 
-// PULL arm: group the PULL tiles' edges by (source block, target), then
-// count.  The grouping kernels run over every tile of a block (each skips
-// tiles of other arms) since the number of PULL tiles is known only on the
-// device.
-static tc_status pull_group_round(tc_ctx *ctx, const DevDag &g, CountBufs &cb, int64_t t0, int64_t t1, int want,
-                                  int b) {
-  unsigned long long *pos = reinterpret_cast<unsigned long long *>(cb.pull_pos);
-  const int gblocks = (int)std::min<int64_t>(t1 - t0, (int64_t)ctx->num_sms * 8);
-  TC_CHECK_CUDA(ctx, cudaMemsetAsync(cb.pull_pos, 0, sizeof(int64_t) * (g.n + 1), ctx->stream));
-  pull_hist_kernel<<<gblocks, PL_GROUP_THREADS, 0, ctx->stream>>>(g.col, cb.arm, cb.pull_wide, want, g.m, t0, t1,
-                                                                  pos);
-  TC_CHECK_LAUNCH(ctx);
-  TC_TRY(exclusive_scan_i64(ctx, cb.pull_pos, cb.pull_pos, g.n + 1, cb.sort_scratch, nullptr));
-  pull_scatter_kernel<<<gblocks, PL_GROUP_THREADS, 0, ctx->stream>>>(g.col, g.src, cb.arm, cb.pull_wide, want, g.m,
-                                                                     t0, t1, pos, cb.pull_base + b, cb.pull_eids,
-                                                                     cb.pull_rids);
-  TC_CHECK_LAUNCH(ctx);
-  // pos[n] (no edge targets n) still holds the round's number of grouped edges
-  pull_base_kernel<<<1, 1, 0, ctx->stream>>>(pos + g.n, cb.pull_base, b);
-  TC_CHECK_LAUNCH(ctx);
-  return TC_OK;
+// Number of keys of the PULL grouping of a graph with n vertices and T tiles.
+static int64_t pull_key_count(int64_t n, int64_t T, PullKeys *pk) {
+  const int64_t per_block = std::max<int64_t>(PL_BLOCK_TILES, (T + PL_MAX_BLOCKS - 1) / PL_MAX_BLOCKS);
+  const int64_t blocks = std::max<int64_t>(1, (T + per_block - 1) / per_block);
+  if (pk) {
+    pk->hub0 = n - std::min<int64_t>(n, PL_HUB);
+    pk->block_edges = per_block * TILE_EDGES;
+    pk->global0 = blocks * PL_HUB;
+  }
+  return blocks * PL_HUB + n;
 }
 
+// PULL arm: group the PULL tiles' edges (one counting sort), then count.  The
+// grouping kernels run over every tile (each skips tiles of other arms) since
+// the number of PULL tiles is known only on the device.
 static tc_status run_pull(tc_ctx *ctx, const DevDag &g, CountBufs &cb, uint32_t *out, int64_t T) {
-  const int64_t per_block = std::max<int64_t>(PL_BLOCK_TILES, (T + PL_MAX_BLOCKS - 1) / PL_MAX_BLOCKS);
-  const int nblocks = (int)((T + per_block - 1) / per_block);
-  pull_wide_kernel<<<grid_for(ctx, g.n, 256, 8), 256, 0, ctx->stream>>>(g.rowptr, g.col, g.n, cb.pull_wide);
+  PullKeys pk;
+  const int64_t K = pull_key_count(g.n, T, &pk);
+  unsigned long long *pos = reinterpret_cast<unsigned long long *>(cb.pull_pos);
+  const int gblocks = (int)std::min<int64_t>(T, (int64_t)ctx->num_sms * 8);
+  TC_CHECK_CUDA(ctx, cudaMemsetAsync(cb.pull_pos, 0, sizeof(int64_t) * (K + 1), ctx->stream));
+  pull_hist_kernel<<<gblocks, PL_GROUP_THREADS, 0, ctx->stream>>>(g.col, cb.arm, g.m, pk, pos);
   TC_CHECK_LAUNCH(ctx);
-  TC_CHECK_CUDA(ctx, cudaMemsetAsync(cb.pull_base, 0, sizeof(long long), ctx->stream));
-  for (int b = 0; b < nblocks; ++b)  // bitmap targets, block by block
-    TC_TRY(pull_group_round(ctx, g, cb, b * per_block, std::min(T, (b + 1) * per_block), 0, b));
-  TC_TRY(pull_group_round(ctx, g, cb, 0, T, 1, nblocks));  // hash targets, all blocks at once
+  TC_TRY(exclusive_scan_i64(ctx, cb.pull_pos, cb.pull_pos, K + 1, cb.sort_scratch, nullptr));
+  pull_scatter_kernel<<<gblocks, PL_GROUP_THREADS, 0, ctx->stream>>>(g.col, g.src, cb.arm, g.m, pk, pos,
+                                                                     cb.pull_eids, cb.pull_rids);
+  TC_CHECK_LAUNCH(ctx);
+  // pos[K] (no edge has key K) still holds the number of grouped edges
   const int grid = ctx->num_sms * ctx->arm_blocks_per_sm[TC_ARM_PULL];
-  pull_kernel<<<grid, PL_THREADS, 0, ctx->stream>>>(g, cb.pull_eids, cb.pull_rids, cb.pull_base + nblocks + 1,
+  pull_kernel<<<grid, PL_THREADS, 0, ctx->stream>>>(g, cb.pull_eids, cb.pull_rids, pos + K,
                                                     ctx->d_heads + TC_ARM_PULL, out, ctx->d_total, cb.tile_cycles);
   TC_CHECK_LAUNCH(ctx);
   return TC_OK;

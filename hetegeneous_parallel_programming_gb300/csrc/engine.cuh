@@ -91,11 +91,9 @@ struct CountBufs {
   unsigned long long *tile_cycles;  // [T] (optional)
   unsigned long long *tile_bytes;   // [T] algorithmic bytes per tile
   unsigned long long *arm_bytes;    // [TC_NUM_ARMS]
-  int64_t *pull_pos;      // [n+1] PULL grouping: in-edge counts, then group offsets
-  uint32_t *pull_eids;    // [m] PULL grouping: edge ids grouped by (source block, target)
+  int64_t *pull_pos;      // [keys+1] PULL grouping: key counts, then group offsets
+  uint32_t *pull_eids;    // [m] PULL grouping: edge ids grouped by key (source block, target)
   int32_t *pull_rids;     // [m] row of each grouped edge
-  long long *pull_base;   // [blocks+2] start of each source block's groups (last: wide targets)
-  uint8_t *pull_wide;     // [n] 1 when a target's list is too wide for the bitmap window
   void *sort_scratch;
 };
 size_t count_scratch_bytes(const tc_ctx *ctx, int64_t n, int64_t m);
