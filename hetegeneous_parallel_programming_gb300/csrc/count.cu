@@ -1054,13 +1054,13 @@ struct PullKeys {
 // key histogram of the PULL tiles' edges: cnt[key] += 1
 __global__ void __launch_bounds__(PL_GROUP_THREADS) pull_hist_kernel(const int32_t *__restrict__ col,
                                                                     const int32_t *__restrict__ arm, int64_t m,
-                                                                    PullKeys pk, unsigned long long *__restrict__ cnt) {
+                                                                    PullKeys pk, unsigned *__restrict__ cnt) {
   const int64_t T = (m + TILE_EDGES - 1) / TILE_EDGES;
   for (int64_t t = blockIdx.x; t < T; t += gridDim.x) {
     if (arm[t] != TC_ARM_PULL) continue;
     const int64_t e1 = min(m, (t + 1) * TILE_EDGES);
     for (int64_t e = t * TILE_EDGES + threadIdx.x; e < e1; e += PL_GROUP_THREADS)
-      atomicAdd(cnt + pk.key(e, __ldg(col + e)), 1ull);
+      atomicAdd(cnt + pk.key(e, __ldg(col + e)), 1u);
   }
 }
 
@@ -1070,7 +1070,7 @@ __global__ void __launch_bounds__(PL_GROUP_THREADS) pull_scatter_kernel(const in
                                                                        const int32_t *__restrict__ src,
                                                                        const int32_t *__restrict__ arm, int64_t m,
                                                                        PullKeys pk,
-                                                                       unsigned long long *__restrict__ pos,
+                                                                       unsigned *__restrict__ pos,
                                                                        uint32_t *__restrict__ eids,
                                                                        int32_t *__restrict__ rids) {
   const int64_t T = (m + TILE_EDGES - 1) / TILE_EDGES;
@@ -1078,7 +1078,7 @@ __global__ void __launch_bounds__(PL_GROUP_THREADS) pull_scatter_kernel(const in
     if (arm[t] != TC_ARM_PULL) continue;
     const int64_t e1 = min(m, (t + 1) * TILE_EDGES);
     for (int64_t e = t * TILE_EDGES + threadIdx.x; e < e1; e += PL_GROUP_THREADS) {
-      const long long slot = (long long)atomicAdd(pos + pk.key(e, __ldg(col + e)), 1ull);
+      const unsigned slot = atomicAdd(pos + pk.key(e, __ldg(col + e)), 1u);
       eids[slot] = (uint32_t)e;
       rids[slot] = __ldg(src + e);
     }
@@ -1234,7 +1234,7 @@ __device__ __forceinline__ unsigned pull_next_chunk(unsigned *head, int64_t np, 
 
 __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint32_t *__restrict__ eids,
                                                          const int32_t *__restrict__ rids,
-                                                         const unsigned long long *__restrict__ npull,
+                                                         const unsigned *__restrict__ npull,
                                                          unsigned *head, uint32_t *out, unsigned long long *total,
                                                          unsigned long long *tile_cycles) {
   __shared__ __align__(16) uint32_t tab[PL_WARPS][PL_ROW];
@@ -1412,7 +1412,7 @@ size_t count_scratch_bytes(const tc_ctx *ctx, int64_t n, int64_t m) {
   sz.take<unsigned long long>(T);
   sz.take<unsigned long long>(T);
   sz.take<unsigned long long>(TC_NUM_ARMS);
-  sz.take<int64_t>(pull_key_count(n, T, nullptr) + 1);
+  sz.take<uint32_t>(pull_key_count(n, T, nullptr) + 1);
   sz.take<uint32_t>(m);
   sz.take<int32_t>(m);
   return sz.used + count_sort_scratch_bytes(ctx, n, T) + 256;
@@ -1431,7 +1431,7 @@ tc_status count_carve(const tc_ctx *ctx, int64_t n, int64_t m, Bump &bump, Count
   cb.tile_cycles = want_cycles ? cyc : nullptr;
   cb.tile_bytes = bump.take<unsigned long long>(T);
   cb.arm_bytes = bump.take<unsigned long long>(TC_NUM_ARMS);
-  cb.pull_pos = bump.take<int64_t>(pull_key_count(n, T, nullptr) + 1);
+  cb.pull_pos = bump.take<uint32_t>(pull_key_count(n, T, nullptr) + 1);
   cb.pull_eids = bump.take<uint32_t>(m);
   cb.pull_rids = bump.take<int32_t>(m);
   cb.sort_scratch = bump.take<char>((int64_t)count_sort_scratch_bytes(ctx, n, T));
@@ -1462,12 +1462,12 @@ static int64_t pull_key_count(int64_t n, int64_t T, PullKeys *pk) {
 static tc_status run_pull(tc_ctx *ctx, const DevDag &g, CountBufs &cb, uint32_t *out, int64_t T) {
   PullKeys pk;
   const int64_t K = pull_key_count(g.n, T, &pk);
-  unsigned long long *pos = reinterpret_cast<unsigned long long *>(cb.pull_pos);
+  unsigned *pos = cb.pull_pos;
   const int gblocks = (int)std::min<int64_t>(T, (int64_t)ctx->num_sms * 8);
-  TC_CHECK_CUDA(ctx, cudaMemsetAsync(cb.pull_pos, 0, sizeof(int64_t) * (K + 1), ctx->stream));
+  TC_CHECK_CUDA(ctx, cudaMemsetAsync(cb.pull_pos, 0, sizeof(uint32_t) * (K + 1), ctx->stream));
   pull_hist_kernel<<<gblocks, PL_GROUP_THREADS, 0, ctx->stream>>>(g.col, cb.arm, g.m, pk, pos);
   TC_CHECK_LAUNCH(ctx);
-  TC_TRY(exclusive_scan_i64(ctx, cb.pull_pos, cb.pull_pos, K + 1, cb.sort_scratch, nullptr));
+  TC_TRY(exclusive_scan_u32(ctx, cb.pull_pos, cb.pull_pos, K + 1, cb.sort_scratch));
   pull_scatter_kernel<<<gblocks, PL_GROUP_THREADS, 0, ctx->stream>>>(g.col, g.src, cb.arm, g.m, pk, pos,
                                                                      cb.pull_eids, cb.pull_rids);
   TC_CHECK_LAUNCH(ctx);

@@ -236,6 +236,8 @@ tc_status radix_sort(tc_ctx *ctx, uint64_t *k0, uint64_t *k1, uint32_t *v0, uint
 
 // Exclusive scan of int64 values (scan.cu helpers in radix_sort.cu).
 size_t scan_scratch_bytes(const tc_ctx *ctx, int64_t N);
+// 32-bit counts whose total stays below 2^32 (scratch as for the int64 scan)
+tc_status exclusive_scan_u32(tc_ctx *ctx, const uint32_t *in, uint32_t *out, int64_t N, void *scratch);
 tc_status exclusive_scan_i64(tc_ctx *ctx, const int64_t *in, int64_t *out, int64_t N, void *scratch,
                              int64_t *d_total_out);
 

@@ -91,7 +91,7 @@ struct CountBufs {
   unsigned long long *tile_cycles;  // [T] (optional)
   unsigned long long *tile_bytes;   // [T] algorithmic bytes per tile
   unsigned long long *arm_bytes;    // [TC_NUM_ARMS]
-  int64_t *pull_pos;      // [keys+1] PULL grouping: key counts, then group offsets
+  uint32_t *pull_pos;     // [keys+1] PULL grouping: key counts, then group offsets
   uint32_t *pull_eids;    // [m] PULL grouping: edge ids grouped by key (source block, target)
   int32_t *pull_rids;     // [m] row of each grouped edge
   void *sort_scratch;

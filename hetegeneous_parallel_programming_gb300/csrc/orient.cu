@@ -384,6 +384,74 @@ __device__ void block_flip_bitonic(int32_t *key, uint32_t *val, int L) {
   }
 }
 
+// Register stages of the same network for one 32-entry chunk (one warp):
+// chunk_sort32 runs levels 2..32 completely; chunk_merge32 runs the
+// comparators at distances 16..1 of a later level (all ascending).  Slots at
+// or beyond L read as +infinity and are not written back.
+template <bool VALS>
+__device__ __forceinline__ void reg_cmp(int32_t &key, uint32_t &val, int lane, int partner) {
+  const int32_t ok = __shfl_sync(TC_FULL_MASK, key, partner);
+  const uint32_t ov = VALS ? __shfl_sync(TC_FULL_MASK, val, partner) : 0u;
+  const bool take = lane < partner ? ok < key : ok > key;
+  if (take) {
+    key = ok;
+    if (VALS) val = ov;
+  }
+}
+
+template <bool VALS, bool FULL>
+__device__ __forceinline__ void chunk_stages32(int32_t *key, uint32_t *val, int c0, int L, int lane) {
+  const int i = c0 + lane;
+  int32_t k = i < L ? key[i] : INT32_MAX;
+  uint32_t v = (VALS && i < L) ? val[i] : 0u;
+  if (FULL) {
+#pragma unroll
+    for (int lv = 2; lv <= 32; lv <<= 1) {
+      reg_cmp<VALS>(k, v, lane, lane ^ (lv - 1));
+#pragma unroll
+      for (int j = lv >> 2; j >= 1; j >>= 1) reg_cmp<VALS>(k, v, lane, lane ^ j);
+    }
+  } else {
+#pragma unroll
+    for (int j = 16; j >= 1; j >>= 1) reg_cmp<VALS>(k, v, lane, lane ^ j);
+  }
+  if (i < L) {
+    key[i] = k;
+    if (VALS) val[i] = v;
+  }
+}
+
+// The flip network for a list in shared memory of up to 32 * 32 * blocks
+// entries, by the block (SYNC_BLOCK) or by one warp: stages with comparator
+// distance >= 32 in shared memory, the rest in registers, 32 entries per
+// warp at a time.
+template <bool VALS, bool SYNC_BLOCK>
+__device__ void hybrid_flip_bitonic(int32_t *key, uint32_t *val, int L, int warp, int nwarps, int lane) {
+  int P = 32;
+  while (P < L) P <<= 1;
+  const int nth = SYNC_BLOCK ? (int)blockDim.x : 32, tid = SYNC_BLOCK ? (int)threadIdx.x : lane;
+  for (int c0 = warp * 32; c0 < P; c0 += nwarps * 32) chunk_stages32<VALS, true>(key, val, c0, L, lane);
+  if (SYNC_BLOCK) __syncthreads(); else __syncwarp();
+  for (int k = 64; k <= P; k <<= 1) {
+    const int h = k >> 1;
+    for (int t = tid; t < P / 2; t += nth) {
+      const int blk = t / h, off = t % h;
+      const int a = blk * k + off, bb = blk * k + k - 1 - off;
+      if (bb < L) cmp_swap<VALS>(key, val, a, bb);
+    }
+    if (SYNC_BLOCK) __syncthreads(); else __syncwarp();
+    for (int j = k >> 2; j >= 32; j >>= 1) {
+      for (int t = tid; t < P / 2; t += nth) {
+        const int a = (t / j) * 2 * j + (t % j), bb = a + j;
+        if (bb < L) cmp_swap<VALS>(key, val, a, bb);
+      }
+      if (SYNC_BLOCK) __syncthreads(); else __syncwarp();
+    }
+    for (int c0 = warp * 32; c0 < P; c0 += nwarps * 32) chunk_stages32<VALS, false>(key, val, c0, L, lane);
+    if (SYNC_BLOCK) __syncthreads(); else __syncwarp();
+  }
+}
+
 template <bool VALS>
 __global__ void seg_sort_warp_kernel(const int64_t *__restrict__ nrowptr, int64_t n, int32_t *__restrict__ ncol,
                                      uint32_t *__restrict__ perm) {
@@ -421,7 +489,8 @@ __global__ void seg_sort_warp_kernel(const int64_t *__restrict__ nrowptr, int64_
 }
 
 // Rows of 33..SEG_WARP_MAX entries: one warp per row sorts in its own slice
-// of shared memory with the same flip network, synchronising with __syncwarp.
+// of shared memory with the same flip network (register stages for
+// distances below 32), synchronising with __syncwarp.
 template <bool VALS>
 __global__ void __launch_bounds__(256) seg_sort_warpsmem_kernel(const int64_t *__restrict__ nrowptr,
                                                                const int32_t *__restrict__ list,
@@ -443,24 +512,7 @@ __global__ void __launch_bounds__(256) seg_sort_warpsmem_kernel(const int64_t *_
       if (VALS) val[k] = perm[b + k];
     }
     __syncwarp();
-    int P = 1;
-    while (P < L) P <<= 1;
-    for (int k = 2; k <= P; k <<= 1) {
-      const int h = k >> 1;
-      for (int t = lane; t < P / 2; t += 32) {
-        const int blk = t / h, off = t % h;
-        const int a = blk * k + off, bb = blk * k + k - 1 - off;
-        if (bb < L) cmp_swap<VALS>(key, val, a, bb);
-      }
-      __syncwarp();
-      for (int j = k >> 2; j >= 1; j >>= 1) {
-        for (int t = lane; t < P / 2; t += 32) {
-          const int a = (t / j) * 2 * j + (t % j), bb = a + j;
-          if (bb < L) cmp_swap<VALS>(key, val, a, bb);
-        }
-        __syncwarp();
-      }
-    }
+    hybrid_flip_bitonic<VALS, false>(key, val, L, 0, 1, lane);
     for (int k = lane; k < L; k += 32) {
       ncol[b + k] = key[k];
       if (VALS) perm[b + k] = val[k];
@@ -485,7 +537,7 @@ __global__ void __launch_bounds__(256) seg_sort_smem_kernel(const int64_t *__res
       if (VALS) sval[k] = perm[b + k];
     }
     __syncthreads();
-    block_flip_bitonic<VALS>(skey, sval, L);
+    hybrid_flip_bitonic<VALS, true>(skey, sval, L, threadIdx.x >> 5, blockDim.x >> 5, threadIdx.x & 31);
     for (int k = threadIdx.x; k < L; k += blockDim.x) {
       ncol[b + k] = skey[k];
       if (VALS) perm[b + k] = sval[k];

@@ -267,7 +267,8 @@ size_t scan_scratch_bytes(const tc_ctx *ctx, int64_t N) {
   return align_up((size_t)(g.G + 1) * sizeof(int64_t), 256);
 }
 
-__global__ void __launch_bounds__(SC_THREADS) sc_reduce_kernel(const int64_t *__restrict__ in, int64_t N,
+template <typename T>
+__global__ void __launch_bounds__(SC_THREADS) sc_reduce_kernel(const T *__restrict__ in, int64_t N,
                                                               int64_t chunk, int64_t *__restrict__ sums) {
   __shared__ long long tmp[33];
   const int64_t b = (int64_t)blockIdx.x * chunk, e = min(N, b + chunk);
@@ -298,7 +299,8 @@ __global__ void __launch_bounds__(1024) sc_top_kernel(int64_t *sums, int G, int6
   }
 }
 
-__global__ void __launch_bounds__(SC_THREADS) sc_down_kernel(const int64_t *in, int64_t *out, int64_t N,
+template <typename T>
+__global__ void __launch_bounds__(SC_THREADS) sc_down_kernel(const T *in, T *out, int64_t N,
                                                             int64_t chunk, const int64_t *__restrict__ sums) {
   __shared__ long long tmp[33];
   const int64_t b = (int64_t)blockIdx.x * chunk, e = min(N, b + chunk);
@@ -316,7 +318,7 @@ __global__ void __launch_bounds__(SC_THREADS) sc_down_kernel(const int64_t *in, 
     long long run = carry + block_exclusive_scan<long long>(s, tmp, &tot);
 #pragma unroll
     for (int k = 0; k < SC_IPT; ++k) {
-      if (my + k < e) out[my + k] = run;
+      if (my + k < e) out[my + k] = (T)run;
       run += x[k];
     }
     carry += tot;
@@ -328,11 +330,24 @@ tc_status exclusive_scan_i64(tc_ctx *ctx, const int64_t *in, int64_t *out, int64
   if (N <= 0) return TC_OK;
   RsGeom g = sc_geom(ctx, N);
   int64_t *sums = (int64_t *)scratch;
-  sc_reduce_kernel<<<g.G, SC_THREADS, 0, ctx->stream>>>(in, N, g.chunk, sums);
+  sc_reduce_kernel<int64_t><<<g.G, SC_THREADS, 0, ctx->stream>>>(in, N, g.chunk, sums);
   TC_CHECK_LAUNCH(ctx);
   sc_top_kernel<<<1, 1024, 0, ctx->stream>>>(sums, g.G, d_total_out);
   TC_CHECK_LAUNCH(ctx);
-  sc_down_kernel<<<g.G, SC_THREADS, 0, ctx->stream>>>(in, out, N, g.chunk, sums);
+  sc_down_kernel<int64_t><<<g.G, SC_THREADS, 0, ctx->stream>>>(in, out, N, g.chunk, sums);
+  TC_CHECK_LAUNCH(ctx);
+  return TC_OK;
+}
+
+tc_status exclusive_scan_u32(tc_ctx *ctx, const uint32_t *in, uint32_t *out, int64_t N, void *scratch) {
+  if (N <= 0) return TC_OK;
+  RsGeom g = sc_geom(ctx, N);
+  int64_t *sums = (int64_t *)scratch;
+  sc_reduce_kernel<uint32_t><<<g.G, SC_THREADS, 0, ctx->stream>>>(in, N, g.chunk, sums);
+  TC_CHECK_LAUNCH(ctx);
+  sc_top_kernel<<<1, 1024, 0, ctx->stream>>>(sums, g.G, nullptr);
+  TC_CHECK_LAUNCH(ctx);
+  sc_down_kernel<uint32_t><<<g.G, SC_THREADS, 0, ctx->stream>>>(in, out, N, g.chunk, sums);
   TC_CHECK_LAUNCH(ctx);
   return TC_OK;
 }
