@@ -1065,27 +1065,25 @@ __global__ void __launch_bounds__(PL_GROUP_THREADS) pull_hist_kernel(const int32
 }
 
 // pos[key] starts at the exclusive scan of the histogram; each edge takes the
-// next slot of its key's group and records its row
+// next slot of its key's group and stores (edge id, row) there
 __global__ void __launch_bounds__(PL_GROUP_THREADS) pull_scatter_kernel(const int32_t *__restrict__ col,
                                                                        const int32_t *__restrict__ src,
                                                                        const int32_t *__restrict__ arm, int64_t m,
                                                                        PullKeys pk,
                                                                        unsigned *__restrict__ pos,
-                                                                       uint32_t *__restrict__ eids,
-                                                                       int32_t *__restrict__ rids) {
+                                                                       uint2 *__restrict__ er) {
   const int64_t T = (m + TILE_EDGES - 1) / TILE_EDGES;
   for (int64_t t = blockIdx.x; t < T; t += gridDim.x) {
     if (arm[t] != TC_ARM_PULL) continue;
     const int64_t e1 = min(m, (t + 1) * TILE_EDGES);
     for (int64_t e = t * TILE_EDGES + threadIdx.x; e < e1; e += PL_GROUP_THREADS) {
       const unsigned slot = atomicAdd(pos + pk.key(e, __ldg(col + e)), 1u);
-      eids[slot] = (uint32_t)e;
-      rids[slot] = __ldg(src + e);
+      er[slot] = make_uint2((uint32_t)e, (uint32_t)__ldg(src + e));  // one 8-byte store
     }
   }
 }
 
-// `eids`/`rids` hold the grouped edge ids and their rows; `npull` points at
+// `er` holds the grouped (edge id, row) pairs; `npull` points at
 // their number.
 //
 // Each warp owns PL_WORDS words of shared memory, all zero between runs, and
@@ -1158,16 +1156,16 @@ __device__ __forceinline__ uint32_t pull_list(const int32_t *__restrict__ A, int
 // Grouped entries [k, k2) (one target) against the warp's table.  The next
 // batch's edge ids and rows are loaded while the current batch probes.
 template <bool BITMAP>
-__device__ __forceinline__ void pull_run(const DevDag &g, const uint32_t *__restrict__ eids,
-                                         const int32_t *__restrict__ rids, int64_t k, int64_t k2,
+__device__ __forceinline__ void pull_run(const DevDag &g, const uint2 *__restrict__ er, int64_t k, int64_t k2,
                                          bool have_b, const uint32_t *tb, int32_t base, int bits,
                                          int lane, uint32_t *out, unsigned long long &acc,
                                          unsigned long long *tile_cycles, unsigned long long build_share) {
   int64_t e_n = -1;
   int32_t r_n = 0;
   if (k + lane < k2) {
-    e_n = eids[k + lane];
-    r_n = rids[k + lane];
+    const uint2 p = er[k + lane];
+    e_n = p.x;
+    r_n = (int32_t)p.y;
   }
   for (int64_t qb = k; qb < k2; qb += 32) {
     const long long t0 = clock64();
@@ -1175,8 +1173,9 @@ __device__ __forceinline__ void pull_run(const DevDag &g, const uint32_t *__rest
     const int32_t r = r_n;
     e_n = -1;
     if (qb + 32 + lane < k2) {  // prefetch for the next batch
-      e_n = eids[qb + 32 + lane];
-      r_n = rids[qb + 32 + lane];
+      const uint2 p = er[qb + 32 + lane];
+      e_n = p.x;
+      r_n = (int32_t)p.y;
     }
     int64_t a0 = 0;
     int na = 0;
@@ -1232,8 +1231,7 @@ __device__ __forceinline__ unsigned pull_next_chunk(unsigned *head, int64_t np, 
   return start;
 }
 
-__global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint32_t *__restrict__ eids,
-                                                         const int32_t *__restrict__ rids,
+__global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint2 *__restrict__ er,
                                                          const unsigned *__restrict__ npull,
                                                          unsigned *head, uint32_t *out, unsigned long long *total,
                                                          unsigned long long *tile_cycles) {
@@ -1255,12 +1253,12 @@ __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint32
     const int64_t p0 = (int64_t)it;
     for (int64_t k = p0; k < p1;) {
       const long long tr0 = clock64();  // profiling: the run's search and table build are its edges' cost too
-      const int32_t v = __ldg(g.col + eids[k]);
+      const int32_t v = __ldg(g.col + er[k].x);
       // end of the run of target v inside this chunk
       int64_t k2 = k + 1;
       for (;;) {
         const int64_t j = k2 + lane;
-        const bool diff = j >= p1 || __ldg(g.col + eids[j]) != v;
+        const bool diff = j >= p1 || __ldg(g.col + er[j].x) != v;
         const unsigned bal = __ballot_sync(TC_FULL_MASK, diff);
         if (bal) { k2 += __ffs(bal) - 1; break; }
         k2 += 32;
@@ -1273,7 +1271,7 @@ __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint32
       if (!bitmap && nb > PL_WORDS / 2) {  // wide window and long list: warp pivot search per edge
         long long tq = tr0;
         for (int64_t q = k; q < k2; ++q) {
-          const int64_t e = eids[q];
+          const int64_t e = er[q].x;
           int32_t s;
           const EdgeLists L = edge_lists(g, e, s);
           uint32_t c = 0;
@@ -1329,9 +1327,9 @@ __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint32
       const unsigned long long build_share =
           tile_cycles ? (unsigned long long)(clock64() - tr0) / (unsigned long long)(k2 - k) : 0ull;
       if (bitmap)
-        pull_run<true>(g, eids, rids, k, k2, nb > 0, tb, bmin, bits, lane, out, acc, tile_cycles, build_share);
+        pull_run<true>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, out, acc, tile_cycles, build_share);
       else
-        pull_run<false>(g, eids, rids, k, k2, nb > 0, tb, bmin, bits, lane, out, acc, tile_cycles, build_share);
+        pull_run<false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, out, acc, tile_cycles, build_share);
       __syncwarp();
       // back to all zero: the touched word range with 16-byte stores, or the
       // list's own words when the window is much wider than the list
@@ -1413,8 +1411,7 @@ size_t count_scratch_bytes(const tc_ctx *ctx, int64_t n, int64_t m) {
   sz.take<unsigned long long>(T);
   sz.take<unsigned long long>(TC_NUM_ARMS);
   sz.take<uint32_t>(pull_key_count(n, T, nullptr) + 1);
-  sz.take<uint32_t>(m);
-  sz.take<int32_t>(m);
+  sz.take<uint2>(m);
   return sz.used + count_sort_scratch_bytes(ctx, n, T) + 256;
 }
 
@@ -1432,8 +1429,7 @@ tc_status count_carve(const tc_ctx *ctx, int64_t n, int64_t m, Bump &bump, Count
   cb.tile_bytes = bump.take<unsigned long long>(T);
   cb.arm_bytes = bump.take<unsigned long long>(TC_NUM_ARMS);
   cb.pull_pos = bump.take<uint32_t>(pull_key_count(n, T, nullptr) + 1);
-  cb.pull_eids = bump.take<uint32_t>(m);
-  cb.pull_rids = bump.take<int32_t>(m);
+  cb.pull_er = bump.take<uint2>(m);
   cb.sort_scratch = bump.take<char>((int64_t)count_sort_scratch_bytes(ctx, n, T));
   return bump.overflow ? TC_ERR_OOM : TC_OK;
 }
@@ -1469,11 +1465,11 @@ static tc_status run_pull(tc_ctx *ctx, const DevDag &g, CountBufs &cb, uint32_t 
   TC_CHECK_LAUNCH(ctx);
   TC_TRY(exclusive_scan_u32(ctx, cb.pull_pos, cb.pull_pos, K + 1, cb.sort_scratch));
   pull_scatter_kernel<<<gblocks, PL_GROUP_THREADS, 0, ctx->stream>>>(g.col, g.src, cb.arm, g.m, pk, pos,
-                                                                     cb.pull_eids, cb.pull_rids);
+                                                                     cb.pull_er);
   TC_CHECK_LAUNCH(ctx);
   // pos[K] (no edge has key K) still holds the number of grouped edges
   const int grid = ctx->num_sms * ctx->arm_blocks_per_sm[TC_ARM_PULL];
-  pull_kernel<<<grid, PL_THREADS, 0, ctx->stream>>>(g, cb.pull_eids, cb.pull_rids, pos + K,
+  pull_kernel<<<grid, PL_THREADS, 0, ctx->stream>>>(g, cb.pull_er, pos + K,
                                                     ctx->d_heads + TC_ARM_PULL, out, ctx->d_total, cb.tile_cycles);
   TC_CHECK_LAUNCH(ctx);
   return TC_OK;

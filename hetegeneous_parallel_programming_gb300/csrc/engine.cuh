@@ -92,8 +92,7 @@ struct CountBufs {
   unsigned long long *tile_bytes;   // [T] algorithmic bytes per tile
   unsigned long long *arm_bytes;    // [TC_NUM_ARMS]
   uint32_t *pull_pos;     // [keys+1] PULL grouping: key counts, then group offsets
-  uint32_t *pull_eids;    // [m] PULL grouping: edge ids grouped by key (source block, target)
-  int32_t *pull_rids;     // [m] row of each grouped edge
+  uint2 *pull_er;         // [m] PULL grouping: (edge id, row) grouped by key (source block, target)
   void *sort_scratch;
 };
 size_t count_scratch_bytes(const tc_ctx *ctx, int64_t n, int64_t m);
