@@ -286,6 +286,13 @@ def engine_arm(args, rank, world, local_rank, dist):
             "roofline": {"bound": "hbm", "kernel": f"arm:{arm}", "achieved": round(achieved, 1), "peak": hbm,
                          "unit": "GB/s", "frac": round(achieved / hbm, 4), "traffic": traffic,
                          "peak_kind": f"{kind} copy bandwidth",
+                         "alg_bytes": "4*(d+(u)+d+(v))+4 per oriented edge: both lists read once per edge, as a "
+                                      "merge would; PULL reads each target list once per run of edges, so frac "
+                                      "can exceed 1",
+                         "dram_achieved": (round(traffic / (st["ms_arm"][arm] * 1e-3) / 1e9, 1)
+                                           if traffic and st["ms_arm"][arm] > 0 else None),
+                         "dram_frac": (round(traffic / (st["ms_arm"][arm] * 1e-3) / 1e9 / hbm, 4)
+                                       if traffic and st["ms_arm"][arm] > 0 else None),
                          "count_phase": {"alg_bytes": int(st["alg_bytes"]),
                                          "achieved": round(st["alg_bytes"] / (st["ms_count"] * 1e-3) / 1e9, 1)
                                          if st["ms_count"] > 0 else None}},
