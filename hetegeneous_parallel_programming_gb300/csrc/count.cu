@@ -1025,6 +1025,7 @@ constexpr int PL_ITEM = 2048;      // largest work chunk (grouped entries)
 constexpr int PL_ITEM_MIN = 256;   // smallest, near the end of the work
 constexpr int PL_UNROLL = 4;
 constexpr int PL_VUNROLL = 2;      // 16-byte row-suffix loads in flight per lane
+constexpr int PL_FUNROLL = 4;      // flattened probing: loads in flight per lane
 constexpr int PL_SHORT = 16;  // row suffixes up to this long are probed by one lane
 constexpr int PL_GROUP_THREADS = 256;
 
@@ -1219,6 +1220,84 @@ __device__ __forceinline__ void pull_run(const DevDag &g, const uint2 *__restric
   }
 }
 
+// The same run when only the total is wanted (no per-edge output): the row
+// suffixes of a batch of 32 edges are probed as one flattened sequence, lane
+// p of a pass reading entry p, so loads stay coalesced, short suffixes idle
+// no lanes, and the next edge's loads issue while this one's are tested.
+// Each lane walks its positions upwards and keeps the edge it is in (end and
+// base of the suffix) in registers, from the batch's prefix sums in shared
+// memory.
+template <bool BITMAP>
+__device__ __forceinline__ void pull_run_total(const DevDag &g, const uint2 *__restrict__ er, int64_t k, int64_t k2,
+                                               bool have_b, const uint32_t *tb, int32_t base, int bits, int lane,
+                                               int32_t *s_end, long long *s_base, unsigned long long &acc,
+                                               unsigned long long *tile_cycles, unsigned long long build_share) {
+  int64_t e_n = -1;
+  int32_t r_n = 0;
+  if (k + lane < k2) {
+    const uint2 p = er[k + lane];
+    e_n = p.x;
+    r_n = (int32_t)p.y;
+  }
+  for (int64_t qb = k; qb < k2; qb += 32) {
+    const long long t0 = clock64();
+    const int64_t e = e_n;
+    const int32_t r = r_n;
+    e_n = -1;
+    if (qb + 32 + lane < k2) {  // prefetch for the next batch
+      const uint2 p = er[qb + 32 + lane];
+      e_n = p.x;
+      r_n = (int32_t)p.y;
+    }
+    int64_t a0 = 0;
+    int na = 0;
+    if (e >= 0 && have_b) {
+      const int64_t re = g.rowptr[r + 1];
+      a0 = g.restrict_after ? e + 1 : g.rowptr[r];
+      na = (int)(re - a0);
+    }
+    int incl = na;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(TC_FULL_MASK, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const int P = __shfl_sync(TC_FULL_MASK, incl, 31);
+    s_end[lane] = incl;
+    s_base[lane] = (long long)a0 - (long long)(incl - na);  // entry of position p: col[s_base + p]
+    __syncwarp();
+    int c = 0, cend = s_end[0];
+    long long cbase = s_base[0];
+    uint32_t h = 0;
+    for (int pb = 0; pb < P; pb += 32 * PL_FUNROLL) {
+      int32_t x[PL_FUNROLL];
+#pragma unroll
+      for (int u = 0; u < PL_FUNROLL; ++u) {
+        const int p = pb + 32 * u + lane;
+        x[u] = 0;
+        if (p < P) {
+          while (p >= cend) {  // ends: s_end[31] == P > p
+            ++c;
+            cend = s_end[c];
+            cbase = s_base[c];
+          }
+          x[u] = __ldg(g.col + cbase + p);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < PL_FUNROLL; ++u)
+        if (pb + 32 * u + lane < P) h += pull_test<BITMAP>(tb, base, bits, x[u]);
+    }
+    acc += h;
+    if (tile_cycles && e >= 0) {  // share of this batch's time by the edge's probe count, plus the build share
+      const unsigned long long dt = (unsigned long long)(clock64() - t0);
+      const unsigned long long tot = (unsigned long long)P + (unsigned long long)min((int64_t)32, k2 - qb);
+      atomicAdd(&tile_cycles[e / TILE_EDGES], dt * (unsigned long long)(na + 1) / tot + build_share);
+    }
+    __syncwarp();
+  }
+}
+
 // Work is taken in chunks of grouped entries that shrink from PL_ITEM to
 // PL_ITEM_MIN as the remaining work falls, so the last chunks end together.
 __device__ __forceinline__ unsigned pull_next_chunk(unsigned *head, int64_t np, int64_t warps, int64_t *end) {
@@ -1236,6 +1315,8 @@ __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint2 
                                                          unsigned *head, uint32_t *out, unsigned long long *total,
                                                          unsigned long long *tile_cycles) {
   __shared__ __align__(16) uint32_t tab[PL_WARPS][PL_ROW];
+  __shared__ int32_t s_end_all[PL_WARPS][32];
+  __shared__ long long s_base_all[PL_WARPS][32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   uint32_t *tb = tab[w];
   for (int q = lane; q < PL_ROW; q += 32) tb[q] = 0u;
@@ -1326,10 +1407,18 @@ __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint2 
       __syncwarp();
       const unsigned long long build_share =
           tile_cycles ? (unsigned long long)(clock64() - tr0) / (unsigned long long)(k2 - k) : 0ull;
-      if (bitmap)
+      if (out == nullptr) {  // total only: flattened probing
+        if (bitmap)
+          pull_run_total<true>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_end_all[w], s_base_all[w], acc,
+                               tile_cycles, build_share);
+        else
+          pull_run_total<false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_end_all[w], s_base_all[w], acc,
+                                tile_cycles, build_share);
+      } else if (bitmap) {
         pull_run<true>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, out, acc, tile_cycles, build_share);
-      else
+      } else {
         pull_run<false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, out, acc, tile_cycles, build_share);
+      }
       __syncwarp();
       // back to all zero: the touched word range with 16-byte stores, or the
       // list's own words when the window is much wider than the list

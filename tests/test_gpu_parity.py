@@ -47,6 +47,8 @@ def test_count_dag_matches_reference_solver(engine, golden):
             ref, ref_pe = oracle.count(orow, ocol, per_edge=True)
             assert total == ref == case["triangles"]
             assert np.array_equal(per_edge, ref_pe)
+            total, _, _ = engine.count_dag(orow, ocol, force_arm=arm)
+            assert total == ref, (case["name"], arm, "total only")
 
 
 @pytest.mark.parametrize("spec", [
@@ -66,6 +68,9 @@ def test_seeded_graphs_bit_exact(engine, spec):
         assert total == ref_total, (spec, sel, arm)
         assert np.array_equal(per_edge, ref_pe), (spec, sel, arm)
         assert st["m"] == len(ocol)
+        # total only (no per-edge output): the arms may take their total-only paths
+        total, _, _ = engine.count(rowptr, colidx, selector=sel, force_arm=arm)
+        assert total == ref_total, (spec, sel, arm, "total only")
     total, _, _ = engine.count(rowptr, colidx)
     assert total == ref_total
 
@@ -80,6 +85,8 @@ def test_pull_source_blocks_bit_exact(engine):
         total, per_edge, st = engine.count(rowptr, colidx, selector=sel, force_arm=arm, edge_counts=True)
         assert total == ref_total, (sel, arm)
         assert np.array_equal(per_edge, ref_pe), (sel, arm)
+        total, _, _ = engine.count(rowptr, colidx, selector=sel, force_arm=arm)
+        assert total == ref_total, (sel, arm, "total only")
 
 
 def test_device_generators_match_host(engine):
@@ -133,6 +140,7 @@ def test_long_rows_every_sort_class(engine):
         total, pe, st = engine.count(rowptr, colidx, force_arm=arm, edge_counts=True)
         assert total == expect, arm
         assert np.array_equal(pe, expect_pe), arm
+        assert engine.count(rowptr, colidx, force_arm=arm)[0] == expect, (arm, "total only")
     assert int(np.diff(drow).max()) > 4096
 
 
