@@ -1025,7 +1025,7 @@ constexpr int PL_ITEM = 2048;      // largest work chunk (grouped entries)
 constexpr int PL_ITEM_MIN = 256;   // smallest, near the end of the work
 constexpr int PL_UNROLL = 4;
 constexpr int PL_VUNROLL = 2;      // 16-byte row-suffix loads in flight per lane
-constexpr int PL_FUNROLL = 4;      // flattened probing: loads in flight per lane
+constexpr int PL_FUNROLL = 8;      // flattened probing: loads in flight per lane
 constexpr int PL_SHORT = 16;  // row suffixes up to this long are probed by one lane
 constexpr int PL_GROUP_THREADS = 256;
 
