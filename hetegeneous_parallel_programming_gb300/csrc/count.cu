@@ -1025,7 +1025,7 @@ constexpr int PL_ITEM = 2048;      // largest work chunk (grouped entries)
 constexpr int PL_ITEM_MIN = 256;   // smallest, near the end of the work
 constexpr int PL_UNROLL = 4;
 constexpr int PL_VUNROLL = 2;      // 16-byte row-suffix loads in flight per lane
-constexpr int PL_FUNROLL = 8;      // flattened probing: loads in flight per lane
+constexpr int PL_GUNROLL = 4;      // flattened probing: 16-byte loads in flight per lane
 constexpr int PL_SHORT = 16;  // row suffixes up to this long are probed by one lane
 constexpr int PL_GROUP_THREADS = 256;
 
@@ -1221,16 +1221,26 @@ __device__ __forceinline__ void pull_run(const DevDag &g, const uint2 *__restric
 }
 
 // The same run when only the total is wanted (no per-edge output): the row
-// suffixes of a batch of 32 edges are probed as one flattened sequence, lane
-// p of a pass reading entry p, so loads stay coalesced, short suffixes idle
-// no lanes, and the next edge's loads issue while this one's are tested.
-// Each lane walks its positions upwards and keeps the edge it is in (end and
-// base of the suffix) in registers, from the batch's prefix sums in shared
-// memory.
+// suffixes of a batch of 32 edges are probed as one flattened sequence of
+// 16-byte groups.  Each suffix is widened to the 16-byte blocks that hold it
+// (at most 3 entries before and after it; an aligned 16-byte block holding a
+// valid entry lies in the same memory page, so the extra reads cannot fault
+// and their entries are masked), so no group straddles two edges.  Lane g of
+// a pass loads group g (coalesced 16-byte loads, PL_GUNROLL in flight per
+// lane) and walks the groups upwards, keeping the edge it is in in registers
+// from the batch's prefix sums in shared memory; the next edges' loads issue
+// while this one's are tested.
+struct PullBatch {
+  int32_t gend[32];   // inclusive prefix sum of the edges' group counts
+  int32_t vlo[32];    // first valid entry of the edge in the batch's entry numbering
+  int32_t vhi[32];    // one past its last valid entry
+  long long vb[32];   // 16-byte block index of group g of the edge: vb + g
+};
+
 template <bool BITMAP>
 __device__ __forceinline__ void pull_run_total(const DevDag &g, const uint2 *__restrict__ er, int64_t k, int64_t k2,
                                                bool have_b, const uint32_t *tb, int32_t base, int bits, int lane,
-                                               int32_t *s_end, long long *s_base, unsigned long long &acc,
+                                               PullBatch &sb, unsigned long long &acc,
                                                unsigned long long *tile_cycles, unsigned long long build_share) {
   int64_t e_n = -1;
   int32_t r_n = 0;
@@ -1256,43 +1266,62 @@ __device__ __forceinline__ void pull_run_total(const DevDag &g, const uint2 *__r
       a0 = g.restrict_after ? e + 1 : g.rowptr[r];
       na = (int)(re - a0);
     }
-    int incl = na;
+    const uintptr_t A = reinterpret_cast<uintptr_t>(g.col + a0);
+    const int off = na > 0 ? (int)((A >> 2) & 3u) : 0;
+    const int ng = na > 0 ? (off + na + 3) >> 2 : 0;
+    int gincl = ng;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(TC_FULL_MASK, incl, o);
-      if (lane >= o) incl += y;
+      const int y = __shfl_up_sync(TC_FULL_MASK, gincl, o);
+      if (lane >= o) gincl += y;
     }
-    const int P = __shfl_sync(TC_FULL_MASK, incl, 31);
-    s_end[lane] = incl;
-    s_base[lane] = (long long)a0 - (long long)(incl - na);  // entry of position p: col[s_base + p]
+    const int G = __shfl_sync(TC_FULL_MASK, gincl, 31);
+    const int gexcl = gincl - ng;
+    sb.gend[lane] = gincl;
+    sb.vlo[lane] = 4 * gexcl + off;
+    sb.vhi[lane] = 4 * gexcl + off + na;
+    sb.vb[lane] = (long long)(A >> 4) - gexcl;
     __syncwarp();
-    int c = 0, cend = s_end[0];
-    long long cbase = s_base[0];
+    int c = 0, cend = sb.gend[0], clo = sb.vlo[0], chi = sb.vhi[0];
+    long long cvb = sb.vb[0];
     uint32_t h = 0;
-    for (int pb = 0; pb < P; pb += 32 * PL_FUNROLL) {
-      int32_t x[PL_FUNROLL];
+    for (int gb = 0; gb < G; gb += 32 * PL_GUNROLL) {
+      int4 q[PL_GUNROLL];
+      int lo[PL_GUNROLL], hi[PL_GUNROLL];  // valid entries of the group: lo <= k < hi
 #pragma unroll
-      for (int u = 0; u < PL_FUNROLL; ++u) {
-        const int p = pb + 32 * u + lane;
-        x[u] = 0;
-        if (p < P) {
-          while (p >= cend) {  // ends: s_end[31] == P > p
+      for (int j = 0; j < PL_GUNROLL; ++j) {
+        const int gi = gb + 32 * j + lane;
+        q[j] = make_int4(0, 0, 0, 0);
+        lo[j] = 0;
+        hi[j] = 0;
+        if (gi < G) {
+          while (gi >= cend) {  // ends: gend[31] == G > gi
             ++c;
-            cend = s_end[c];
-            cbase = s_base[c];
+            cend = sb.gend[c];
+            clo = sb.vlo[c];
+            chi = sb.vhi[c];
+            cvb = sb.vb[c];
           }
-          x[u] = __ldg(g.col + cbase + p);
+          q[j] = __ldg(reinterpret_cast<const int4 *>((uintptr_t)(cvb + gi) << 4));
+          lo[j] = clo - 4 * gi;
+          hi[j] = chi - 4 * gi;
         }
       }
 #pragma unroll
-      for (int u = 0; u < PL_FUNROLL; ++u)
-        if (pb + 32 * u + lane < P) h += pull_test<BITMAP>(tb, base, bits, x[u]);
+      for (int j = 0; j < PL_GUNROLL; ++j) {
+        const int32_t xs[4] = {q[j].x, q[j].y, q[j].z, q[j].w};
+#pragma unroll
+        for (int t = 0; t < 4; ++t)
+          if (t >= lo[j] && t < hi[j]) h += pull_test<BITMAP>(tb, base, bits, xs[t]);
+      }
     }
     acc += h;
-    if (tile_cycles && e >= 0) {  // share of this batch's time by the edge's probe count, plus the build share
-      const unsigned long long dt = (unsigned long long)(clock64() - t0);
-      const unsigned long long tot = (unsigned long long)P + (unsigned long long)min((int64_t)32, k2 - qb);
-      atomicAdd(&tile_cycles[e / TILE_EDGES], dt * (unsigned long long)(na + 1) / tot + build_share);
+    if (tile_cycles) {  // share of this batch's time by the edge's probe count, plus the build share
+      const unsigned tot = __reduce_add_sync(TC_FULL_MASK, (unsigned)(e >= 0 ? na + 1 : 0));
+      if (e >= 0) {
+        const unsigned long long dt = (unsigned long long)(clock64() - t0);
+        atomicAdd(&tile_cycles[e / TILE_EDGES], dt * (unsigned long long)(na + 1) / tot + build_share);
+      }
     }
     __syncwarp();
   }
@@ -1315,8 +1344,7 @@ __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint2 
                                                          unsigned *head, uint32_t *out, unsigned long long *total,
                                                          unsigned long long *tile_cycles) {
   __shared__ __align__(16) uint32_t tab[PL_WARPS][PL_ROW];
-  __shared__ int32_t s_end_all[PL_WARPS][32];
-  __shared__ long long s_base_all[PL_WARPS][32];
+  __shared__ PullBatch s_batch[PL_WARPS];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   uint32_t *tb = tab[w];
   for (int q = lane; q < PL_ROW; q += 32) tb[q] = 0u;
@@ -1409,10 +1437,10 @@ __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint2 
           tile_cycles ? (unsigned long long)(clock64() - tr0) / (unsigned long long)(k2 - k) : 0ull;
       if (out == nullptr) {  // total only: flattened probing
         if (bitmap)
-          pull_run_total<true>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_end_all[w], s_base_all[w], acc,
+          pull_run_total<true>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], acc,
                                tile_cycles, build_share);
         else
-          pull_run_total<false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_end_all[w], s_base_all[w], acc,
+          pull_run_total<false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], acc,
                                 tile_cycles, build_share);
       } else if (bitmap) {
         pull_run<true>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, out, acc, tile_cycles, build_share);
