@@ -1024,9 +1024,7 @@ constexpr int PL_WORDS = 2048;  // per warp: a 65536-id bitmap or a 2048-slot ha
 constexpr int PL_ITEM = 2048;      // largest work chunk (grouped entries)
 constexpr int PL_ITEM_MIN = 256;   // smallest, near the end of the work
 constexpr int PL_UNROLL = 4;
-constexpr int PL_VUNROLL = 2;      // 16-byte row-suffix loads in flight per lane
 constexpr int PL_GUNROLL = 4;      // flattened probing: 16-byte loads in flight per lane
-constexpr int PL_SHORT = 16;  // row suffixes up to this long are probed by one lane
 constexpr int PL_GROUP_THREADS = 256;
 
 // One counting sort groups the PULL tiles' edges.  A target among the top
@@ -1097,9 +1095,7 @@ __global__ void __launch_bounds__(PL_GROUP_THREADS) pull_scatter_kernel(const in
 // bucket only when all four are taken, so one 16-byte read answers a probe
 // unless that bucket is full.  After the run the warp zeroes what it wrote.  A
 // bitmap test needs no bounds check: ids outside the window land on zero
-// words or, past the table, on the guard word.  Probing is edge by edge: a
-// row suffix of at most PL_SHORT entries is read by its own lane, a longer
-// one by the whole warp with 16-byte loads (four entries per lane per load).
+// words or, past the table, on the guard word.
 constexpr int PL_ROW = PL_WORDS + 4;  // words per warp: table + guard, 16-byte rows
 
 template <bool BITMAP>
@@ -1119,108 +1115,7 @@ __device__ __forceinline__ uint32_t pull_test(const uint32_t *tb, int32_t base, 
   }
 }
 
-template <bool BITMAP>
-__device__ __forceinline__ uint32_t pull_test4(const uint32_t *tb, int32_t base, int bits, int4 q) {
-  return pull_test<BITMAP>(tb, base, bits, q.x) + pull_test<BITMAP>(tb, base, bits, q.y) +
-         pull_test<BITMAP>(tb, base, bits, q.z) + pull_test<BITMAP>(tb, base, bits, q.w);
-}
-
-// Hits of the whole list A[0, nl) (warp-wide; every lane returns its part).
-// The unaligned head, the first 16-byte loads and the tail are all issued
-// before the first test, so a list of up to 32*4*PL_VUNROLL entries costs one
-// memory round trip.
-template <bool BITMAP>
-__device__ __forceinline__ uint32_t pull_list(const int32_t *__restrict__ A, int nl, const uint32_t *tb,
-                                              int32_t base, int bits, int lane) {
-  const int head = min(nl, (int)((4u - (uint32_t)((reinterpret_cast<uintptr_t>(A) >> 2) & 3u)) & 3u));
-  const int4 *V = reinterpret_cast<const int4 *>(A + head);  // 16-byte aligned
-  const int rest = nl - head, nv = rest >> 2, tail = rest & 3;
-  const int32_t xh = lane < head ? __ldg(A + lane) : 0;
-  const int32_t xt = lane < tail ? __ldg(A + head + 4 * nv + lane) : 0;
-  uint32_t h = 0;
-  for (int v0 = 0; v0 < nv; v0 += 32 * PL_VUNROLL) {
-    int4 q[PL_VUNROLL];
-#pragma unroll
-    for (int u = 0; u < PL_VUNROLL; ++u) {
-      const int j = v0 + 32 * u + lane;
-      q[u] = j < nv ? __ldg(V + j) : make_int4(0, 0, 0, 0);
-    }
-#pragma unroll
-    for (int u = 0; u < PL_VUNROLL; ++u)
-      if (v0 + 32 * u + lane < nv) h += pull_test4<BITMAP>(tb, base, bits, q[u]);
-  }
-  if (lane < head) h += pull_test<BITMAP>(tb, base, bits, xh);
-  if (lane < tail) h += pull_test<BITMAP>(tb, base, bits, xt);
-  return h;
-}
-
-// Grouped entries [k, k2) (one target) against the warp's table.  The next
-// batch's edge ids and rows are loaded while the current batch probes.
-template <bool BITMAP>
-__device__ __forceinline__ void pull_run(const DevDag &g, const uint2 *__restrict__ er, int64_t k, int64_t k2,
-                                         bool have_b, const uint32_t *tb, int32_t base, int bits,
-                                         int lane, uint32_t *out, unsigned long long &acc,
-                                         unsigned long long *tile_cycles, unsigned long long build_share) {
-  int64_t e_n = -1;
-  int32_t r_n = 0;
-  if (k + lane < k2) {
-    const uint2 p = er[k + lane];
-    e_n = p.x;
-    r_n = (int32_t)p.y;
-  }
-  for (int64_t qb = k; qb < k2; qb += 32) {
-    const long long t0 = clock64();
-    const int64_t e = e_n;
-    const int32_t r = r_n;
-    e_n = -1;
-    if (qb + 32 + lane < k2) {  // prefetch for the next batch
-      const uint2 p = er[qb + 32 + lane];
-      e_n = p.x;
-      r_n = (int32_t)p.y;
-    }
-    int64_t a0 = 0;
-    int na = 0;
-    if (e >= 0 && have_b) {
-      const int64_t re = g.rowptr[r + 1];
-      a0 = g.restrict_after ? e + 1 : g.rowptr[r];
-      na = (int)(re - a0);
-    }
-    uint32_t c = 0;
-    if (na <= PL_SHORT) {  // short suffix: this lane alone
-      const int32_t *a = g.col + a0;
-      for (int j0 = 0; j0 < na; j0 += 4) {
-        int32_t x[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) x[u] = j0 + u < na ? __ldg(a + j0 + u) : 0;
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-          if (j0 + u < na) c += pull_test<BITMAP>(tb, base, bits, x[u]);
-      }
-    }
-    unsigned longm = __ballot_sync(TC_FULL_MASK, na > PL_SHORT);
-    while (longm) {  // long suffixes: the whole warp, one edge at a time
-      const int l = __ffs(longm) - 1;
-      longm &= longm - 1;
-      const long long b = __shfl_sync(TC_FULL_MASK, (long long)a0, l);
-      const int nl = __shfl_sync(TC_FULL_MASK, na, l);
-      const uint32_t h = __reduce_add_sync(TC_FULL_MASK, pull_list<BITMAP>(g.col + b, nl, tb, base, bits, lane));
-      if (lane == l) c = h;
-    }
-    if (e >= 0) {
-      put_edge_count(g, out, e, c);
-      acc += c;
-    }
-    if (tile_cycles) {  // share of this batch's time by the edge's probe count, plus the build share
-      const unsigned tot = __reduce_add_sync(TC_FULL_MASK, (unsigned)(e >= 0 ? na + 1 : 0));
-      if (e >= 0) {
-        const unsigned long long dt = (unsigned long long)(clock64() - t0);
-        atomicAdd(&tile_cycles[e / TILE_EDGES], dt * (unsigned long long)(na + 1) / tot + build_share);
-      }
-    }
-  }
-}
-
-// The same run when only the total is wanted (no per-edge output): the row
+// Grouped entries [k, k2) (one target) against the warp's table: the row
 // suffixes of a batch of 32 edges are probed as one flattened sequence of
 // 16-byte groups.  Each suffix is widened to the 16-byte blocks that hold it
 // (at most 3 entries before and after it; an aligned 16-byte block holding a
@@ -1229,19 +1124,23 @@ __device__ __forceinline__ void pull_run(const DevDag &g, const uint2 *__restric
 // a pass loads group g (coalesced 16-byte loads, PL_GUNROLL in flight per
 // lane) and walks the groups upwards, keeping the edge it is in in registers
 // from the batch's prefix sums in shared memory; the next edges' loads issue
-// while this one's are tested.
+// while this one's are tested; the next batch's (edge, row) pairs are
+// loaded while this batch probes.  With PER_EDGE each lane sums its hits per
+// edge and adds them to the edge's shared counter when it moves on to the
+// next edge.
 struct PullBatch {
   int32_t gend[32];   // inclusive prefix sum of the edges' group counts
   int32_t vlo[32];    // first valid entry of the edge in the batch's entry numbering
   int32_t vhi[32];    // one past its last valid entry
   long long vb[32];   // 16-byte block index of group g of the edge: vb + g
+  uint32_t hits[32];  // PER_EDGE: triangles of each edge of the batch
 };
 
-template <bool BITMAP>
-__device__ __forceinline__ void pull_run_total(const DevDag &g, const uint2 *__restrict__ er, int64_t k, int64_t k2,
-                                               bool have_b, const uint32_t *tb, int32_t base, int bits, int lane,
-                                               PullBatch &sb, unsigned long long &acc,
-                                               unsigned long long *tile_cycles, unsigned long long build_share) {
+template <bool BITMAP, bool PER_EDGE>
+__device__ __forceinline__ void pull_run(const DevDag &g, const uint2 *__restrict__ er, int64_t k, int64_t k2,
+                                         bool have_b, const uint32_t *tb, int32_t base, int bits, int lane,
+                                         PullBatch &sb, uint32_t *out, unsigned long long &acc,
+                                         unsigned long long *tile_cycles, unsigned long long build_share) {
   int64_t e_n = -1;
   int32_t r_n = 0;
   if (k + lane < k2) {
@@ -1281,13 +1180,16 @@ __device__ __forceinline__ void pull_run_total(const DevDag &g, const uint2 *__r
     sb.vlo[lane] = 4 * gexcl + off;
     sb.vhi[lane] = 4 * gexcl + off + na;
     sb.vb[lane] = (long long)(A >> 4) - gexcl;
+    if (PER_EDGE) sb.hits[lane] = 0u;
     __syncwarp();
     int c = 0, cend = sb.gend[0], clo = sb.vlo[0], chi = sb.vhi[0];
     long long cvb = sb.vb[0];
     uint32_t h = 0;
+    int hc = 0;  // PER_EDGE: the edge h belongs to
     for (int gb = 0; gb < G; gb += 32 * PL_GUNROLL) {
       int4 q[PL_GUNROLL];
       int lo[PL_GUNROLL], hi[PL_GUNROLL];  // valid entries of the group: lo <= k < hi
+      int ce[PL_GUNROLL];                  // PER_EDGE: edge of the group
 #pragma unroll
       for (int j = 0; j < PL_GUNROLL; ++j) {
         const int gi = gb + 32 * j + lane;
@@ -1306,16 +1208,32 @@ __device__ __forceinline__ void pull_run_total(const DevDag &g, const uint2 *__r
           lo[j] = clo - 4 * gi;
           hi[j] = chi - 4 * gi;
         }
+        ce[j] = c;
       }
 #pragma unroll
       for (int j = 0; j < PL_GUNROLL; ++j) {
+        if (PER_EDGE && ce[j] != hc) {
+          if (h) atomicAdd(&sb.hits[hc], h);
+          hc = ce[j];
+          h = 0;
+        }
         const int32_t xs[4] = {q[j].x, q[j].y, q[j].z, q[j].w};
 #pragma unroll
         for (int t = 0; t < 4; ++t)
           if (t >= lo[j] && t < hi[j]) h += pull_test<BITMAP>(tb, base, bits, xs[t]);
       }
     }
-    acc += h;
+    if (PER_EDGE) {
+      if (h) atomicAdd(&sb.hits[hc], h);
+      __syncwarp();
+      if (e >= 0) {
+        const uint32_t cnt = sb.hits[lane];
+        put_edge_count(g, out, e, cnt);
+        acc += cnt;
+      }
+    } else {
+      acc += h;
+    }
     if (tile_cycles) {  // share of this batch's time by the edge's probe count, plus the build share
       const unsigned tot = __reduce_add_sync(TC_FULL_MASK, (unsigned)(e >= 0 ? na + 1 : 0));
       if (e >= 0) {
@@ -1435,17 +1353,19 @@ __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint2 
       __syncwarp();
       const unsigned long long build_share =
           tile_cycles ? (unsigned long long)(clock64() - tr0) / (unsigned long long)(k2 - k) : 0ull;
-      if (out == nullptr) {  // total only: flattened probing
+      if (out == nullptr) {  // total only
         if (bitmap)
-          pull_run_total<true>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], acc,
-                               tile_cycles, build_share);
+          pull_run<true, false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc, tile_cycles,
+                                build_share);
         else
-          pull_run_total<false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], acc,
-                                tile_cycles, build_share);
+          pull_run<false, false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc, tile_cycles,
+                                 build_share);
       } else if (bitmap) {
-        pull_run<true>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, out, acc, tile_cycles, build_share);
+        pull_run<true, true>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc, tile_cycles,
+                             build_share);
       } else {
-        pull_run<false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, out, acc, tile_cycles, build_share);
+        pull_run<false, true>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc, tile_cycles,
+                              build_share);
       }
       __syncwarp();
       // back to all zero: the touched word range with 16-byte stores, or the
