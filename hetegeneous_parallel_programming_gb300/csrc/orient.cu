@@ -463,8 +463,11 @@ __global__ void seg_sort_warp_kernel(const int64_t *__restrict__ nrowptr, int64_
     if (L < 2 || L > 32) continue;
     int32_t key = lane < L ? ncol[b + lane] : INT32_MAX;
     uint32_t val = (VALS && lane < L) ? perm[b + lane] : 0u;
+    int P = 2;  // levels up to the row's padded length only (warp-uniform)
+    while (P < L) P <<= 1;
 #pragma unroll
     for (int k = 2; k <= 32; k <<= 1) {
+      if (k > P) break;
       {
         const int partner = lane ^ (k - 1);
         const int32_t ok = __shfl_sync(TC_FULL_MASK, key, partner);
