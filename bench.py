@@ -173,10 +173,10 @@ def cpu_sample(rowptr_h, colidx_h, target_s: float):
     step = max(1, n // 1024)
     for _ in range(10):
         dt = run_cpu_sample(rowptr_h, colidx_h, orow, ocol, step)
-        if dt >= 0.5 * target_s or step == 1:
+        if 0.5 * target_s <= dt <= 2.0 * target_s or (step == 1 and dt < target_s):
             break
-        # sample cost scales as 1/step; aim at the target, at most 16x per round
-        step = max(1, int(step * max(dt, target_s / 16) / target_s))
+        # sample cost scales as 1/step; aim at the target, at most 16x per round either way
+        step = max(1, round(step * min(max(dt, target_s / 16), 16 * target_s) / target_s))
     kept_rows = np.diff(orow)[::step]
     return orow, ocol, step, int(kept_rows.sum()), t_full_orient
 
