@@ -248,6 +248,27 @@ class Engine:
             out = out[:st.m]
         return int(tot.value), out, st.as_dict()
 
+    def count_vertices(self, rowptr, colidx, *, validate: bool = True):
+        """Triangles through every vertex of a symmetric CSR: (total, uint64 counts per vertex, stats dict)."""
+        rowptr, colidx = _i64(rowptr), _i32(colidx)
+        g = _ffi.Csr(len(rowptr) - 1, len(colidx), _ptr(rowptr).value, _ptr(colidx).value, 0)
+        o = _opts("fixed", None, validate)
+        tot = C.c_uint64(0)
+        st = _ffi.Stats()
+        out = np.zeros(max(len(rowptr) - 1, 1), np.uint64)
+        self._chk(self._L.tc_count_vertices(self._h, C.byref(g), C.byref(o), C.byref(tot), _ptr(out), C.byref(st)))
+        return int(tot.value), out[:len(rowptr) - 1], st.as_dict()
+
+    def clustering(self, rowptr, colidx, *, validate: bool = True):
+        """Local clustering coefficient of every vertex, 2 t(u) / (deg(u) (deg(u) - 1)) (0 below degree 2),
+        and the global transitivity 3 T / (number of paths of length 2)."""
+        total, t, _ = self.count_vertices(rowptr, colidx, validate=validate)
+        deg = np.diff(np.asarray(rowptr, np.int64)).astype(np.float64)
+        pairs = deg * (deg - 1) / 2
+        local = np.divide(t.astype(np.float64), pairs, out=np.zeros_like(pairs), where=pairs > 0)
+        wedges = pairs.sum()
+        return local, (3.0 * total / wedges if wedges > 0 else 0.0)
+
     def count_dag(self, rowptr, colidx, *, selector: str = "fixed", force_arm=None, edge_counts: bool = False,
                   validate: bool = True):
         rowptr, colidx = _i64(rowptr), _i32(colidx)

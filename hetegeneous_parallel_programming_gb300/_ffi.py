@@ -92,6 +92,7 @@ _SIGS = {
     "tc_orient": (C.c_int, [P, C.POINTER(Csr), P, P, I64, PI64]),
     "tc_count": (C.c_int, [P, C.POINTER(Csr), C.POINTER(Opts), PU64, P, I64, C.POINTER(Stats)]),
     "tc_count_dag": (C.c_int, [P, C.POINTER(Csr), C.POINTER(Opts), PU64, P, I64, C.POINTER(Stats)]),
+    "tc_count_vertices": (C.c_int, [P, C.POINTER(Csr), C.POINTER(Opts), PU64, P, C.POINTER(Stats)]),
     "tc_batch_count": (C.c_int, [P, C.POINTER(Batch), C.POINTER(Opts), P, C.POINTER(Stats)]),
     "tc_count_dag_noalloc": (C.c_int, [C.c_int, P, P, I64, I64, P, P, P]),
     "tc_count_edges": (C.c_int, [P, I64, I64, P, P, I32, C.POINTER(Opts), PU64, C.POINTER(Stats)]),

@@ -276,6 +276,85 @@ tc_status tc_count(tc_ctx *ctx, const tc_csr *g, const tc_opts *opts_in, uint64_
   return TC_OK;
 }
 
+
+// Triangles through every vertex.  Every triangle u < v < w (ranks) is found
+// once, on edge u->v with w the hit: the per-edge counts give the lowest
+// (u: row sums) and middle (v: in-edge sums) vertex; the PULL arm adds, per
+// hit, one to entry u->w (top counts), whose in-edge sums give the highest.
+tc_status tc_count_vertices(tc_ctx *ctx, const tc_csr *g, const tc_opts *opts_in, uint64_t *total,
+                            uint64_t *vertex_counts, tc_stats *stats) {
+  if (!ctx || !total || !vertex_counts) return set_error(ctx, TC_ERR_INVALID_ARG, "null ctx, total or vertex_counts");
+  TC_TRY(check_csr_args(ctx, g));
+  tc_opts o;
+  tc_opts_default(&o);
+  if (opts_in) o = *opts_in;
+  o.selector = TC_SELECT_FORCE;  // only the PULL arm attributes the top edge of a triangle
+  o.force_arm = TC_ARM_PULL;
+  TC_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
+  ctx->launches = 0;
+  tc_stats st;
+  memset(&st, 0, sizeof(st));
+  Sizer sz;
+  if (!g->on_device) { sz.take<int64_t>(g->n + 1); sz.take<int32_t>(g->nnz); }
+  orient_sizes(ctx, g->n, g->nnz, false, false, sz);
+  sz.used += count_scratch_bytes(ctx, g->n, g->nnz);
+  sz.take<uint32_t>(g->nnz);
+  sz.take<uint32_t>(g->nnz);
+  sz.take<unsigned long long>(g->n);
+  if (!g->on_device) sz.take<unsigned long long>(g->n);
+  TC_TRY(arena_reserve(ctx, sz.used));
+  Bump bump{ctx->arena, ctx->arena_cap};
+  TC_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->d_flags, 0, sizeof(unsigned) * 8, ctx->stream));
+  TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[0], ctx->stream));
+  DevCSR d;
+  TC_TRY(stage_csr(ctx, g, bump, d, &st.h2d_bytes));
+  OrientBufs ob;
+  orient_carve(ctx, d.n, d.nnz, false, false, bump, ob);
+  CountBufs cb;
+  if (count_carve(ctx, d.n, d.nnz, bump, cb, o.record_tile_costs != 0) != TC_OK || bump.overflow)
+    return set_error(ctx, TC_ERR_OOM, "arena overflow");
+  uint32_t *d_c = bump.take<uint32_t>(d.nnz);
+  uint32_t *d_top = bump.take<uint32_t>(d.nnz);
+  unsigned long long *d_t = bump.take<unsigned long long>(d.n);
+  unsigned long long *d_vc = g->on_device ? reinterpret_cast<unsigned long long *>(vertex_counts)
+                                          : bump.take<unsigned long long>(d.n);
+  if (bump.overflow) return set_error(ctx, TC_ERR_OOM, "arena overflow");
+  int64_t m = 0;
+  float ms_a = 0;
+  TC_TRY(orient_front(ctx, d, o, ob, &m, &st.ms_validate, &ms_a));
+  st.ms_h2d = elapsed(ctx->ev[0], ctx->ev[1]);
+  TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[4], ctx->stream));
+  DevDag dag;
+  TC_TRY(orient_phase_b(ctx, d, ob, m, false, false, &dag));
+  TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[5], ctx->stream));
+  if (m > 0) TC_CHECK_CUDA(ctx, cudaMemsetAsync(d_top, 0, sizeof(uint32_t) * (size_t)m, ctx->stream));
+  dag.top = d_top;
+  TC_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->d_total, 0, sizeof(unsigned long long), ctx->stream));
+  TC_TRY(run_count(ctx, dag, o, cb, d_c, true));
+  TC_TRY(launch_vertex_sums(ctx, dag, d_c, d_top, d_t, ob.rank, d_vc));
+  TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[6], ctx->stream));
+  if (!g->on_device && d.n > 0) {
+    TC_CHECK_CUDA(ctx, cudaMemcpyAsync(vertex_counts, d_vc, sizeof(uint64_t) * (size_t)d.n, cudaMemcpyDeviceToHost,
+                                       ctx->stream));
+    st.d2h_bytes += sizeof(uint64_t) * (size_t)d.n;
+  }
+  TC_CHECK_CUDA(ctx, cudaMemcpyAsync(&ctx->h_pinned[2], ctx->d_total, sizeof(unsigned long long),
+                                     cudaMemcpyDeviceToHost, ctx->stream));
+  st.d2h_bytes += sizeof(unsigned long long);
+  TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[7], ctx->stream));
+  TC_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  *total = ctx->h_pinned[2];
+  count_stats(ctx, &st, true);
+  st.ms_orient = ms_a + elapsed(ctx->ev[4], ctx->ev[5]);
+  st.ms_d2h = elapsed(ctx->ev[6], ctx->ev[7]);
+  st.ms_total = elapsed(ctx->ev[0], ctx->ev[7]);
+  st.m = m;
+  st.tiles = (m + TILE_EDGES - 1) / TILE_EDGES;
+  st.kernel_launches = ctx->launches;
+  if (stats) *stats = st;
+  return TC_OK;
+}
+
 tc_status tc_count_dag(tc_ctx *ctx, const tc_csr *dag_in, const tc_opts *opts_in, uint64_t *total,
                        uint32_t *edge_counts, int64_t edge_capacity, tc_stats *stats) {
   if (!ctx || !total) return set_error(ctx, TC_ERR_INVALID_ARG, "null ctx or total");

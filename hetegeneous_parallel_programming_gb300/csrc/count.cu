@@ -1004,6 +1004,28 @@ __global__ void __launch_bounds__(BM_THREADS) bitmap_kernel(DevDag g, const uint
   flush_total(acc, total);
 }
 
+// Per-vertex mode, long and wide target lists: the warp's lanes binary-search
+// the keys of A in B; a key found at A[i] adds one to topA[i] (the DAG entry
+// of A[i]).
+__device__ __forceinline__ uint32_t top_search_count(const int32_t *__restrict__ A, int na,
+                                                     const int32_t *__restrict__ B, int nb, uint32_t *topA,
+                                                     int lane) {
+  uint32_t c = 0;
+  for (int i = lane; i < na; i += 32) {
+    const int32_t key = __ldg(A + i);
+    int lo = 0, hi = nb;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (__ldg(B + mid) < key) lo = mid + 1; else hi = mid;
+    }
+    if (lo < nb && __ldg(B + lo) == key) {
+      ++c;
+      atomicAdd(topA + i, 1u);
+    }
+  }
+  return c;
+}
+
 // ---- PULL (edges grouped by target) ---------------------------------------------------
 //
 // The edges of PULL tiles are grouped by target v with a counting sort per
@@ -1136,7 +1158,7 @@ struct PullBatch {
   uint32_t hits[32];  // PER_EDGE: triangles of each edge of the batch
 };
 
-template <bool BITMAP, bool PER_EDGE>
+template <bool BITMAP, bool PER_EDGE, bool TOP>
 __device__ __forceinline__ void pull_run(const DevDag &g, const uint2 *__restrict__ er, int64_t k, int64_t k2,
                                          bool have_b, const uint32_t *tb, int32_t base, int bits, int lane,
                                          PullBatch &sb, uint32_t *out, unsigned long long &acc,
@@ -1190,6 +1212,7 @@ __device__ __forceinline__ void pull_run(const DevDag &g, const uint2 *__restric
       int4 q[PL_GUNROLL];
       int lo[PL_GUNROLL], hi[PL_GUNROLL];  // valid entries of the group: lo <= k < hi
       int ce[PL_GUNROLL];                  // PER_EDGE: edge of the group
+      long long gfirst[PL_GUNROLL];        // TOP: DAG entry index of the group's first slot
 #pragma unroll
       for (int j = 0; j < PL_GUNROLL; ++j) {
         const int gi = gb + 32 * j + lane;
@@ -1209,6 +1232,7 @@ __device__ __forceinline__ void pull_run(const DevDag &g, const uint2 *__restric
           hi[j] = chi - 4 * gi;
         }
         ce[j] = c;
+        if (TOP) gfirst[j] = (long long)((((uintptr_t)(cvb + gi)) << 4) - reinterpret_cast<uintptr_t>(g.col)) >> 2;
       }
 #pragma unroll
       for (int j = 0; j < PL_GUNROLL; ++j) {
@@ -1220,7 +1244,12 @@ __device__ __forceinline__ void pull_run(const DevDag &g, const uint2 *__restric
         const int32_t xs[4] = {q[j].x, q[j].y, q[j].z, q[j].w};
 #pragma unroll
         for (int t = 0; t < 4; ++t)
-          if (t >= lo[j] && t < hi[j]) h += pull_test<BITMAP>(tb, base, bits, xs[t]);
+          if (t >= lo[j] && t < hi[j]) {
+            const uint32_t hit = pull_test<BITMAP>(tb, base, bits, xs[t]);
+            h += hit;
+            // the hit closes triangle (u, v, x): entry u->x joins its lowest and highest vertex
+            if (TOP && hit) atomicAdd(g.top + gfirst[j] + t, 1u);
+          }
       }
     }
     if (PER_EDGE) {
@@ -1257,6 +1286,9 @@ __device__ __forceinline__ unsigned pull_next_chunk(unsigned *head, int64_t np, 
   return start;
 }
 
+// TOP: per-vertex mode (g.top set, per-edge output), a separate
+// instantiation so the plain kernel keeps its registers.
+template <bool TOP>
 __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint2 *__restrict__ er,
                                                          const unsigned *__restrict__ npull,
                                                          unsigned *head, uint32_t *out, unsigned long long *total,
@@ -1303,7 +1335,8 @@ __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint2 
           const EdgeLists L = edge_lists(g, e, s);
           uint32_t c = 0;
           if (L.na > 0 && L.nb > 0) {
-            if (L.na <= L.nb) c = pivot_search_count(L.a, L.na, L.b, L.nb, lane);
+            if (TOP) c = top_search_count(L.a, L.na, L.b, L.nb, g.top + (L.a - g.col), lane);
+            else if (L.na <= L.nb) c = pivot_search_count(L.a, L.na, L.b, L.nb, lane);
             else c = pivot_search_count(L.b, L.nb, L.a, L.na, lane);
           }
           c = warp_sum(c);
@@ -1353,18 +1386,25 @@ __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint2 
       __syncwarp();
       const unsigned long long build_share =
           tile_cycles ? (unsigned long long)(clock64() - tr0) / (unsigned long long)(k2 - k) : 0ull;
-      if (out == nullptr) {  // total only
+      if (TOP) {  // per-vertex counts: per-edge output plus the top-edge attribution
         if (bitmap)
-          pull_run<true, false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc, tile_cycles,
+          pull_run<true, true, true>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc, tile_cycles,
+                                     build_share);
+        else
+          pull_run<false, true, true>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc,
+                                      tile_cycles, build_share);
+      } else if (out == nullptr) {  // total only
+        if (bitmap)
+          pull_run<true, false, false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc, tile_cycles,
                                 build_share);
         else
-          pull_run<false, false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc, tile_cycles,
+          pull_run<false, false, false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc, tile_cycles,
                                  build_share);
       } else if (bitmap) {
-        pull_run<true, true>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc, tile_cycles,
+        pull_run<true, true, false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc, tile_cycles,
                              build_share);
       } else {
-        pull_run<false, true>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc, tile_cycles,
+        pull_run<false, true, false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc, tile_cycles,
                               build_share);
       }
       __syncwarp();
@@ -1406,7 +1446,7 @@ static ArmKernel arm_kernel(int arm) {
   }
 }
 static const void *arm_func(int arm) {
-  return arm == TC_ARM_PULL ? (const void *)pull_kernel : (const void *)arm_kernel(arm);
+  return arm == TC_ARM_PULL ? (const void *)pull_kernel<false> : (const void *)arm_kernel(arm);
 }
 static int arm_threads(int arm) {
   return arm == TC_ARM_BITMAP ? BM_THREADS : arm == TC_ARM_HASH ? HT_THREADS : arm == TC_ARM_PULL ? PL_THREADS : CT_THREADS;
@@ -1506,7 +1546,11 @@ static tc_status run_pull(tc_ctx *ctx, const DevDag &g, CountBufs &cb, uint32_t 
   TC_CHECK_LAUNCH(ctx);
   // pos[K] (no edge has key K) still holds the number of grouped edges
   const int grid = ctx->num_sms * ctx->arm_blocks_per_sm[TC_ARM_PULL];
-  pull_kernel<<<grid, PL_THREADS, 0, ctx->stream>>>(g, cb.pull_er, pos + K,
+  if (g.top)
+    pull_kernel<true><<<grid, PL_THREADS, 0, ctx->stream>>>(g, cb.pull_er, pos + K, ctx->d_heads + TC_ARM_PULL,
+                                                           out, ctx->d_total, cb.tile_cycles);
+  else
+    pull_kernel<false><<<grid, PL_THREADS, 0, ctx->stream>>>(g, cb.pull_er, pos + K,
                                                     ctx->d_heads + TC_ARM_PULL, out, ctx->d_total, cb.tile_cycles);
   TC_CHECK_LAUNCH(ctx);
   return TC_OK;
@@ -1571,6 +1615,37 @@ static float ev_ms(cudaEvent_t a, cudaEvent_t b) {
     return 0;
   }
   return ms;
+}
+
+// Triangles through each vertex of the relabelled DAG from the per-edge
+// counts c (edge r->s is the lowest pair of c[e] triangles) and the top
+// counts (edge r->s joins the lowest and highest vertex of top[e]
+// triangles): t[r] += c[e], t[s] += c[e] + top[e]; then per input id.
+__global__ void vertex_sum_kernel(DevDag g, const uint32_t *__restrict__ c, const uint32_t *__restrict__ top,
+                                  unsigned long long *__restrict__ t) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < g.m; e += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t ce = c[e], te = top[e];
+    if (ce) atomicAdd(t + g.src[e], (unsigned long long)ce);
+    if (ce + te) atomicAdd(t + g.col[e], (unsigned long long)(ce + te));
+  }
+}
+
+__global__ void vertex_unrank_kernel(const unsigned long long *__restrict__ t, const int32_t *__restrict__ rank,
+                                     int64_t n, unsigned long long *__restrict__ out) {
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x)
+    out[u] = t[rank[u]];
+}
+
+tc_status launch_vertex_sums(tc_ctx *ctx, const DevDag &g, const uint32_t *c, const uint32_t *top,
+                             unsigned long long *t, const int32_t *rank, unsigned long long *out) {
+  TC_CHECK_CUDA(ctx, cudaMemsetAsync(t, 0, sizeof(unsigned long long) * (size_t)g.n, ctx->stream));
+  if (g.m > 0) {
+    vertex_sum_kernel<<<grid_for(ctx, g.m, 256, 8), 256, 0, ctx->stream>>>(g, c, top, t);
+    TC_CHECK_LAUNCH(ctx);
+  }
+  vertex_unrank_kernel<<<grid_for(ctx, g.n, 256, 8), 256, 0, ctx->stream>>>(t, rank, g.n, out);
+  TC_CHECK_LAUNCH(ctx);
+  return TC_OK;
 }
 
 void count_stats(tc_ctx *ctx, tc_stats *st, bool timing) {

@@ -34,6 +34,8 @@ struct DevDag {
   const int32_t *src = nullptr;      // [m] row of each edge
   const uint32_t *perm = nullptr;    // [m] output slot of each edge (null: identity)
   const int32_t *indeg = nullptr;    // [n] in-degree of each vertex in the DAG
+  uint32_t *top = nullptr;           // [m] per-vertex mode: triangles in which edge e joins the
+                                     // lowest and the highest vertex (PULL arm only)
   int restrict_after = 0;
 };
 
@@ -96,6 +98,10 @@ struct CountBufs {
   void *sort_scratch;
 };
 size_t count_scratch_bytes(const tc_ctx *ctx, int64_t n, int64_t m);
+// per-vertex triangle counts from the per-edge and top counts of a relabelled
+// DAG, written per input id (rank[u] is u's relabelled id); t is [n] scratch
+tc_status launch_vertex_sums(tc_ctx *ctx, const DevDag &g, const uint32_t *c, const uint32_t *top,
+                             unsigned long long *t, const int32_t *rank, unsigned long long *out);
 tc_status count_carve(const tc_ctx *ctx, int64_t n, int64_t m, Bump &bump, CountBufs &cb, bool want_cycles);
 // Enqueues plan, queue build and every arm kernel on the ctx stream (no host
 // sync, so it can be captured into a CUDA graph); adds the count into

@@ -146,6 +146,16 @@ tc_status tc_count(tc_ctx *ctx, const tc_csr *g, const tc_opts *opts, uint64_t *
 tc_status tc_count_dag(tc_ctx *ctx, const tc_csr *dag, const tc_opts *opts, uint64_t *total,
                        uint32_t *edge_counts, int64_t edge_capacity, tc_stats *stats);
 
+/* Triangles through every vertex of a symmetric graph: vertex_counts[u]
+ * (n entries, input ids, memory kind of g->on_device) = number of triangles
+ * that contain u, and *total = number of triangles.  The per-vertex counts
+ * the reference's CPU intersection (Graph::intersect_num, graph.cc:376-406)
+ * is the building block of, e.g. for clustering coefficients
+ * 2*t(u) / (deg(u)*(deg(u)-1)).  Runs the PULL arm on every tile (the
+ * selector in opts is ignored; validate is honoured). */
+tc_status tc_count_vertices(tc_ctx *ctx, const tc_csr *g, const tc_opts *opts, uint64_t *total,
+                            uint64_t *vertex_counts, tc_stats *stats);
+
 /* ---- allocation-free variant ------------------------------------------- */
 
 /* Size of the fixed device scratch array behind tc_count_dag_noalloc.  Every

@@ -41,6 +41,8 @@ def lib() -> C.CDLL:
         h.oracle_orient.argtypes = [I64, P, P, P, P]
         h.oracle_count.restype = C.c_uint64
         h.oracle_count.argtypes = [I64, P, P, P]
+        h.oracle_count_vertices.restype = C.c_uint64
+        h.oracle_count_vertices.argtypes = [I64, P, P, P]
         h.oracle_count_rows.restype = C.c_uint64
         h.oracle_count_rows.argtypes = [I64, P, P, I64, I64, I64, P]
         h.oracle_orient_rows_cost.restype = I64
@@ -91,6 +93,16 @@ def count_sample(dag_rowptr, dag_colidx, row_step: int):
 def orient_sample_cost(rowptr, colidx, row_step: int) -> int:
     n = len(rowptr) - 1
     return int(lib().oracle_orient_rows_cost(n, _p(rowptr), _p(colidx), int(row_step)))
+
+
+def vertex_triangles(rowptr, colidx):
+    """Triangles through every vertex of a symmetric CSR (orient, then the
+    merge of graph.cc:376-391 enumerating common neighbours) -> (total, uint64[n])."""
+    orow, ocol = orient(rowptr, colidx)
+    n = len(orow) - 1
+    t = np.zeros(max(n, 1), np.uint64)
+    total = lib().oracle_count_vertices(n, _p(orow), _p(ocol), _p(t))
+    return int(total), t[:n]
 
 
 def triangles(rowptr, colidx, per_edge: bool = False):

@@ -104,6 +104,46 @@ uint64_t oracle_count(int64_t n, const int64_t *rowptr, const int32_t *colidx, u
   return oracle_count_rows(n, rowptr, colidx, 0, n, 1, per_edge);
 }
 
+/* Triangles through every vertex of an oriented graph with sorted rows: the
+ * merge of graph.cc:376-391 enumerates, for every edge u->v, each common
+ * out-neighbour w; triangle {u, v, w} adds one to t[u], t[v] and t[w]
+ * (t has n entries, zeroed here).  Returns the number of triangles. */
+uint64_t oracle_count_vertices(int64_t n, const int64_t *rowptr, const int32_t *colidx, uint64_t *t) {
+  for (int64_t i = 0; i < n; ++i) t[i] = 0;
+  uint64_t total = 0;
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : total)
+  for (int64_t u = 0; u < n; ++u) {
+    const int32_t *nu = colidx + rowptr[u];
+    const int64_t du = rowptr[u + 1] - rowptr[u];
+    for (int64_t k = 0; k < du; ++k) {
+      const int32_t v = nu[k];
+      const int32_t *nv = colidx + rowptr[v];
+      const int64_t dv = rowptr[v + 1] - rowptr[v];
+      int64_t i = 0, j = 0;
+      uint64_t c = 0;
+      while (i < du && j < dv) {
+        if (nu[i] < nv[j]) ++i;
+        else if (nv[j] < nu[i]) ++j;
+        else {
+#pragma omp atomic
+          t[nu[i]] += 1;
+          ++c;
+          ++i;
+          ++j;
+        }
+      }
+      if (c) {
+#pragma omp atomic
+        t[u] += c;
+#pragma omp atomic
+        t[v] += c;
+      }
+      total += c;
+    }
+  }
+  return total;
+}
+
 /* Orientation restricted to a sample of rows (every row_step-th row), for
  * the bounded CPU baseline: same work per sampled row as oracle_orient.
  * Returns the number of kept edges of the sampled rows. */

@@ -89,6 +89,82 @@ def test_pull_source_blocks_bit_exact(engine):
         assert total == ref_total, (sel, arm, "total only")
 
 
+def wide_long_lists_graph(k=1100, step=64):
+    """Clique on vertex 0 plus k vertices K spread every `step`-th id, and a
+    triangle-free k-regular bipartite graph on all other ids.  Every vertex
+    has degree k, so ranks follow ids; the first ~74 vertices of K have
+    out-lists longer than 1024 entries spanning more than 65536 ids (the PULL
+    arm's fallback search).  Triangles: C(k+1, 3), all inside the clique."""
+    K = np.arange(1, 1 + k * step, step)[:k]
+    n = int(K[-1]) + 2
+    fill = np.setdiff1d(np.arange(1, n), K)
+    fill = fill[: len(fill) - len(fill) % 2]
+    A, B = fill[0::2], fill[1::2]
+    clique = np.concatenate([[0], K])
+    iu, ju = np.triu_indices(len(clique), 1)
+    j = np.arange(k)
+    bs = np.repeat(A, k)
+    bd = B[(np.repeat(np.arange(len(A)), k) + np.tile(j, len(A))) % len(B)]
+    src = np.concatenate([clique[iu], bs]).astype(np.int32)
+    dst = np.concatenate([clique[ju], bd]).astype(np.int32)
+    return n, src, dst, clique
+
+
+def test_pull_fallback_wide_long_lists(engine):
+    k = 1100
+    n, src, dst, clique = wide_long_lists_graph(k)
+    rowptr, colidx = engine.csr_from_edges(n, src, dst)
+    assert np.all(np.diff(rowptr) == k)
+    expect = (k + 1) * k * (k - 1) // 6
+    drow, dcol = engine.orient(rowptr, colidx)
+    srcs = np.repeat(np.arange(n), np.diff(drow))
+    in_clique = np.zeros(n, bool)
+    in_clique[clique] = True
+    above = np.zeros(n, np.int64)  # clique vertices with a larger id (= higher rank)
+    above[clique] = len(clique) - 1 - np.arange(len(clique))
+    expect_pe = np.where(in_clique[srcs] & in_clique[dcol], above[dcol], 0).astype(np.uint32)
+    for arm in [None, 9]:
+        total, pe, st = engine.count(rowptr, colidx, force_arm=arm, edge_counts=True)
+        assert total == expect, arm
+        assert np.array_equal(pe, expect_pe), arm
+        assert engine.count(rowptr, colidx, force_arm=arm)[0] == expect, (arm, "total only")
+    total, t, _ = engine.count_vertices(rowptr, colidx)
+    assert total == expect
+    expect_t = np.zeros(n, np.uint64)
+    expect_t[clique] = k * (k - 1) // 2
+    assert np.array_equal(t, expect_t)
+
+
+def test_vertex_counts_golden(engine, golden):
+    for case in golden:
+        rowptr, colidx = csr_of(case)
+        total, t, st = engine.count_vertices(rowptr, colidx)
+        assert total == case["triangles"], case["name"]
+        assert t.tolist() == case["per_vertex"], case["name"]
+
+
+@pytest.mark.parametrize("spec", [
+    tc.GenSpec("er", n=16384, avg_degree=16, seed=0),
+    tc.GenSpec("rmat", scale=16, edge_factor=16, seed=1),
+    tc.GenSpec("chung_lu", n=50000, avg_degree=24, gamma=2.1, seed=3),
+    tc.GenSpec("rgg", n=8000, avg_degree=40, seed=4),
+    tc.GenSpec("rmat", scale=20, edge_factor=16, seed=4),  # several PULL source blocks
+])
+def test_vertex_counts_seeded(engine, spec):
+    rowptr, colidx = gen_csr(spec)
+    ref_total, ref_t = oracle.vertex_triangles(rowptr, colidx)
+    for _ in range(2):  # the top counts start from zero every call
+        total, t, _ = engine.count_vertices(rowptr, colidx)
+        assert total == ref_total
+        assert np.array_equal(t, ref_t)
+    local, transitivity = engine.clustering(rowptr, colidx)
+    deg = np.diff(rowptr).astype(np.float64)
+    pairs = deg * (deg - 1) / 2
+    ref_local = np.divide(ref_t.astype(np.float64), pairs, out=np.zeros_like(pairs), where=pairs > 0)
+    assert np.allclose(local, ref_local, rtol=0, atol=1e-12)
+    assert abs(transitivity - 3 * ref_total / pairs.sum()) < 1e-12
+
+
 def test_device_generators_match_host(engine):
     import torch
     for spec in [tc.GenSpec("er", n=100000, avg_degree=8, seed=11),

@@ -45,6 +45,33 @@ def test_exhaustive_six_vertex_graphs():
         assert oracle.triangles(rowptr, colidx) == oracle.brute_force_triangles(6, edges)
 
 
+def test_golden_per_vertex(golden):
+    """Triangles through every vertex against networkx's per-vertex counts."""
+    for case in golden:
+        rowptr, colidx = csr_of(case)
+        total, t = oracle.vertex_triangles(rowptr, colidx)
+        assert total == case["triangles"], case["name"]
+        assert t.tolist() == case["per_vertex"], case["name"]
+        assert int(t.sum()) == 3 * total
+
+
+def test_random_graphs_per_vertex_brute_force():
+    rng = np.random.default_rng(11)
+    for n in (7, 9, 12):
+        pairs = list(itertools.combinations(range(n), 2))
+        for _ in range(200):
+            keep = rng.random(len(pairs)) < rng.random()
+            edges = [p for p, k in zip(pairs, keep) if k]
+            adj = np.zeros((n, n), bool)
+            for u, v in edges:
+                adj[u, v] = adj[v, u] = True
+            expect = [sum(adj[x, y] for x, y in itertools.combinations(np.flatnonzero(adj[u]), 2)) for u in range(n)]
+            src = np.array([u for u, _ in edges], np.int32)
+            dst = np.array([v for _, v in edges], np.int32)
+            rowptr, colidx = oracle.csr_from_edges(n, src, dst)
+            assert oracle.vertex_triangles(rowptr, colidx)[1].tolist() == expect
+
+
 def test_random_seven_vertex_graphs():
     rng = np.random.default_rng(7)
     pairs = list(itertools.combinations(range(7), 2))
