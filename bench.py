@@ -237,6 +237,18 @@ def engine_arm(args, rank, world, local_rank, dist):
         per_edge_check = {"sum_of_per_edge_counts": pe_sum, "equals_total": pe_sum == total}
         if pe_sum != total:
             raise SystemExit("per-edge counts do not sum to the total")
+    per_vertex = None
+    if not args.no_per_vertex:  # triangles through every vertex, on the same device CSR
+        tv = torch.empty(n, dtype=torch.int64, device=dev)
+        ms_v, (tot_v, _) = timed(lambda: eng.count_vertices_device(n, nnz, rowptr.data_ptr(), colidx.data_ptr(),
+                                                                   tv.data_ptr()),
+                                 max(1, min(args.steps, 5)), 3, eng, torch, dist)
+        tsum = int(tv.sum().item())  # size-independent property: every triangle has three vertices
+        if tot_v != total or tsum != 3 * total:
+            raise SystemExit("per-vertex counts disagree with the total")
+        per_vertex = {"gteps": round(world * m / (ms_v * 1e-3) / 1e9, 4), "ms_per_step": round(ms_v, 3),
+                      "sum_of_vertex_counts_equals_3T": True}
+        del tv
     # e2e through the public API with pinned host buffers (H2D + D2H inside)
     rowptr_h = rowptr.cpu().pin_memory()
     colidx_h = colidx.cpu().pin_memory()
@@ -298,6 +310,7 @@ def engine_arm(args, rank, world, local_rank, dist):
                                          if st["ms_count"] > 0 else None}},
             "gpu_launches": int(st["kernel_launches"]) * args.steps,
             "per_edge_counts": per_edge_check,
+            "per_vertex_counts": per_vertex,
             "clocks": clk.summary(),
         }
     if not args.no_batched:
@@ -420,6 +433,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--per-edge", action="store_true", help="also write per-edge local counts every step")
+    ap.add_argument("--no-per-vertex", action="store_true", help="skip the per-vertex triangle count timing")
     ap.add_argument("--force-arm", default=None, help="run every tile on this arm (profiling)")
     ap.add_argument("--ref-step-seconds", type=float, default=4.0)
     args = ap.parse_args()

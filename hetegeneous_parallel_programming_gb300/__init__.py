@@ -315,6 +315,17 @@ class Engine:
                                    C.byref(st)))
         return int(tot.value), st.as_dict()
 
+    def count_vertices_device(self, n: int, nnz: int, rowptr_ptr: int, colidx_ptr: int, vertex_counts_ptr: int, *,
+                              validate: bool = True):
+        """Per-vertex triangle counts of a device-resident CSR into a device uint64 buffer of n entries."""
+        g = _ffi.Csr(int(n), int(nnz), int(rowptr_ptr), int(colidx_ptr), 1)
+        o = _opts("fixed", None, validate)
+        tot = C.c_uint64(0)
+        st = _ffi.Stats()
+        self._chk(self._L.tc_count_vertices(self._h, C.byref(g), C.byref(o), C.byref(tot),
+                                            C.c_void_p(vertex_counts_ptr), C.byref(st)))
+        return int(tot.value), st.as_dict()
+
     def count_host_ptr(self, n: int, nnz: int, rowptr_ptr: int, colidx_ptr: int, *, selector: str = "fixed",
                        force_arm=None, validate: bool = True):
         """Like count() but on caller-owned host buffers (e.g. pinned memory)."""
