@@ -21,6 +21,7 @@ from ._ffi import (ARM_NAMES, GEN_CHUNG_LU, GEN_ER, GEN_RGG, GEN_RMAT, SELECT_FI
                    SELECT_LEARNED, TC_MLP_FEATURES, TC_MLP_PARAM_COUNT, TC_NUM_ARMS, TILE_EDGES)
 
 __all__ = ["TCError", "Engine", "Graph", "TCSolver", "GenSpec", "gen_edges_host", "gen_batch_host",
+           "load_vlabels", "save_vlabels",
            "csr_from_edges_host",
            "load_graphminer", "save_graphminer", "check_csr", "ARM_NAMES", "TC_NUM_ARMS", "TC_MLP_FEATURES",
            "TC_MLP_PARAM_COUNT", "TILE_EDGES"]
@@ -180,6 +181,18 @@ def save_graphminer(prefix: str, rowptr: np.ndarray, colidx: np.ndarray) -> None
                                          _ptr(colidx)))
 
 
+def load_vlabels(prefix: str, n: int) -> np.ndarray:
+    """Vertex labels of a GraphMiner graph (prefix.vlabel.bin, one byte per vertex)."""
+    out = np.zeros(int(n), np.uint8)
+    _check(_ffi.lib().tc_load_vlabels(str(prefix).encode(), int(n), _ptr(out)))
+    return out
+
+
+def save_vlabels(prefix: str, labels: np.ndarray) -> None:
+    labels = np.ascontiguousarray(labels, np.uint8)
+    _check(_ffi.lib().tc_save_vlabels(str(prefix).encode(), len(labels), _ptr(labels)))
+
+
 def check_csr(rowptr: np.ndarray, colidx: np.ndarray, sorted_simple: bool = True) -> None:
     rowptr, colidx = _i64(rowptr), _i32(colidx)
     _check(_ffi.lib().tc_check_csr_host(len(rowptr) - 1, len(colidx), _ptr(rowptr), _ptr(colidx),
@@ -258,6 +271,25 @@ class Engine:
         out = np.zeros(max(len(rowptr) - 1, 1), np.uint64)
         self._chk(self._L.tc_count_vertices(self._h, C.byref(g), C.byref(o), C.byref(tot), _ptr(out), C.byref(st)))
         return int(tot.value), out[:len(rowptr) - 1], st.as_dict()
+
+    def count_labelled(self, rowptr, colidx, labels, label: int, *, edge_counts: bool = False,
+                       validate: bool = True):
+        """Common out-neighbours carrying `label` over every oriented edge (the reference's labelled
+        intersection on the degree-ordered DAG): (total, per-edge counts or None, stats dict)."""
+        rowptr, colidx = _i64(rowptr), _i32(colidx)
+        labels = np.ascontiguousarray(labels, np.uint8)
+        if len(labels) != len(rowptr) - 1:
+            raise ValueError("one label per vertex")
+        g = _ffi.Csr(len(rowptr) - 1, len(colidx), _ptr(rowptr).value, _ptr(colidx).value, 0)
+        o = _opts("fixed", None, validate)
+        tot = C.c_uint64(0)
+        st = _ffi.Stats()
+        out = np.empty(max(len(colidx), 1), np.uint32) if edge_counts else None
+        self._chk(self._L.tc_count_labelled(self._h, C.byref(g), _ptr(labels), int(label), C.byref(o), C.byref(tot),
+                                            _ptr(out), len(colidx) if edge_counts else 0, C.byref(st)))
+        if out is not None:
+            out = out[:st.m]
+        return int(tot.value), out, st.as_dict()
 
     def clustering(self, rowptr, colidx, *, validate: bool = True):
         """Local clustering coefficient of every vertex, 2 t(u) / (deg(u) (deg(u) - 1)) (0 below degree 2),

@@ -93,6 +93,7 @@ _SIGS = {
     "tc_count": (C.c_int, [P, C.POINTER(Csr), C.POINTER(Opts), PU64, P, I64, C.POINTER(Stats)]),
     "tc_count_dag": (C.c_int, [P, C.POINTER(Csr), C.POINTER(Opts), PU64, P, I64, C.POINTER(Stats)]),
     "tc_count_vertices": (C.c_int, [P, C.POINTER(Csr), C.POINTER(Opts), PU64, P, C.POINTER(Stats)]),
+    "tc_count_labelled": (C.c_int, [P, C.POINTER(Csr), P, I32, C.POINTER(Opts), PU64, P, I64, C.POINTER(Stats)]),
     "tc_batch_count": (C.c_int, [P, C.POINTER(Batch), C.POINTER(Opts), P, C.POINTER(Stats)]),
     "tc_count_dag_noalloc": (C.c_int, [C.c_int, P, P, I64, I64, P, P, P]),
     "tc_count_edges": (C.c_int, [P, I64, I64, P, P, I32, C.POINTER(Opts), PU64, C.POINTER(Stats)]),
@@ -114,6 +115,8 @@ _SIGS = {
     "tc_load_graphminer": (C.c_int, [C.c_char_p, PI64, PI64, C.POINTER(PI64), C.POINTER(C.POINTER(C.c_int32)),
                                      PI64]),
     "tc_save_graphminer": (C.c_int, [C.c_char_p, I64, I64, P, P]),
+    "tc_load_vlabels": (C.c_int, [C.c_char_p, I64, P]),
+    "tc_save_vlabels": (C.c_int, [C.c_char_p, I64, P]),
     "tc_csr_free": (None, [P, P]),
     "tc_check_csr_host": (C.c_int, [I64, I64, P, P, I32]),
 }

@@ -277,6 +277,92 @@ tc_status tc_count(tc_ctx *ctx, const tc_csr *g, const tc_opts *opts_in, uint64_
 }
 
 
+// Labelled counts: for every oriented edge u->v, the common out-neighbours w
+// whose label is `label` (the reference's labelled intersection, on the DAG).
+tc_status tc_count_labelled(tc_ctx *ctx, const tc_csr *g, const uint8_t *vertex_labels, int32_t label,
+                            const tc_opts *opts_in, uint64_t *total, uint32_t *edge_counts, int64_t edge_capacity,
+                            tc_stats *stats) {
+  if (!ctx || !total || !vertex_labels) return set_error(ctx, TC_ERR_INVALID_ARG, "null ctx, total or vertex_labels");
+  if (label < 0 || label > 255) return set_error(ctx, TC_ERR_INVALID_ARG, "label %d outside [0, 255]", label);
+  TC_TRY(check_csr_args(ctx, g));
+  tc_opts o;
+  tc_opts_default(&o);
+  if (opts_in) o = *opts_in;
+  o.selector = TC_SELECT_FORCE;  // only the PULL arm filters hits by label
+  o.force_arm = TC_ARM_PULL;
+  TC_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
+  ctx->launches = 0;
+  tc_stats st;
+  memset(&st, 0, sizeof(st));
+  const bool want_edges = edge_counts != nullptr;
+  Sizer sz;
+  if (!g->on_device) { sz.take<int64_t>(g->n + 1); sz.take<int32_t>(g->nnz); sz.take<uint8_t>(g->n); }
+  orient_sizes(ctx, g->n, g->nnz, want_edges, false, sz);
+  sz.used += count_scratch_bytes(ctx, g->n, g->nnz);
+  sz.take<uint8_t>(g->n);
+  if (want_edges && !g->on_device) sz.take<uint32_t>(g->nnz);
+  TC_TRY(arena_reserve(ctx, sz.used));
+  Bump bump{ctx->arena, ctx->arena_cap};
+  TC_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->d_flags, 0, sizeof(unsigned) * 8, ctx->stream));
+  TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[0], ctx->stream));
+  DevCSR d;
+  TC_TRY(stage_csr(ctx, g, bump, d, &st.h2d_bytes));
+  const uint8_t *d_lab_in = vertex_labels;
+  if (!g->on_device) {
+    uint8_t *tmp = bump.take<uint8_t>(d.n);
+    if (bump.overflow) return set_error(ctx, TC_ERR_OOM, "arena overflow");
+    TC_CHECK_CUDA(ctx, cudaMemcpyAsync(tmp, vertex_labels, (size_t)d.n, cudaMemcpyHostToDevice, ctx->stream));
+    st.h2d_bytes += (uint64_t)d.n;
+    d_lab_in = tmp;
+  }
+  OrientBufs ob;
+  orient_carve(ctx, d.n, d.nnz, want_edges, false, bump, ob);
+  CountBufs cb;
+  if (count_carve(ctx, d.n, d.nnz, bump, cb, o.record_tile_costs != 0) != TC_OK || bump.overflow)
+    return set_error(ctx, TC_ERR_OOM, "arena overflow");
+  uint8_t *d_lab = bump.take<uint8_t>(d.n);
+  uint32_t *d_out = nullptr;
+  if (want_edges) d_out = g->on_device ? edge_counts : bump.take<uint32_t>(d.nnz);
+  if (bump.overflow) return set_error(ctx, TC_ERR_OOM, "arena overflow");
+  int64_t m = 0;
+  float ms_a = 0;
+  TC_TRY(orient_front(ctx, d, o, ob, &m, &st.ms_validate, &ms_a));
+  st.ms_h2d = elapsed(ctx->ev[0], ctx->ev[1]);
+  if (want_edges && edge_capacity < m)
+    return set_error(ctx, TC_ERR_INVALID_ARG, "edge_counts holds %lld entries, %lld oriented edges",
+                     (long long)edge_capacity, (long long)m);
+  TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[4], ctx->stream));
+  DevDag dag;
+  TC_TRY(orient_phase_b(ctx, d, ob, m, want_edges, false, &dag));
+  TC_TRY(launch_relabel_u8(ctx, d_lab_in, ob.rank, d.n, d_lab));
+  TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[5], ctx->stream));
+  dag.vlabel = d_lab;
+  dag.label = label;
+  TC_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->d_total, 0, sizeof(unsigned long long), ctx->stream));
+  TC_TRY(run_count(ctx, dag, o, cb, d_out, true));
+  TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[6], ctx->stream));
+  if (want_edges && !g->on_device && m > 0) {
+    TC_CHECK_CUDA(ctx, cudaMemcpyAsync(edge_counts, d_out, sizeof(uint32_t) * (size_t)m, cudaMemcpyDeviceToHost,
+                                       ctx->stream));
+    st.d2h_bytes += sizeof(uint32_t) * (size_t)m;
+  }
+  TC_CHECK_CUDA(ctx, cudaMemcpyAsync(&ctx->h_pinned[2], ctx->d_total, sizeof(unsigned long long),
+                                     cudaMemcpyDeviceToHost, ctx->stream));
+  st.d2h_bytes += sizeof(unsigned long long);
+  TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[7], ctx->stream));
+  TC_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  *total = ctx->h_pinned[2];
+  count_stats(ctx, &st, true);
+  st.ms_orient = ms_a + elapsed(ctx->ev[4], ctx->ev[5]);
+  st.ms_d2h = elapsed(ctx->ev[6], ctx->ev[7]);
+  st.ms_total = elapsed(ctx->ev[0], ctx->ev[7]);
+  st.m = m;
+  st.tiles = (m + TILE_EDGES - 1) / TILE_EDGES;
+  st.kernel_launches = ctx->launches;
+  if (stats) *stats = st;
+  return TC_OK;
+}
+
 // Triangles through every vertex.  Every triangle u < v < w (ranks) is found
 // once, on edge u->v with w the hit: the per-edge counts give the lowest
 // (u: row sums) and middle (v: in-edge sums) vertex; the PULL arm adds, per

@@ -1004,12 +1004,13 @@ __global__ void __launch_bounds__(BM_THREADS) bitmap_kernel(DevDag g, const uint
   flush_total(acc, total);
 }
 
-// Per-vertex mode, long and wide target lists: the warp's lanes binary-search
-// the keys of A in B; a key found at A[i] adds one to topA[i] (the DAG entry
-// of A[i]).
-__device__ __forceinline__ uint32_t top_search_count(const int32_t *__restrict__ A, int na,
-                                                     const int32_t *__restrict__ B, int nb, uint32_t *topA,
-                                                     int lane) {
+// Per-vertex and labelled modes, long and wide target lists: the warp's
+// lanes binary-search the keys of A in B.  A key found at A[i] counts when
+// its label is `label` (lbl set) and adds one to topA[i], the DAG entry of
+// A[i] (topA set).
+__device__ __forceinline__ uint32_t attr_search_count(const int32_t *__restrict__ A, int na,
+                                                      const int32_t *__restrict__ B, int nb, uint32_t *topA,
+                                                      const uint8_t *__restrict__ lbl, int label, int lane) {
   uint32_t c = 0;
   for (int i = lane; i < na; i += 32) {
     const int32_t key = __ldg(A + i);
@@ -1018,9 +1019,9 @@ __device__ __forceinline__ uint32_t top_search_count(const int32_t *__restrict__
       const int mid = (lo + hi) >> 1;
       if (__ldg(B + mid) < key) lo = mid + 1; else hi = mid;
     }
-    if (lo < nb && __ldg(B + lo) == key) {
+    if (lo < nb && __ldg(B + lo) == key && (!lbl || lbl[key] == label)) {
       ++c;
-      atomicAdd(topA + i, 1u);
+      if (topA) atomicAdd(topA + i, 1u);
     }
   }
   return c;
@@ -1158,7 +1159,7 @@ struct PullBatch {
   uint32_t hits[32];  // PER_EDGE: triangles of each edge of the batch
 };
 
-template <bool BITMAP, bool PER_EDGE, bool TOP>
+template <bool BITMAP, bool PER_EDGE, bool TOP, bool LABEL>
 __device__ __forceinline__ void pull_run(const DevDag &g, const uint2 *__restrict__ er, int64_t k, int64_t k2,
                                          bool have_b, const uint32_t *tb, int32_t base, int bits, int lane,
                                          PullBatch &sb, uint32_t *out, unsigned long long &acc,
@@ -1245,7 +1246,8 @@ __device__ __forceinline__ void pull_run(const DevDag &g, const uint2 *__restric
 #pragma unroll
         for (int t = 0; t < 4; ++t)
           if (t >= lo[j] && t < hi[j]) {
-            const uint32_t hit = pull_test<BITMAP>(tb, base, bits, xs[t]);
+            uint32_t hit = pull_test<BITMAP>(tb, base, bits, xs[t]);
+            if (LABEL && hit) hit = g.vlabel[xs[t]] == g.label;  // the reference's labelled intersection
             h += hit;
             // the hit closes triangle (u, v, x): entry u->x joins its lowest and highest vertex
             if (TOP && hit) atomicAdd(g.top + gfirst[j] + t, 1u);
@@ -1286,9 +1288,10 @@ __device__ __forceinline__ unsigned pull_next_chunk(unsigned *head, int64_t np, 
   return start;
 }
 
-// TOP: per-vertex mode (g.top set, per-edge output), a separate
-// instantiation so the plain kernel keeps its registers.
-template <bool TOP>
+// MODE 1: per-vertex counts (g.top set, per-edge output); MODE 2: labelled
+// counts (g.vlabel set).  Separate instantiations, so the plain kernel
+// (MODE 0) keeps its registers.
+template <int MODE>
 __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint2 *__restrict__ er,
                                                          const unsigned *__restrict__ npull,
                                                          unsigned *head, uint32_t *out, unsigned long long *total,
@@ -1335,7 +1338,9 @@ __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint2 
           const EdgeLists L = edge_lists(g, e, s);
           uint32_t c = 0;
           if (L.na > 0 && L.nb > 0) {
-            if (TOP) c = top_search_count(L.a, L.na, L.b, L.nb, g.top + (L.a - g.col), lane);
+            if (MODE != 0)
+              c = attr_search_count(L.a, L.na, L.b, L.nb, MODE == 1 ? g.top + (L.a - g.col) : nullptr,
+                                    MODE == 2 ? g.vlabel : nullptr, g.label, lane);
             else if (L.na <= L.nb) c = pivot_search_count(L.a, L.na, L.b, L.nb, lane);
             else c = pivot_search_count(L.b, L.nb, L.a, L.na, lane);
           }
@@ -1386,25 +1391,26 @@ __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint2 
       __syncwarp();
       const unsigned long long build_share =
           tile_cycles ? (unsigned long long)(clock64() - tr0) / (unsigned long long)(k2 - k) : 0ull;
-      if (TOP) {  // per-vertex counts: per-edge output plus the top-edge attribution
+      constexpr bool LAB = MODE == 2;
+      if (MODE == 1) {  // per-vertex counts: per-edge output plus the top-edge attribution
         if (bitmap)
-          pull_run<true, true, true>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc, tile_cycles,
-                                     build_share);
+          pull_run<true, true, true, false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc,
+                                            tile_cycles, build_share);
         else
-          pull_run<false, true, true>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc,
-                                      tile_cycles, build_share);
+          pull_run<false, true, true, false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc,
+                                             tile_cycles, build_share);
       } else if (out == nullptr) {  // total only
         if (bitmap)
-          pull_run<true, false, false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc, tile_cycles,
+          pull_run<true, false, false, LAB>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc, tile_cycles,
                                 build_share);
         else
-          pull_run<false, false, false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc, tile_cycles,
+          pull_run<false, false, false, LAB>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc, tile_cycles,
                                  build_share);
       } else if (bitmap) {
-        pull_run<true, true, false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc, tile_cycles,
+        pull_run<true, true, false, LAB>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc, tile_cycles,
                              build_share);
       } else {
-        pull_run<false, true, false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc, tile_cycles,
+        pull_run<false, true, false, LAB>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc, tile_cycles,
                               build_share);
       }
       __syncwarp();
@@ -1446,7 +1452,7 @@ static ArmKernel arm_kernel(int arm) {
   }
 }
 static const void *arm_func(int arm) {
-  return arm == TC_ARM_PULL ? (const void *)pull_kernel<false> : (const void *)arm_kernel(arm);
+  return arm == TC_ARM_PULL ? (const void *)pull_kernel<0> : (const void *)arm_kernel(arm);
 }
 static int arm_threads(int arm) {
   return arm == TC_ARM_BITMAP ? BM_THREADS : arm == TC_ARM_HASH ? HT_THREADS : arm == TC_ARM_PULL ? PL_THREADS : CT_THREADS;
@@ -1547,10 +1553,13 @@ static tc_status run_pull(tc_ctx *ctx, const DevDag &g, CountBufs &cb, uint32_t 
   // pos[K] (no edge has key K) still holds the number of grouped edges
   const int grid = ctx->num_sms * ctx->arm_blocks_per_sm[TC_ARM_PULL];
   if (g.top)
-    pull_kernel<true><<<grid, PL_THREADS, 0, ctx->stream>>>(g, cb.pull_er, pos + K, ctx->d_heads + TC_ARM_PULL,
-                                                           out, ctx->d_total, cb.tile_cycles);
+    pull_kernel<1><<<grid, PL_THREADS, 0, ctx->stream>>>(g, cb.pull_er, pos + K, ctx->d_heads + TC_ARM_PULL, out,
+                                                        ctx->d_total, cb.tile_cycles);
+  else if (g.vlabel)
+    pull_kernel<2><<<grid, PL_THREADS, 0, ctx->stream>>>(g, cb.pull_er, pos + K, ctx->d_heads + TC_ARM_PULL, out,
+                                                        ctx->d_total, cb.tile_cycles);
   else
-    pull_kernel<false><<<grid, PL_THREADS, 0, ctx->stream>>>(g, cb.pull_er, pos + K,
+    pull_kernel<0><<<grid, PL_THREADS, 0, ctx->stream>>>(g, cb.pull_er, pos + K,
                                                     ctx->d_heads + TC_ARM_PULL, out, ctx->d_total, cb.tile_cycles);
   TC_CHECK_LAUNCH(ctx);
   return TC_OK;
@@ -1634,6 +1643,19 @@ __global__ void vertex_unrank_kernel(const unsigned long long *__restrict__ t, c
                                      int64_t n, unsigned long long *__restrict__ out) {
   for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x)
     out[u] = t[rank[u]];
+}
+
+__global__ void relabel_u8_kernel(const uint8_t *__restrict__ in, const int32_t *__restrict__ rank, int64_t n,
+                                  uint8_t *__restrict__ out) {
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x)
+    out[rank[u]] = in[u];
+}
+
+tc_status launch_relabel_u8(tc_ctx *ctx, const uint8_t *in, const int32_t *rank, int64_t n, uint8_t *out) {
+  if (n <= 0) return TC_OK;
+  relabel_u8_kernel<<<grid_for(ctx, n, 256, 8), 256, 0, ctx->stream>>>(in, rank, n, out);
+  TC_CHECK_LAUNCH(ctx);
+  return TC_OK;
 }
 
 tc_status launch_vertex_sums(tc_ctx *ctx, const DevDag &g, const uint32_t *c, const uint32_t *top,

@@ -36,6 +36,8 @@ struct DevDag {
   const int32_t *indeg = nullptr;    // [n] in-degree of each vertex in the DAG
   uint32_t *top = nullptr;           // [m] per-vertex mode: triangles in which edge e joins the
                                      // lowest and the highest vertex (PULL arm only)
+  const uint8_t *vlabel = nullptr;   // [n] labelled mode: vertex labels (relabelled ids; PULL arm only)
+  int label = 0;                     // labelled mode: count common neighbours with this label
   int restrict_after = 0;
 };
 
@@ -98,6 +100,8 @@ struct CountBufs {
   void *sort_scratch;
 };
 size_t count_scratch_bytes(const tc_ctx *ctx, int64_t n, int64_t m);
+// out[rank[u]] = in[u] for n one-byte values (vertex labels into relabelled ids)
+tc_status launch_relabel_u8(tc_ctx *ctx, const uint8_t *in, const int32_t *rank, int64_t n, uint8_t *out);
 // per-vertex triangle counts from the per-edge and top counts of a relabelled
 // DAG, written per input id (rank[u] is u's relabelled id); t is [n] scratch
 tc_status launch_vertex_sums(tc_ctx *ctx, const DevDag &g, const uint32_t *c, const uint32_t *top,

@@ -501,6 +501,49 @@ tc_status tc_save_graphminer(const char *prefix, int64_t n, int64_t nnz, const i
   return TC_OK;
 }
 
+tc_status tc_load_vlabels(const char *prefix, int64_t n, uint8_t *labels) {
+  if (!prefix || n < 1 || !labels) {
+    set_global_error("tc_load_vlabels: bad arguments");
+    return TC_ERR_INVALID_ARG;
+  }
+  if (!read_exact(std::string(prefix) + ".vlabel.bin", labels, (size_t)n)) {
+    set_global_error("%s.vlabel.bin missing or not %lld bytes", prefix, (long long)n);
+    return TC_ERR_IO;
+  }
+  return TC_OK;
+}
+
+tc_status tc_save_vlabels(const char *prefix, int64_t n, const uint8_t *labels) {
+  if (!prefix || n < 1 || !labels) {
+    set_global_error("tc_save_vlabels: bad arguments");
+    return TC_ERR_INVALID_ARG;
+  }
+  const std::string p(prefix);
+  long long v[10] = {0};
+  {
+    std::ifstream meta((p + ".meta.txt").c_str());
+    if (!meta) { set_global_error("cannot open %s.meta.txt (save the graph first)", prefix); return TC_ERR_IO; }
+    for (int i = 0; i < 10; ++i) meta >> v[i];
+    if (!meta) { set_global_error("%s.meta.txt: expected 10 integers", prefix); return TC_ERR_IO; }
+  }
+  if (v[0] != n) { set_global_error("%s.meta.txt holds n=%lld, not %lld", prefix, v[0], (long long)n); return TC_ERR_INVALID_ARG; }
+  int maxl = 0;
+  for (int64_t u = 0; u < n; ++u) maxl = std::max<int>(maxl, labels[u]);
+  v[4] = 1;         // vlabel_size: one byte per vertex
+  v[8] = maxl + 1;  // num_vertex_classes
+  FILE *f = fopen((p + ".meta.txt").c_str(), "w");
+  if (!f) { set_global_error("cannot write %s.meta.txt", prefix); return TC_ERR_IO; }
+  fprintf(f, "%lld\n%lld\n%lld %lld %lld %lld\n%lld\n%lld\n%lld\n%lld\n", v[0], v[1], v[2], v[3], v[4], v[5], v[6],
+          v[7], v[8], v[9]);
+  fclose(f);
+  f = fopen((p + ".vlabel.bin").c_str(), "wb");
+  if (!f) { set_global_error("cannot write %s.vlabel.bin", prefix); return TC_ERR_IO; }
+  const bool ok = fwrite(labels, 1, (size_t)n, f) == (size_t)n;
+  fclose(f);
+  if (!ok) { set_global_error("short write of %s.vlabel.bin", prefix); return TC_ERR_IO; }
+  return TC_OK;
+}
+
 void tc_csr_free(int64_t *rowptr, int32_t *colidx) {
   free(rowptr);
   free(colidx);

@@ -156,6 +156,17 @@ tc_status tc_count_dag(tc_ctx *ctx, const tc_csr *dag, const tc_opts *opts, uint
 tc_status tc_count_vertices(tc_ctx *ctx, const tc_csr *g, const tc_opts *opts, uint64_t *total,
                             uint64_t *vertex_counts, tc_stats *stats);
 
+/* Labelled intersections on the oriented graph: for every oriented edge
+ * u->v, the common out-neighbours w with vertex_labels[w] == label
+ * (Graph::intersect_num(v, u, label), graph.cc:376-391 with the label test);
+ * *total sums them over all edges (the triangles whose highest vertex
+ * carries the label).  vertex_labels: n bytes, input ids, memory kind of
+ * g->on_device; edge_counts as for tc_count.  Runs the PULL arm on every
+ * tile (the selector in opts is ignored; validate is honoured). */
+tc_status tc_count_labelled(tc_ctx *ctx, const tc_csr *g, const uint8_t *vertex_labels, int32_t label,
+                            const tc_opts *opts, uint64_t *total, uint32_t *edge_counts, int64_t edge_capacity,
+                            tc_stats *stats);
+
 /* ---- allocation-free variant ------------------------------------------- */
 
 /* Size of the fixed device scratch array behind tc_count_dag_noalloc.  Every
@@ -313,6 +324,11 @@ tc_status tc_load_graphminer(const char *prefix, int64_t *n, int64_t *nnz, int64
 tc_status tc_save_graphminer(const char *prefix, int64_t n, int64_t nnz, const int64_t *rowptr,
                              const int32_t *colidx);
 void tc_csr_free(int64_t *rowptr, int32_t *colidx);
+/* Vertex labels of a GraphMiner graph: prefix.vlabel.bin, one byte per
+ * vertex (graph.cc, "read vertex labels"); saving also records the label
+ * size and class count in prefix.meta.txt, which must exist. */
+tc_status tc_load_vlabels(const char *prefix, int64_t n, uint8_t *labels);
+tc_status tc_save_vlabels(const char *prefix, int64_t n, const uint8_t *labels);
 
 /* Host CSR checks: rowptr monotone, ids in range, rows strictly ascending,
  * no self loops (the contract of tc_count). */

@@ -41,6 +41,8 @@ def lib() -> C.CDLL:
         h.oracle_orient.argtypes = [I64, P, P, P, P]
         h.oracle_count.restype = C.c_uint64
         h.oracle_count.argtypes = [I64, P, P, P]
+        h.oracle_count_labelled.restype = C.c_uint64
+        h.oracle_count_labelled.argtypes = [I64, P, P, P, C.c_int, P]
         h.oracle_count_vertices.restype = C.c_uint64
         h.oracle_count_vertices.argtypes = [I64, P, P, P]
         h.oracle_count_rows.restype = C.c_uint64
@@ -93,6 +95,16 @@ def count_sample(dag_rowptr, dag_colidx, row_step: int):
 def orient_sample_cost(rowptr, colidx, row_step: int) -> int:
     n = len(rowptr) - 1
     return int(lib().oracle_orient_rows_cost(n, _p(rowptr), _p(colidx), int(row_step)))
+
+
+def labelled(rowptr, colidx, labels, label: int, per_edge: bool = False):
+    """Orient, then graph.cc:376-391 with the label test on every oriented edge -> (total, per-edge or None)."""
+    orow, ocol = orient(rowptr, colidx)
+    n = len(orow) - 1
+    labels = np.ascontiguousarray(labels, np.uint8)
+    out = np.zeros(max(len(ocol), 1), np.uint32) if per_edge else None
+    total = lib().oracle_count_labelled(n, _p(orow), _p(ocol), _p(labels), int(label), _p(out) if per_edge else None)
+    return int(total), (out[:len(ocol)] if per_edge else None)
 
 
 def vertex_triangles(rowptr, colidx):

@@ -104,6 +104,36 @@ uint64_t oracle_count(int64_t n, const int64_t *rowptr, const int32_t *colidx, u
   return oracle_count_rows(n, rowptr, colidx, 0, n, 1, per_edge);
 }
 
+/* graph.cc:376-391 with the label test: over every edge u->v of an oriented
+ * graph with sorted rows, the common out-neighbours w with labels[w] ==
+ * label.  per_edge (optional, indexed like colidx) receives each edge's
+ * count. */
+uint64_t oracle_count_labelled(int64_t n, const int64_t *rowptr, const int32_t *colidx, const uint8_t *labels,
+                               int label, uint32_t *per_edge) {
+  uint64_t total = 0;
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : total)
+  for (int64_t u = 0; u < n; ++u) {
+    const int32_t *nu = colidx + rowptr[u];
+    const int64_t du = rowptr[u + 1] - rowptr[u];
+    for (int64_t k = 0; k < du; ++k) {
+      const int32_t v = nu[k];
+      const int32_t *nv = colidx + rowptr[v];
+      const int64_t dv = rowptr[v + 1] - rowptr[v];
+      int64_t i = 0, j = 0;
+      uint32_t num = 0;
+      while (i < du && j < dv) {
+        const int32_t a = nu[i], b = nv[j];
+        if (a <= b) ++i;
+        if (b <= a) ++j;
+        if (a == b && labels[a] == label) ++num;
+      }
+      if (per_edge) per_edge[rowptr[u] + k] = num;
+      total += num;
+    }
+  }
+  return total;
+}
+
 /* Triangles through every vertex of an oriented graph with sorted rows: the
  * merge of graph.cc:376-391 enumerates, for every edge u->v, each common
  * out-neighbour w; triangle {u, v, w} adds one to t[u], t[v] and t[w]

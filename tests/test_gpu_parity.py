@@ -165,6 +165,38 @@ def test_vertex_counts_seeded(engine, spec):
     assert abs(transitivity - 3 * ref_total / pairs.sum()) < 1e-12
 
 
+def test_labelled_counts_golden(engine, golden):
+    rng = np.random.default_rng(9)
+    for case in golden:
+        rowptr, colidx = csr_of(case)
+        labels = rng.integers(0, 3, len(rowptr) - 1).astype(np.uint8)
+        for label in range(3):
+            ref, ref_pe = oracle.labelled(rowptr, colidx, labels, label, per_edge=True)
+            total, pe, _ = engine.count_labelled(rowptr, colidx, labels, label, edge_counts=True)
+            assert total == ref, (case["name"], label)
+            assert np.array_equal(pe, ref_pe), (case["name"], label)
+
+
+@pytest.mark.parametrize("spec", [
+    tc.GenSpec("er", n=16384, avg_degree=16, seed=0),
+    tc.GenSpec("rmat", scale=16, edge_factor=16, seed=1),
+    tc.GenSpec("chung_lu", n=50000, avg_degree=24, gamma=2.1, seed=3),
+    tc.GenSpec("rmat", scale=20, edge_factor=16, seed=4),
+])
+def test_labelled_counts_seeded(engine, spec):
+    rowptr, colidx = gen_csr(spec)
+    labels = np.random.default_rng(5).integers(0, 4, len(rowptr) - 1).astype(np.uint8)
+    ref_all = oracle.triangles(rowptr, colidx)
+    totals = []
+    for label in range(4):
+        ref, ref_pe = oracle.labelled(rowptr, colidx, labels, label, per_edge=True)
+        total, pe, _ = engine.count_labelled(rowptr, colidx, labels, label, edge_counts=True)
+        assert total == ref and np.array_equal(pe, ref_pe), label
+        assert engine.count_labelled(rowptr, colidx, labels, label)[0] == ref, (label, "total only")
+        totals.append(total)
+    assert sum(totals) == ref_all  # every triangle's highest vertex carries one label
+
+
 def test_device_generators_match_host(engine):
     import torch
     for spec in [tc.GenSpec("er", n=100000, avg_degree=8, seed=11),

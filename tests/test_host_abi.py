@@ -96,6 +96,21 @@ def test_graphminer_round_trip(tmp_path):
     assert g.V() == n and g.E() == len(c) and g.get_degree(3) == r[4] - r[3]
 
 
+def test_vertex_labels_round_trip(tmp_path):
+    n, s, d = tc.gen_edges_host(tc.GenSpec("er", n=300, avg_degree=5, seed=2))
+    r, c = tc.csr_from_edges_host(n, s, d)
+    tc.save_graphminer(str(tmp_path / "g"), r, c)
+    labels = np.random.default_rng(1).integers(0, 5, n).astype(np.uint8)
+    tc.save_vlabels(str(tmp_path / "g"), labels)
+    meta = (tmp_path / "g.meta.txt").read_text().split()
+    assert meta[4] == "1" and int(meta[8]) == int(labels.max()) + 1  # label size, vertex classes
+    assert np.array_equal(tc.load_vlabels(str(tmp_path / "g"), n), labels)
+    r2, c2 = tc.load_graphminer(str(tmp_path / "g"))  # the graph still loads
+    assert np.array_equal(r, r2) and np.array_equal(c, c2)
+    with pytest.raises(tc.TCError):
+        tc.load_vlabels(str(tmp_path / "g"), n + 1)  # wrong length
+
+
 def test_graphminer_malformed_files(tmp_path):
     r = np.array([0, 1, 2], np.int64)
     c = np.array([1, 0], np.int32)

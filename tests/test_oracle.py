@@ -72,6 +72,29 @@ def test_random_graphs_per_vertex_brute_force():
             assert oracle.vertex_triangles(rowptr, colidx)[1].tolist() == expect
 
 
+def test_labelled_counts_python_statement(golden):
+    """graph.cc:376-391 with the label test, stated in Python on the oriented graph."""
+    rng = np.random.default_rng(3)
+    for case in golden:
+        rowptr, colidx = csr_of(case)
+        n = len(rowptr) - 1
+        labels = rng.integers(0, 3, n).astype(np.uint8)
+        orow, ocol = oracle.orient(rowptr, colidx)
+        totals = []
+        for label in range(3):
+            expect_pe = []
+            for u in range(n):
+                nu = ocol[orow[u]:orow[u + 1]]
+                for v in nu:
+                    nv = set(ocol[orow[v]:orow[v + 1]].tolist())
+                    expect_pe.append(sum(1 for w in nu.tolist() if w in nv and labels[w] == label))
+            total, pe = oracle.labelled(rowptr, colidx, labels, label, per_edge=True)
+            assert pe.tolist() == expect_pe, (case["name"], label)
+            assert total == sum(expect_pe)
+            totals.append(total)
+        assert sum(totals) == case["triangles"], case["name"]
+
+
 def test_random_seven_vertex_graphs():
     rng = np.random.default_rng(7)
     pairs = list(itertools.combinations(range(7), 2))
