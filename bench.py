@@ -249,6 +249,20 @@ def engine_arm(args, rank, world, local_rank, dist):
         per_vertex = {"gteps": round(world * m / (ms_v * 1e-3) / 1e9, 4), "ms_per_step": round(ms_v, 3),
                       "sum_of_vertex_counts_equals_3T": True}
         del tv
+        # labelled intersections: 4 seeded random label classes; the classes' totals add up to T
+        gen = torch.Generator(device=dev)
+        gen.manual_seed(0)
+        lab = torch.randint(0, 4, (n,), dtype=torch.uint8, device=dev, generator=gen)
+        ms_l, (tot_l0, _) = timed(lambda: eng.count_labelled_device(n, nnz, rowptr.data_ptr(), colidx.data_ptr(),
+                                                                    lab.data_ptr(), 0),
+                                  max(1, min(args.steps, 5)), 3, eng, torch, dist)
+        parts = [tot_l0] + [eng.count_labelled_device(n, nnz, rowptr.data_ptr(), colidx.data_ptr(), lab.data_ptr(),
+                                                      k)[0] for k in (1, 2, 3)]
+        if sum(parts) != total:
+            raise SystemExit("labelled counts over all classes do not add up to the total")
+        per_vertex["labelled"] = {"gteps": round(world * m / (ms_l * 1e-3) / 1e9, 4), "ms_per_step": round(ms_l, 3),
+                                  "label_classes": 4, "sum_over_classes_equals_T": True}
+        del lab
     # e2e through the public API with pinned host buffers (H2D + D2H inside)
     rowptr_h = rowptr.cpu().pin_memory()
     colidx_h = colidx.cpu().pin_memory()

@@ -358,6 +358,17 @@ class Engine:
                                             C.c_void_p(vertex_counts_ptr), C.byref(st)))
         return int(tot.value), st.as_dict()
 
+    def count_labelled_device(self, n: int, nnz: int, rowptr_ptr: int, colidx_ptr: int, labels_ptr: int, label: int,
+                              *, validate: bool = True):
+        """Labelled count of a device-resident CSR with device labels (n bytes): (total, stats dict)."""
+        g = _ffi.Csr(int(n), int(nnz), int(rowptr_ptr), int(colidx_ptr), 1)
+        o = _opts("fixed", None, validate)
+        tot = C.c_uint64(0)
+        st = _ffi.Stats()
+        self._chk(self._L.tc_count_labelled(self._h, C.byref(g), C.c_void_p(labels_ptr), int(label), C.byref(o),
+                                            C.byref(tot), None, 0, C.byref(st)))
+        return int(tot.value), st.as_dict()
+
     def count_host_ptr(self, n: int, nnz: int, rowptr_ptr: int, colidx_ptr: int, *, selector: str = "fixed",
                        force_arm=None, validate: bool = True):
         """Like count() but on caller-owned host buffers (e.g. pinned memory)."""
