@@ -1029,24 +1029,24 @@ __device__ __forceinline__ uint32_t attr_search_count(const int32_t *__restrict_
 
 // ---- PULL (edges grouped by target) ---------------------------------------------------
 //
-// The edges of PULL tiles are grouped by target v with a counting sort per
-// source block (in-edge histogram, exclusive scan, scatter of edge and row
-// ids; tiles of other arms are skipped whole, so the grouping costs little
-// when no tile chose PULL).
-// A warp takes up to 2048 grouped entries; for each run of equal v it loads N+(v)
-// once into its shared-memory bitmap or hash table and probes, for every
-// in-edge u->v of the run, the part of N+(u) that can close a triangle (the
-// row after v in relabelled order), flattened over 32 edges at a time.  Hub
-// targets have thousands of in-edges, so one table serves them all and each
-// edge costs its row suffix at one shared-memory test per entry, not a
-// search per key.  The order inside a group depends on atomics; counts do not.
+// The edges of PULL tiles are grouped by target v with one counting sort
+// (key histogram, exclusive scan, scatter of (edge, row) records; tiles of
+// other arms are skipped whole, so the grouping costs little when no tile
+// chose PULL).  A warp takes up to 2048 grouped entries; for each run of
+// equal v it loads N+(v) once into its shared-memory bitmap or hash table and
+// probes, for every in-edge u->v of the run, the part of N+(u) that can close
+// a triangle (the row after v in relabelled order), 32 edges at a time as one
+// flattened sequence of 16-byte groups.  Hub targets have thousands of
+// in-edges, so one table serves them all and each edge costs its row suffix
+// at one shared-memory test per entry, not a search per key.  The order
+// inside a group depends on atomics; counts do not.
 
 constexpr int PL_THREADS = 128;
 constexpr int PL_WARPS = PL_THREADS / 32;
 constexpr int PL_WORDS = 2048;  // per warp: a 65536-id bitmap or a 2048-slot hash table
 constexpr int PL_ITEM = 2048;      // largest work chunk (grouped entries)
 constexpr int PL_ITEM_MIN = 256;   // smallest, near the end of the work
-constexpr int PL_UNROLL = 4;
+constexpr int PL_UNROLL = 4;      // table build: list loads in flight per lane
 constexpr int PL_GUNROLL = 4;      // flattened probing: 16-byte loads in flight per lane
 constexpr int PL_GROUP_THREADS = 256;
 
