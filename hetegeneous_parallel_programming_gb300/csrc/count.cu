@@ -92,12 +92,27 @@ __device__ int mlp_select(const float *__restrict__ w, const float *f, int lane)
   return best;
 }
 
+// Grouping key of the PULL arm's counting sort (see the PULL section).
+struct PullKeys {
+  int64_t hub0;         // first hub id: n - min(n, hub_span)
+  int64_t hub_span;     // hub ids, one key per (source block, hub)
+  int64_t block_edges;  // edges per source block
+  int64_t global0;      // first key of the non-hub part: blocks * hub_span
+  __device__ __forceinline__ int64_t key(int64_t e, int32_t v) const {
+    return v >= hub0 ? (e / block_edges) * hub_span + (v - hub0) : global0 + v;
+  }
+};
+
+// One warp per tile: features, the arm, the queue key and the algorithmic
+// bytes; a tile that goes to PULL also adds its edges' grouping keys to the
+// PULL histogram while its columns are still in cache.
 __global__ void __launch_bounds__(PLAN_THREADS) plan_kernel(DevDag g, int64_t T, int selector, int force_arm,
                                                            const float *__restrict__ mlp, float *__restrict__ feats,
                                                            int32_t *__restrict__ arm_out,
                                                            uint64_t *__restrict__ qkeys,
                                                            uint32_t *__restrict__ qvals,
-                                                           unsigned long long *__restrict__ tile_bytes) {
+                                                           unsigned long long *__restrict__ tile_bytes,
+                                                           PullKeys pk, unsigned *__restrict__ pull_cnt) {
   extern __shared__ float s_w[];
   const int lane = threadIdx.x & 31;
   if (selector == TC_SELECT_LEARNED) {
@@ -173,7 +188,10 @@ __global__ void __launch_bounds__(PLAN_THREADS) plan_kernel(DevDag g, int64_t T,
   if (selector == TC_SELECT_FORCE) arm = force_arm;
   else if (selector == TC_SELECT_LEARNED) arm = mlp_select(s_w, f, lane);
   else arm = fixed_select(st);
+  arm = __shfl_sync(TC_FULL_MASK, arm, 0);
   if (lane < TC_MLP_FEATURES) feats[t * TC_MLP_FEATURES + lane] = f[lane];
+  if (arm == TC_ARM_PULL)
+    for (int64_t e = e0 + lane; e < e1; e += 32) atomicAdd(pull_cnt + pk.key(e, g.col[e]), 1u);
   if (lane == 0) {
     arm_out[t] = arm;
     const unsigned long long W40 = (1ULL << 40) - 1;
@@ -1064,27 +1082,6 @@ constexpr int64_t PL_HUB = (int64_t)PL_WORDS * 32;  // 65536
 constexpr int64_t PL_BLOCK_TILES = 2560;            // 10.5M edges, 42 MB of adjacency
 constexpr int PL_MAX_BLOCKS = 64;
 
-struct PullKeys {
-  int64_t hub0;         // first hub id: n - min(n, PL_HUB)
-  int64_t block_edges;  // edges per source block
-  int64_t global0;      // first key of the non-hub part: blocks * PL_HUB
-  __device__ __forceinline__ int64_t key(int64_t e, int32_t v) const {
-    return v >= hub0 ? (e / block_edges) * PL_HUB + (v - hub0) : global0 + v;
-  }
-};
-
-// key histogram of the PULL tiles' edges: cnt[key] += 1
-__global__ void __launch_bounds__(PL_GROUP_THREADS) pull_hist_kernel(const int32_t *__restrict__ col,
-                                                                    const int32_t *__restrict__ arm, int64_t m,
-                                                                    PullKeys pk, unsigned *__restrict__ cnt) {
-  const int64_t T = (m + TILE_EDGES - 1) / TILE_EDGES;
-  for (int64_t t = blockIdx.x; t < T; t += gridDim.x) {
-    if (arm[t] != TC_ARM_PULL) continue;
-    const int64_t e1 = min(m, (t + 1) * TILE_EDGES);
-    for (int64_t e = t * TILE_EDGES + threadIdx.x; e < e1; e += PL_GROUP_THREADS)
-      atomicAdd(cnt + pk.key(e, __ldg(col + e)), 1u);
-  }
-}
 
 // pos[key] starts at the exclusive scan of the histogram; each edge takes the
 // next slot of its key's group and stores (edge id, row) there
@@ -1528,6 +1525,7 @@ static int64_t pull_key_count(int64_t n, int64_t T, PullKeys *pk) {
   const int64_t per_block = std::max<int64_t>(PL_BLOCK_TILES, (T + PL_MAX_BLOCKS - 1) / PL_MAX_BLOCKS);
   const int64_t blocks = std::max<int64_t>(1, (T + per_block - 1) / per_block);
   if (pk) {
+    pk->hub_span = PL_HUB;
     pk->hub0 = n - std::min<int64_t>(n, PL_HUB);
     pk->block_edges = per_block * TILE_EDGES;
     pk->global0 = blocks * PL_HUB;
@@ -1535,17 +1533,15 @@ static int64_t pull_key_count(int64_t n, int64_t T, PullKeys *pk) {
   return blocks * PL_HUB + n;
 }
 
-// PULL arm: group the PULL tiles' edges (one counting sort), then count.  The
-// grouping kernels run over every tile (each skips tiles of other arms) since
-// the number of PULL tiles is known only on the device.
+// PULL arm: group the PULL tiles' edges (one counting sort: plan_kernel
+// counted the keys), then count.  The scatter kernel runs over every tile
+// (each block skips tiles of other arms) since the number of PULL tiles is
+// known only on the device.
 static tc_status run_pull(tc_ctx *ctx, const DevDag &g, CountBufs &cb, uint32_t *out, int64_t T) {
   PullKeys pk;
   const int64_t K = pull_key_count(g.n, T, &pk);
   unsigned *pos = cb.pull_pos;
   const int gblocks = (int)std::min<int64_t>(T, (int64_t)ctx->num_sms * 8);
-  TC_CHECK_CUDA(ctx, cudaMemsetAsync(cb.pull_pos, 0, sizeof(uint32_t) * (K + 1), ctx->stream));
-  pull_hist_kernel<<<gblocks, PL_GROUP_THREADS, 0, ctx->stream>>>(g.col, cb.arm, g.m, pk, pos);
-  TC_CHECK_LAUNCH(ctx);
   TC_TRY(exclusive_scan_u32(ctx, cb.pull_pos, cb.pull_pos, K + 1, cb.sort_scratch));
   pull_scatter_kernel<<<gblocks, PL_GROUP_THREADS, 0, ctx->stream>>>(g.col, g.src, cb.arm, g.m, pk, pos,
                                                                      cb.pull_er);
@@ -1578,9 +1574,12 @@ tc_status run_count(tc_ctx *ctx, const DevDag &g, const tc_opts &opts, CountBufs
   } else {
     const int plan_blocks = (int)((T + (PLAN_THREADS / 32) - 1) / (PLAN_THREADS / 32));
     const size_t plan_smem = opts.selector == TC_SELECT_LEARNED ? TC_MLP_PARAM_COUNT * sizeof(float) : 0;
+    PullKeys pk;
+    const int64_t K = pull_key_count(g.n, T, &pk);
+    TC_CHECK_CUDA(ctx, cudaMemsetAsync(cb.pull_pos, 0, sizeof(uint32_t) * (K + 1), ctx->stream));
     plan_kernel<<<plan_blocks, PLAN_THREADS, plan_smem, ctx->stream>>>(g, T, opts.selector, opts.force_arm,
                                                                        ctx->d_mlp, cb.features, cb.arm, cb.qkeys0,
-                                                                       cb.qvals0, cb.tile_bytes);
+                                                                       cb.qvals0, cb.tile_bytes, pk, cb.pull_pos);
     TC_CHECK_LAUNCH(ctx);
   }
   uint64_t *sk = cb.qkeys0;
