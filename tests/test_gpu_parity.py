@@ -315,12 +315,30 @@ def test_batch_matches_per_graph(engine):
     ([0, 1, 2, 5], [1, 0]),             # rowptr[n] != nnz
 ])
 def test_invalid_graphs_rejected(engine, rowptr, colidx):
-    with pytest.raises(tc.TCError) as ei:
-        engine.count(np.array(rowptr), np.array(colidx))
-    assert ei.value.status == 2
+    n = len(rowptr) - 1
+    calls = [lambda: engine.count(np.array(rowptr), np.array(colidx)),
+             lambda: engine.count_vertices(np.array(rowptr), np.array(colidx)),
+             lambda: engine.count_labelled(np.array(rowptr), np.array(colidx), np.zeros(n, np.uint8), 0)]
+    for call in calls:
+        with pytest.raises(tc.TCError) as ei:
+            call()
+        assert ei.value.status == 2
     # the ctx stays usable
-    total, _, _ = engine.count(np.array([0, 2, 4, 6]), np.array([1, 2, 0, 2, 0, 1]))
-    assert total == 1
+    tri = (np.array([0, 2, 4, 6]), np.array([1, 2, 0, 2, 0, 1]))
+    assert engine.count(*tri)[0] == 1
+    total, t, _ = engine.count_vertices(*tri)
+    assert total == 1 and t.tolist() == [1, 1, 1]
+
+
+def test_labelled_arguments_checked(engine):
+    tri = (np.array([0, 2, 4, 6]), np.array([1, 2, 0, 2, 0, 1]))
+    with pytest.raises(tc.TCError):
+        engine.count_labelled(*tri, np.zeros(3, np.uint8), 256)  # labels are bytes
+    with pytest.raises(ValueError):
+        engine.count_labelled(*tri, np.zeros(2, np.uint8), 0)    # one label per vertex
+    labels = np.array([0, 1, 2], np.uint8)
+    # the triangle's highest vertex (rank order: equal degrees, so id 2) carries label 2
+    assert [engine.count_labelled(*tri, labels, lab)[0] for lab in range(3)] == [0, 0, 1]
 
 
 def test_empty_and_tiny(engine):
