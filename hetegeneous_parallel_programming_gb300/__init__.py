@@ -23,7 +23,7 @@ from ._ffi import (ARM_NAMES, GEN_CHUNG_LU, GEN_ER, GEN_RGG, GEN_RMAT, SELECT_FI
 __all__ = ["TCError", "Engine", "Graph", "TCSolver", "GenSpec", "gen_edges_host", "gen_batch_host",
            "load_vlabels", "save_vlabels",
            "csr_from_edges_host",
-           "load_graphminer", "save_graphminer", "check_csr", "ARM_NAMES", "TC_NUM_ARMS", "TC_MLP_FEATURES",
+           "load_graphminer", "save_graphminer", "load_metis_part", "assemble_metis", "PART_RULES", "check_csr", "ARM_NAMES", "TC_NUM_ARMS", "TC_MLP_FEATURES",
            "TC_MLP_PARAM_COUNT", "TILE_EDGES"]
 
 
@@ -193,6 +193,49 @@ def save_vlabels(prefix: str, labels: np.ndarray) -> None:
     _check(_ffi.lib().tc_save_vlabels(str(prefix).encode(), len(labels), _ptr(labels)))
 
 
+def load_metis_part(prefix: str) -> dict:
+    """One partition file set of a METIS-partitioned graph (prefix e.g.
+    "<graph dir>/metis/pgraph0"): sizes from the meta file and the arrays
+    rowptr [n+1], colidx [nnz], vertex_list [n_real], part [n]
+    (graph_partition.cc:501-594 writes them, graph.cc:16-58 reads them)."""
+    L = _ffi.lib()
+    mp = _ffi.MetisPart()
+    _check(L.tc_load_metis_part(str(prefix).encode(), C.byref(mp)))
+    try:
+        out = {k: int(getattr(mp, k)) for k in ("n", "n_real", "nnz", "max_subg_nv", "max_subg_ne", "max_degree")}
+        out["rowptr"] = np.ctypeslib.as_array(mp.rowptr, shape=(mp.n + 1,)).copy()
+        out["colidx"] = np.ctypeslib.as_array(mp.colidx, shape=(max(mp.nnz, 1),))[:mp.nnz].copy()
+        out["vertex_list"] = np.ctypeslib.as_array(mp.vertex_list, shape=(max(mp.n_real, 1),))[:mp.n_real].copy()
+        out["part"] = np.ctypeslib.as_array(mp.part, shape=(mp.n,)).copy()
+    finally:
+        L.tc_metis_part_free(C.byref(mp))
+    return out
+
+
+def assemble_metis(prefix: str, num_parts: int) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """The whole oriented graph from partition file sets prefix0 ..
+    prefix{num_parts-1}: (rowptr, colidx, part), each row taken from the
+    partition that owns it, after the consistency checks of tc_assemble_metis."""
+    L = _ffi.lib()
+    n, nnz = C.c_int64(0), C.c_int64(0)
+    rp = C.POINTER(C.c_int64)()
+    cl = C.POINTER(C.c_int32)()
+    pt = C.POINTER(C.c_int64)()
+    _check(L.tc_assemble_metis(str(prefix).encode(), int(num_parts), C.byref(n), C.byref(nnz), C.byref(rp),
+                               C.byref(cl), C.byref(pt)))
+    try:
+        rowptr = np.ctypeslib.as_array(rp, shape=(n.value + 1,)).copy()
+        colidx = np.ctypeslib.as_array(cl, shape=(max(nnz.value, 1),))[:nnz.value].copy()
+        part = np.ctypeslib.as_array(pt, shape=(n.value,)).copy()
+    finally:
+        L.tc_csr_free(C.cast(rp, C.c_void_p), C.cast(cl, C.c_void_p))
+        L.tc_host_free(C.cast(pt, C.c_void_p))
+    return rowptr, colidx, part
+
+
+PART_RULES = {"source": _ffi.PART_BY_SOURCE, "push_pull": _ffi.PART_PUSH_PULL}
+
+
 def check_csr(rowptr: np.ndarray, colidx: np.ndarray, sorted_simple: bool = True) -> None:
     rowptr, colidx = _i64(rowptr), _i32(colidx)
     _check(_ffi.lib().tc_check_csr_host(len(rowptr) - 1, len(colidx), _ptr(rowptr), _ptr(colidx),
@@ -314,6 +357,28 @@ class Engine:
         if out is not None:
             out = out[:len(colidx)]
         return int(tot.value), out, st.as_dict()
+
+    def count_dag_parts(self, rowptr, colidx, part, num_parts: int, *, rule: str = "source",
+                        selector: str = "fixed", force_arm=None, validate: bool = True):
+        """Per-partition partial counts of an oriented graph split by part
+        (int64[n]): (total, part_totals uint64[num_parts], stats).  rule
+        "source" credits edge u->v to part[u]; "push_pull" follows the
+        reference's push/pull split (a cross-partition edge with
+        d+(u) < d+(v) is credited to part[v])."""
+        rowptr, colidx = _i64(rowptr), _i32(colidx)
+        part = np.ascontiguousarray(part, np.int64)
+        if len(part) != len(rowptr) - 1:
+            raise ValueError(f"part holds {len(part)} entries, the graph {len(rowptr) - 1} vertices")
+        if rule not in PART_RULES:
+            raise ValueError(f"rule must be one of {sorted(PART_RULES)}")
+        g = _ffi.Csr(len(rowptr) - 1, len(colidx), _ptr(rowptr).value, _ptr(colidx).value, 0)
+        o = _opts(selector, force_arm, validate)
+        tot = C.c_uint64(0)
+        out = np.zeros(max(int(num_parts), 1), np.uint64)
+        st = _ffi.Stats()
+        self._chk(self._L.tc_count_dag_parts(self._h, C.byref(g), _ptr(part), int(num_parts), PART_RULES[rule],
+                                             C.byref(o), C.byref(tot), _ptr(out), C.byref(st)))
+        return int(tot.value), out[:int(num_parts)], st.as_dict()
 
     def count_edges(self, n: int, src, dst, *, selector: str = "fixed", force_arm=None):
         """Triangles of an undirected edge list (duplicates and self loops allowed)."""

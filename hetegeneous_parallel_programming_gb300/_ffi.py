@@ -57,6 +57,16 @@ class Stats(C.Structure):
         return d
 
 
+class MetisPart(C.Structure):
+    _fields_ = [("n", C.c_int64), ("n_real", C.c_int64), ("nnz", C.c_int64), ("max_subg_nv", C.c_int64),
+                ("max_subg_ne", C.c_int64), ("max_degree", C.c_int64), ("rowptr", C.POINTER(C.c_int64)),
+                ("colidx", C.POINTER(C.c_int32)), ("vertex_list", C.POINTER(C.c_int32)),
+                ("part", C.POINTER(C.c_int64))]
+
+
+PART_BY_SOURCE, PART_PUSH_PULL = 0, 1
+
+
 class Batch(C.Structure):
     _fields_ = [("num_graphs", C.c_int64), ("vtx_off", C.c_void_p), ("rowptr", C.c_void_p),
                 ("colidx", C.c_void_p), ("on_device", C.c_int32)]
@@ -96,6 +106,7 @@ _SIGS = {
     "tc_count_labelled": (C.c_int, [P, C.POINTER(Csr), P, I32, C.POINTER(Opts), PU64, P, I64, C.POINTER(Stats)]),
     "tc_batch_count": (C.c_int, [P, C.POINTER(Batch), C.POINTER(Opts), P, C.POINTER(Stats)]),
     "tc_count_dag_noalloc": (C.c_int, [C.c_int, P, P, I64, I64, P, P, P]),
+    "tc_count_dag_parts": (C.c_int, [P, C.POINTER(Csr), P, I32, I32, C.POINTER(Opts), PU64, P, C.POINTER(Stats)]),
     "tc_count_edges": (C.c_int, [P, I64, I64, P, P, I32, C.POINTER(Opts), PU64, C.POINTER(Stats)]),
     "tc_tile_profile": (C.c_int, [P, C.POINTER(Csr), P, P, I64, PI64]),
     "tc_plan_arms": (C.c_int, [P, C.POINTER(Csr), C.POINTER(Opts), P, I64, PI64]),
@@ -118,6 +129,11 @@ _SIGS = {
     "tc_load_vlabels": (C.c_int, [C.c_char_p, I64, P]),
     "tc_save_vlabels": (C.c_int, [C.c_char_p, I64, P]),
     "tc_csr_free": (None, [P, P]),
+    "tc_load_metis_part": (C.c_int, [C.c_char_p, C.POINTER(MetisPart)]),
+    "tc_metis_part_free": (None, [C.POINTER(MetisPart)]),
+    "tc_assemble_metis": (C.c_int, [C.c_char_p, I32, PI64, PI64, C.POINTER(PI64), C.POINTER(C.POINTER(C.c_int32)),
+                                    C.POINTER(PI64)]),
+    "tc_host_free": (None, [P]),
     "tc_check_csr_host": (C.c_int, [I64, I64, P, P, I32]),
 }
 

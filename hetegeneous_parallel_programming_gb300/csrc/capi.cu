@@ -17,6 +17,7 @@ const char *flag_text(unsigned f) {
   if (f & VF_SELF_LOOP) return "a row holds a self loop";
   if (f & VF_UNSORTED) return "a row is not strictly ascending (unsorted or duplicate neighbours)";
   if (f & VF_TIMEOUT) return "a bounded device wait gave up";
+  if (f & VF_PART_RANGE) return "a partition id is outside [0, num_parts)";
   return "invalid graph";
 }
 
@@ -441,8 +442,17 @@ tc_status tc_count_vertices(tc_ctx *ctx, const tc_csr *g, const tc_opts *opts_in
   return TC_OK;
 }
 
-tc_status tc_count_dag(tc_ctx *ctx, const tc_csr *dag_in, const tc_opts *opts_in, uint64_t *total,
-                       uint32_t *edge_counts, int64_t edge_capacity, tc_stats *stats) {
+// Partitioned counting on top of tc_count_dag: the graph's part table and
+// where the per-partition sums go (host memory).
+struct PartReq {
+  const int64_t *part;
+  int32_t num_parts;
+  int32_t rule;
+  uint64_t *totals;
+};
+
+static tc_status count_dag_impl(tc_ctx *ctx, const tc_csr *dag_in, const tc_opts *opts_in, uint64_t *total,
+                                uint32_t *edge_counts, int64_t edge_capacity, tc_stats *stats, const PartReq *pr) {
   if (!ctx || !total) return set_error(ctx, TC_ERR_INVALID_ARG, "null ctx or total");
   TC_TRY(check_csr_args(ctx, dag_in));
   tc_opts o;
@@ -457,12 +467,18 @@ tc_status tc_count_dag(tc_ctx *ctx, const tc_csr *dag_in, const tc_opts *opts_in
   if (want_edges && edge_capacity < m)
     return set_error(ctx, TC_ERR_INVALID_ARG, "edge_counts holds %lld entries, %lld edges", (long long)edge_capacity,
                      (long long)m);
+  // partitioned sums need per-edge counts on the device
+  const bool dev_edges = want_edges || pr != nullptr;
   Sizer sz;
   if (!dag_in->on_device) { sz.take<int64_t>(dag_in->n + 1); sz.take<int32_t>(m); }
   sz.take<int32_t>(m);
   sz.take<int32_t>(dag_in->n);
   sz.used += count_scratch_bytes(ctx, dag_in->n, m);
-  if (want_edges && !dag_in->on_device) sz.take<uint32_t>(m);
+  if (dev_edges && !(want_edges && dag_in->on_device)) sz.take<uint32_t>(m);
+  if (pr) {
+    if (!dag_in->on_device) sz.take<int64_t>(dag_in->n);
+    sz.take<unsigned long long>(pr->num_parts);
+  }
   TC_TRY(arena_reserve(ctx, sz.used));
   Bump bump{ctx->arena, ctx->arena_cap};
   TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[0], ctx->stream));
@@ -474,7 +490,23 @@ tc_status tc_count_dag(tc_ctx *ctx, const tc_csr *dag_in, const tc_opts *opts_in
   if (count_carve(ctx, dag_in->n, m, bump, cb, o.record_tile_costs != 0) != TC_OK || bump.overflow)
     return set_error(ctx, TC_ERR_OOM, "arena overflow");
   uint32_t *d_out = nullptr;
-  if (want_edges) d_out = dag_in->on_device ? edge_counts : bump.take<uint32_t>(m);
+  if (dev_edges) d_out = (want_edges && dag_in->on_device) ? edge_counts : bump.take<uint32_t>(m);
+  const int64_t *d_part = nullptr;
+  unsigned long long *d_pt = nullptr;
+  if (pr) {
+    if (dag_in->on_device) {
+      d_part = pr->part;
+    } else {
+      int64_t *hp = bump.take<int64_t>(dag_in->n);
+      if (bump.overflow) return set_error(ctx, TC_ERR_OOM, "arena overflow");
+      TC_CHECK_CUDA(ctx, cudaMemcpyAsync(hp, pr->part, sizeof(int64_t) * (size_t)dag_in->n, cudaMemcpyHostToDevice,
+                                         ctx->stream));
+      st.h2d_bytes += sizeof(int64_t) * (size_t)dag_in->n;
+      d_part = hp;
+    }
+    d_pt = bump.take<unsigned long long>(pr->num_parts);
+    if (bump.overflow) return set_error(ctx, TC_ERR_OOM, "arena overflow");
+  }
   TC_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->d_flags, 0, sizeof(unsigned) * 8, ctx->stream));
   TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[1], ctx->stream));
   // A DAG row may hold any larger-or-smaller ids; only sortedness is required.
@@ -500,17 +532,27 @@ tc_status tc_count_dag(tc_ctx *ctx, const tc_csr *dag_in, const tc_opts *opts_in
   dag.restrict_after = 0;
   TC_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->d_total, 0, sizeof(unsigned long long), ctx->stream));
   TC_TRY(run_count(ctx, dag, o, cb, d_out, true));
+  if (pr) TC_TRY(launch_part_sums(ctx, dag, d_out, d_part, pr->num_parts, pr->rule, d_pt));
   TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[6], ctx->stream));
   if (want_edges && !dag_in->on_device && m > 0) {
     TC_CHECK_CUDA(ctx, cudaMemcpyAsync(edge_counts, d_out, sizeof(uint32_t) * (size_t)m, cudaMemcpyDeviceToHost,
                                        ctx->stream));
     st.d2h_bytes += sizeof(uint32_t) * (size_t)m;
   }
+  if (pr) {
+    TC_CHECK_CUDA(ctx, cudaMemcpyAsync(pr->totals, d_pt, sizeof(uint64_t) * (size_t)pr->num_parts,
+                                       cudaMemcpyDeviceToHost, ctx->stream));
+    TC_CHECK_CUDA(ctx, cudaMemcpyAsync(&ctx->h_pinned[1], ctx->d_flags, sizeof(unsigned) * 2, cudaMemcpyDeviceToHost,
+                                       ctx->stream));
+    st.d2h_bytes += sizeof(uint64_t) * (size_t)pr->num_parts;
+  }
   TC_CHECK_CUDA(ctx, cudaMemcpyAsync(&ctx->h_pinned[2], ctx->d_total, sizeof(unsigned long long),
                                      cudaMemcpyDeviceToHost, ctx->stream));
   st.d2h_bytes += sizeof(unsigned long long);
   TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[7], ctx->stream));
   TC_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (pr && (ctx->h_pinned[1] & VF_PART_RANGE))
+    return set_error(ctx, TC_ERR_INVALID_ARG, "%s", flag_text(VF_PART_RANGE));
   *total = ctx->h_pinned[2];
   count_stats(ctx, &st, true);
   st.ms_h2d = elapsed(ctx->ev[0], ctx->ev[1]);
@@ -523,6 +565,22 @@ tc_status tc_count_dag(tc_ctx *ctx, const tc_csr *dag_in, const tc_opts *opts_in
   st.kernel_launches = ctx->launches;
   if (stats) *stats = st;
   return TC_OK;
+}
+
+tc_status tc_count_dag(tc_ctx *ctx, const tc_csr *dag_in, const tc_opts *opts_in, uint64_t *total,
+                       uint32_t *edge_counts, int64_t edge_capacity, tc_stats *stats) {
+  return count_dag_impl(ctx, dag_in, opts_in, total, edge_counts, edge_capacity, stats, nullptr);
+}
+
+tc_status tc_count_dag_parts(tc_ctx *ctx, const tc_csr *dag, const int64_t *part, int32_t num_parts, int32_t rule,
+                             const tc_opts *opts, uint64_t *total, uint64_t *part_totals, tc_stats *stats) {
+  if (!ctx) return set_error(ctx, TC_ERR_INVALID_ARG, "null ctx");
+  if (!part || !part_totals || num_parts < 1)
+    return set_error(ctx, TC_ERR_INVALID_ARG, "null part or part_totals, or num_parts=%d < 1", (int)num_parts);
+  if (rule != TC_PART_BY_SOURCE && rule != TC_PART_PUSH_PULL)
+    return set_error(ctx, TC_ERR_INVALID_ARG, "unknown partition rule %d", (int)rule);
+  const PartReq pr{part, num_parts, rule, part_totals};
+  return count_dag_impl(ctx, dag, opts, total, nullptr, 0, stats, &pr);
 }
 
 tc_status tc_orient(tc_ctx *ctx, const tc_csr *g, int64_t *dag_rowptr, int32_t *dag_colidx, int64_t dag_capacity,

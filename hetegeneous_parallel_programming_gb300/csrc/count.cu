@@ -1357,7 +1357,7 @@ __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint2 
       }
       int bits = 3;  // hash mode: log2 of the bucket count, one bucket per entry up to 512 entries
       if (!bitmap)
-        while ((1 << bits) < nb && (4 << bits) < PL_WORDS) ++bits;
+        while ((1 << bits) < nb && (8 << bits) <= PL_WORDS) ++bits;
       // build: PL_UNROLL list loads in flight per lane
       for (int q0 = 0; q0 < nb; q0 += 32 * PL_UNROLL) {
         int32_t x[PL_UNROLL];
@@ -1666,6 +1666,87 @@ tc_status launch_vertex_sums(tc_ctx *ctx, const DevDag &g, const uint32_t *c, co
   }
   vertex_unrank_kernel<<<grid_for(ctx, g.n, 256, 8), 256, 0, ctx->stream>>>(t, rank, g.n, out);
   TC_CHECK_LAUNCH(ctx);
+  return TC_OK;
+}
+
+// ---- per-partition sums ---------------------------------------------------------
+// Each thread folds PS_CHUNK consecutive edges (rows are contiguous, so the
+// credited partition rarely changes inside a chunk) and adds each run's sum
+// once: into a block-shared table when the partitions fit, else straight
+// into the global counters.
+constexpr int PS_THREADS = 256;
+constexpr int PS_CHUNK = 16;
+constexpr int PS_SMEM_PARTS = 4096;
+
+__global__ void part_check_kernel(const int64_t *__restrict__ part, int64_t n, int num_parts, unsigned *flags) {
+  bool bad = false;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = part[u];
+    bad |= p < 0 || p >= num_parts;
+  }
+  if (__any_sync(TC_FULL_MASK, bad) && (threadIdx.x & 31) == 0) atomicOr(flags, (unsigned)VF_PART_RANGE);
+}
+
+__global__ void __launch_bounds__(PS_THREADS) part_sum_kernel(DevDag g, const uint32_t *__restrict__ c,
+                                                              const int64_t *__restrict__ part, int num_parts,
+                                                              int rule, unsigned long long *__restrict__ out) {
+  extern __shared__ unsigned long long sp[];
+  const bool shared_table = num_parts <= PS_SMEM_PARTS;
+  if (shared_table)
+    for (int q = threadIdx.x; q < num_parts; q += blockDim.x) sp[q] = 0ull;
+  __syncthreads();
+  unsigned long long *dst = shared_table ? sp : out;
+  const int64_t chunks = (g.m + PS_CHUNK - 1) / PS_CHUNK;
+  for (int64_t ch = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; ch < chunks;
+       ch += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e1 = min(ch * PS_CHUNK + PS_CHUNK, g.m);
+    int run = -1;
+    unsigned long long acc = 0;
+    int32_t u_prev = -1;
+    int64_t pu = 0, du = 0;
+    for (int64_t e = ch * PS_CHUNK; e < e1; ++e) {
+      const uint32_t ce = c[e];
+      if (ce == 0) continue;
+      const int32_t u = g.src[e];
+      if (u != u_prev) {
+        u_prev = u;
+        pu = part[u];
+        du = g.rowptr[u + 1] - g.rowptr[u];
+      }
+      int64_t p = pu;
+      if (rule == TC_PART_PUSH_PULL) {
+        const int32_t v = g.col[e];
+        const int64_t pv = part[v];
+        if (pv != pu && du < g.rowptr[v + 1] - g.rowptr[v]) p = pv;
+      }
+      if (p < 0 || p >= num_parts) continue;  // flagged by part_check_kernel
+      if ((int)p != run) {
+        if (run >= 0) atomicAdd(dst + run, acc);
+        run = (int)p;
+        acc = 0;
+      }
+      acc += ce;
+    }
+    if (run >= 0) atomicAdd(dst + run, acc);
+  }
+  if (shared_table) {
+    __syncthreads();
+    for (int q = threadIdx.x; q < num_parts; q += blockDim.x)
+      if (sp[q]) atomicAdd(out + q, sp[q]);
+  }
+}
+
+tc_status launch_part_sums(tc_ctx *ctx, const DevDag &g, const uint32_t *c, const int64_t *part, int num_parts,
+                           int rule, unsigned long long *out) {
+  TC_CHECK_CUDA(ctx, cudaMemsetAsync(out, 0, sizeof(unsigned long long) * (size_t)num_parts, ctx->stream));
+  part_check_kernel<<<grid_for(ctx, g.n, 256, 8), 256, 0, ctx->stream>>>(part, g.n, num_parts, ctx->d_flags);
+  TC_CHECK_LAUNCH(ctx);
+  if (g.m > 0) {
+    const size_t smem = num_parts <= PS_SMEM_PARTS ? sizeof(unsigned long long) * (size_t)num_parts : 0;
+    part_sum_kernel<<<grid_for(ctx, (g.m + PS_CHUNK - 1) / PS_CHUNK, PS_THREADS, 4), PS_THREADS, smem,
+                      ctx->stream>>>(g, c, part, num_parts, rule, out);
+    TC_CHECK_LAUNCH(ctx);
+  }
   return TC_OK;
 }
 

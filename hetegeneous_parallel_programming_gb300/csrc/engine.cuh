@@ -14,7 +14,8 @@ enum : unsigned {
   VF_ID_RANGE = 4u,        // column id outside [0, n)
   VF_SELF_LOOP = 8u,
   VF_UNSORTED = 16u,       // row not strictly ascending (or duplicate)
-  VF_TIMEOUT = 32u         // a bounded device wait gave up
+  VF_TIMEOUT = 32u,        // a bounded device wait gave up
+  VF_PART_RANGE = 64u      // a partition id outside [0, num_parts)
 };
 
 // A CSR resident on the device.
@@ -106,6 +107,11 @@ tc_status launch_relabel_u8(tc_ctx *ctx, const uint8_t *in, const int32_t *rank,
 // DAG, written per input id (rank[u] is u's relabelled id); t is [n] scratch
 tc_status launch_vertex_sums(tc_ctx *ctx, const DevDag &g, const uint32_t *c, const uint32_t *top,
                              unsigned long long *t, const int32_t *rank, unsigned long long *out);
+// Per-partition sums of the per-edge counts c: out[p] += c[e] for the edges
+// that `rule` (tc_part_rule) credits to partition p; part ids are checked
+// (VF_PART_RANGE).  out: num_parts device counters, zeroed here.
+tc_status launch_part_sums(tc_ctx *ctx, const DevDag &g, const uint32_t *c, const int64_t *part, int num_parts,
+                           int rule, unsigned long long *out);
 tc_status count_carve(const tc_ctx *ctx, int64_t n, int64_t m, Bump &bump, CountBufs &cb, bool want_cycles);
 // Enqueues plan, queue build and every arm kernel on the ctx stream (no host
 // sync, so it can be captured into a CUDA graph); adds the count into

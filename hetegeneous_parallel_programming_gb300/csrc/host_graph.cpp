@@ -501,6 +501,167 @@ tc_status tc_save_graphminer(const char *prefix, int64_t n, int64_t nnz, const i
   return TC_OK;
 }
 
+// ---- METIS partition files (read-only) --------------------------------------
+
+void tc_metis_part_free(tc_metis_part *p) {
+  if (!p) return;
+  free(p->rowptr);
+  free(p->colidx);
+  free(p->vertex_list);
+  free(p->part);
+  p->rowptr = nullptr;
+  p->colidx = nullptr;
+  p->vertex_list = nullptr;
+  p->part = nullptr;
+}
+
+void tc_host_free(void *p) { free(p); }
+
+tc_status tc_load_metis_part(const char *prefix, tc_metis_part *out) {
+  if (!prefix || !out) {
+    set_global_error("tc_load_metis_part: null argument");
+    return TC_ERR_INVALID_ARG;
+  }
+  memset(out, 0, sizeof(*out));
+  const std::string p(prefix);
+  std::ifstream meta((p + ".meta.txt").c_str());
+  if (!meta) { set_global_error("cannot open %s.meta.txt", prefix); return TC_ERR_IO; }
+  long long v[6] = {0, 0, 0, 0, 0, 0};
+  for (long long &x : v) meta >> x;
+  if (!meta) { set_global_error("%s.meta.txt: expected 6 integers", prefix); return TC_ERR_IO; }
+  const long long n = v[0], n_real = v[1], nnz = v[2];
+  if (n < 1 || n > 2147483647LL || n_real < 0 || n_real > n || nnz < 0) {
+    set_global_error("%s.meta.txt: bad sizes n=%lld n_real=%lld nnz=%lld", prefix, n, n_real, nnz);
+    return TC_ERR_IO;
+  }
+  tc_metis_part r;
+  r.n = n;
+  r.n_real = n_real;
+  r.nnz = nnz;
+  r.max_subg_nv = v[3];
+  r.max_subg_ne = v[4];
+  r.max_degree = v[5];
+  r.rowptr = (int64_t *)malloc(sizeof(int64_t) * (size_t)(n + 1));
+  r.colidx = (int32_t *)malloc(sizeof(int32_t) * (size_t)std::max<long long>(nnz, 1));
+  r.vertex_list = (int32_t *)malloc(sizeof(int32_t) * (size_t)std::max<long long>(n_real, 1));
+  r.part = (int64_t *)malloc(sizeof(int64_t) * (size_t)n);
+  if (!r.rowptr || !r.colidx || !r.vertex_list || !r.part) {
+    tc_metis_part_free(&r);
+    set_global_error("host allocation failed");
+    return TC_ERR_OOM;
+  }
+  if (!read_exact(p + ".vertex.bin", r.rowptr, sizeof(int64_t) * (size_t)(n + 1)) ||
+      !read_exact(p + ".edge.bin", r.colidx, sizeof(int32_t) * (size_t)nnz) ||
+      !read_exact(p + ".vertex_list.bin", r.vertex_list, sizeof(int32_t) * (size_t)n_real) ||
+      !read_exact(p + ".part.bin", r.part, sizeof(int64_t) * (size_t)n)) {
+    tc_metis_part_free(&r);
+    set_global_error("%s: .vertex.bin / .edge.bin / .vertex_list.bin / .part.bin missing or of the wrong length",
+                     prefix);
+    return TC_ERR_IO;
+  }
+  tc_status st = tc_check_csr_host(n, nnz, r.rowptr, r.colidx, 0);
+  if (st != TC_OK) { tc_metis_part_free(&r); return st; }
+  for (long long i = 0; i < n_real; ++i) {
+    if (r.vertex_list[i] < 0 || r.vertex_list[i] >= n) {
+      tc_metis_part_free(&r);
+      set_global_error("%s.vertex_list.bin: vertex %d outside [0, %lld)", prefix, (int)r.vertex_list[i], n);
+      return TC_ERR_INVALID_GRAPH;
+    }
+  }
+  *out = r;
+  return TC_OK;
+}
+
+tc_status tc_assemble_metis(const char *prefix, int32_t num_parts, int64_t *n_out, int64_t *nnz_out,
+                            int64_t **rowptr_out, int32_t **colidx_out, int64_t **part_out) {
+  if (!prefix || num_parts < 1 || !n_out || !nnz_out || !rowptr_out || !colidx_out) {
+    set_global_error("tc_assemble_metis: bad arguments");
+    return TC_ERR_INVALID_ARG;
+  }
+  std::vector<tc_metis_part> parts((size_t)num_parts);
+  for (tc_metis_part &q : parts) memset(&q, 0, sizeof(q));
+  auto fail = [&](tc_status s) {
+    for (tc_metis_part &q : parts) tc_metis_part_free(&q);
+    return s;
+  };
+  for (int32_t k = 0; k < num_parts; ++k) {
+    const std::string pk = std::string(prefix) + std::to_string(k);
+    tc_status st = tc_load_metis_part(pk.c_str(), &parts[(size_t)k]);
+    if (st != TC_OK) return fail(st);
+  }
+  const int64_t n = parts[0].n;
+  const int64_t *part = parts[0].part;
+  int64_t owned = 0;
+  for (int32_t k = 0; k < num_parts; ++k) {
+    const tc_metis_part &q = parts[(size_t)k];
+    if (q.n != n || memcmp(q.part, part, sizeof(int64_t) * (size_t)n) != 0) {
+      set_global_error("%s%d: vertex count or part table differs from %s0", prefix, (int)k, prefix);
+      return fail(TC_ERR_INVALID_GRAPH);
+    }
+    owned += q.n_real;
+  }
+  for (int64_t v = 0; v < n; ++v) {
+    if (part[v] < 0 || part[v] >= num_parts) {
+      set_global_error("%s0.part.bin: vertex %lld in partition %lld, outside [0, %d)", prefix, (long long)v,
+                       (long long)part[v], (int)num_parts);
+      return fail(TC_ERR_INVALID_GRAPH);
+    }
+  }
+  if (owned != n) {
+    set_global_error("the vertex lists hold %lld vertices, the graph %lld", (long long)owned, (long long)n);
+    return fail(TC_ERR_INVALID_GRAPH);
+  }
+  // each vertex_list is its partition's vertices in ascending order
+  std::vector<int64_t> seen((size_t)num_parts, 0);
+  for (int64_t v = 0; v < n; ++v) {
+    const tc_metis_part &q = parts[(size_t)part[v]];
+    const int64_t i = seen[(size_t)part[v]]++;
+    if (i >= q.n_real || q.vertex_list[i] != v) {
+      set_global_error("%s%lld.vertex_list.bin does not list partition %lld's vertices in order (vertex %lld)", prefix,
+                       (long long)part[v], (long long)part[v], (long long)v);
+      return fail(TC_ERR_INVALID_GRAPH);
+    }
+  }
+  // rows: owned rows from their partition, every other row empty
+  int64_t *rowptr = (int64_t *)malloc(sizeof(int64_t) * (size_t)(n + 1));
+  if (!rowptr) { set_global_error("host allocation failed"); return fail(TC_ERR_OOM); }
+  rowptr[0] = 0;
+  for (int64_t v = 0; v < n; ++v) {
+    for (int32_t k = 0; k < num_parts; ++k) {
+      const tc_metis_part &q = parts[(size_t)k];
+      if (k != part[v] && q.rowptr[v + 1] != q.rowptr[v]) {
+        free(rowptr);
+        set_global_error("%s%d: row %lld holds entries but vertex %lld belongs to partition %lld", prefix, (int)k,
+                         (long long)v, (long long)v, (long long)part[v]);
+        return fail(TC_ERR_INVALID_GRAPH);
+      }
+    }
+    const tc_metis_part &o = parts[(size_t)part[v]];
+    rowptr[v + 1] = rowptr[v] + (o.rowptr[v + 1] - o.rowptr[v]);
+  }
+  const int64_t nnz = rowptr[n];
+  int32_t *col = (int32_t *)malloc(sizeof(int32_t) * (size_t)std::max<int64_t>(nnz, 1));
+  int64_t *part_copy = part_out ? (int64_t *)malloc(sizeof(int64_t) * (size_t)n) : nullptr;
+  if (!col || (part_out && !part_copy)) {
+    free(rowptr); free(col); free(part_copy);
+    set_global_error("host allocation failed");
+    return fail(TC_ERR_OOM);
+  }
+#pragma omp parallel for schedule(dynamic, 4096)
+  for (int64_t v = 0; v < n; ++v) {
+    const tc_metis_part &o = parts[(size_t)part[v]];
+    memcpy(col + rowptr[v], o.colidx + o.rowptr[v], sizeof(int32_t) * (size_t)(rowptr[v + 1] - rowptr[v]));
+  }
+  if (part_copy) memcpy(part_copy, part, sizeof(int64_t) * (size_t)n);
+  fail(TC_OK);
+  *n_out = n;
+  *nnz_out = nnz;
+  *rowptr_out = rowptr;
+  *colidx_out = col;
+  if (part_out) *part_out = part_copy;
+  return TC_OK;
+}
+
 tc_status tc_load_vlabels(const char *prefix, int64_t n, uint8_t *labels) {
   if (!prefix || n < 1 || !labels) {
     set_global_error("tc_load_vlabels: bad arguments");

@@ -330,6 +330,69 @@ void tc_csr_free(int64_t *rowptr, int32_t *colidx);
 tc_status tc_load_vlabels(const char *prefix, int64_t n, uint8_t *labels);
 tc_status tc_save_vlabels(const char *prefix, int64_t n, const uint8_t *labels);
 
+/* One partition of a METIS-partitioned GraphMiner graph, the files the
+ * reference's partitioner writes (PartitionedGraph::metis_write_into_file,
+ * successful_push_pull/graph_partition.cc:501-594) and its partitioned
+ * loader reads (successful_push_pull/graph.cc:16-58 under USE_METIS):
+ *   prefix.meta.txt         n n_real nnz max_subg_nv max_subg_ne max_degree
+ *   prefix.vertex.bin       int64[n+1]: rows of all n vertices, only the
+ *                           partition's own vertices have entries
+ *   prefix.edge.bin         int32[nnz]: neighbours, global ids
+ *   prefix.vertex_list.bin  int32[n_real]: the partition's own vertices
+ *   prefix.part.bin         int64[n]: the partition of every vertex
+ * prefix names one file set, e.g. "<graph dir>/metis/pgraph0".  The
+ * partitioner runs on the oriented graph (metis_partition.cc:11), so the
+ * rows are out-lists of the degree-ordered DAG.  Read-only here: building
+ * partitions needs libmetis, which this engine does not use. */
+typedef struct tc_metis_part {
+  int64_t n, n_real, nnz, max_subg_nv, max_subg_ne, max_degree;
+  int64_t *rowptr;       /* [n+1]    malloc'd                                 */
+  int32_t *colidx;       /* [nnz]    malloc'd                                 */
+  int32_t *vertex_list;  /* [n_real] malloc'd                                 */
+  int64_t *part;         /* [n]      malloc'd                                 */
+} tc_metis_part;
+
+/* Read one partition; checks the sizes against the meta file and that the
+ * rows are monotone with ids in [0, n).  Release with tc_metis_part_free. */
+tc_status tc_load_metis_part(const char *prefix, tc_metis_part *out);
+void tc_metis_part_free(tc_metis_part *p);
+
+/* The whole oriented graph from its num_parts partition file sets
+ * prefix0 .. prefix{num_parts-1} (prefix e.g. "<graph dir>/metis/pgraph"):
+ * row v comes from the partition that owns v.  Checks that every file set
+ * has the same n and part table, that part values lie in [0, num_parts),
+ * that each vertex_list is exactly the partition's vertices in ascending
+ * order, that only owned rows hold entries and that the row lengths add
+ * up.  rowptr/colidx are released with tc_csr_free, part (optional, int64[n])
+ * with tc_host_free. */
+tc_status tc_assemble_metis(const char *prefix, int32_t num_parts, int64_t *n, int64_t *nnz, int64_t **rowptr,
+                            int32_t **colidx, int64_t **part);
+void tc_host_free(void *p);
+
+/* Which partition an edge u->v's intersection is credited to. */
+typedef enum tc_part_rule {
+  /* part[u]: the owner of the row (the local loop of the reference's
+   * partitioned solver, successful_push_pull/bs_warp_vertex_nvshmem.cuh:25-40,
+   * and its pull path, :133-136) */
+  TC_PART_BY_SOURCE = 0,
+  /* the reference's push/pull split: an edge whose ends lie in different
+   * partitions with d+(u) < d+(v) is pushed to and counted by part[v]
+   * (bs_warp_vertex_nvshmem.cuh:127-132 and the receiver, :224-232); every
+   * other edge by part[u] */
+  TC_PART_PUSH_PULL = 1
+} tc_part_rule;
+
+/* Per-partition partial counts on an oriented graph (the tc_count_dag
+ * contract) whose vertices are split by part[v] in [0, num_parts):
+ * part_totals[p] = sum of |N+(u) n N+(v)| over the edges u->v that `rule`
+ * credits to p, i.e. what PE p of the reference's partitioned solver adds to
+ * its total; *total = their sum.  part: int64[n] (the part.bin type), memory
+ * kind of dag->on_device; part_totals: uint64[num_parts], host memory.  A
+ * part value outside [0, num_parts) is rejected with TC_ERR_INVALID_ARG. */
+tc_status tc_count_dag_parts(tc_ctx *ctx, const tc_csr *dag, const int64_t *part, int32_t num_parts,
+                             int32_t rule, const tc_opts *opts, uint64_t *total, uint64_t *part_totals,
+                             tc_stats *stats);
+
 /* Host CSR checks: rowptr monotone, ids in range, rows strictly ascending,
  * no self loops (the contract of tc_count). */
 tc_status tc_check_csr_host(int64_t n, int64_t nnz, const int64_t *rowptr, const int32_t *colidx,

@@ -117,6 +117,49 @@ def vertex_triangles(rowptr, colidx):
     return int(total), t[:n]
 
 
+def partition_totals(dag_rowptr, dag_colidx, part, num_parts: int, rule: str = "source"):
+    """Per-PE partial counts of the reference's partitioned solver
+    (successful_push_pull/bs_warp_vertex_nvshmem.cuh) on an oriented graph:
+    every PE walks its own vertices u (:25-29); an edge u->v inside the
+    partition is counted there (:36-38); a cross-partition edge is pulled
+    and counted by part[u] when d+(u) >= d+(v), else pushed to and counted
+    by part[v] (:127-136, receiver :224-232).  rule "source" credits every
+    edge to part[u].  -> (total, uint64[num_parts])."""
+    dag_rowptr = np.ascontiguousarray(dag_rowptr, np.int64)
+    dag_colidx = np.ascontiguousarray(dag_colidx, np.int32)
+    part = np.asarray(part, np.int64)
+    total, pe = count(dag_rowptr, dag_colidx, per_edge=True)
+    dplus = np.diff(dag_rowptr)
+    src = np.repeat(np.arange(len(dplus)), dplus)
+    dst = dag_colidx.astype(np.int64)
+    credit = part[src].copy()
+    if rule == "push_pull":
+        push = (part[dst] != part[src]) & (dplus[src] < dplus[dst])
+        credit[push] = part[dst][push]
+    elif rule != "source":
+        raise ValueError(rule)
+    out = np.zeros(num_parts, np.uint64)
+    np.add.at(out, credit, pe.astype(np.uint64))
+    return total, out
+
+
+def py_partition_totals(dag_rowptr, dag_colidx, part, num_parts: int, rule: str = "source"):
+    """partition_totals stated as the PE loops themselves, in pure Python
+    (small graphs only): PE p walks u in its vertex list, v in N+(u)."""
+    n = len(dag_rowptr) - 1
+    rows = [set(int(x) for x in dag_colidx[dag_rowptr[u]:dag_rowptr[u + 1]]) for u in range(n)]
+    out = [0] * num_parts
+    for p in range(num_parts):
+        for u in (x for x in range(n) if part[x] == p):
+            for v in dag_colidx[dag_rowptr[u]:dag_rowptr[u + 1]]:
+                c = len(rows[u] & rows[int(v)])
+                if rule == "push_pull" and part[v] != p and len(rows[u]) < len(rows[int(v)]):
+                    out[int(part[v])] += c  # pushed: the receiver on part[v] counts it
+                else:
+                    out[p] += c
+    return sum(out), out
+
+
 def triangles(rowptr, colidx, per_edge: bool = False):
     """Full CPU path: orient then count."""
     orow, ocol = orient(rowptr, colidx)

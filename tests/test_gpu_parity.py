@@ -372,3 +372,71 @@ def test_cli_matches_reference_usage(golden, tmp_path):
                          capture_output=True, text=True, timeout=300)
     assert out.returncode == 0, out.stderr
     assert f"total_num_triangles = {case['triangles']}" in out.stdout
+
+
+def test_partition_counts_golden(engine, golden):
+    """Per-PE partial counts of the partitioned solver, both credit rules."""
+    rng = np.random.default_rng(21)
+    for case in golden:
+        rowptr, colidx = csr_of(case)
+        orow, ocol = oracle.orient(rowptr, colidx)
+        for k in (1, 3):
+            part = rng.integers(0, k, len(orow) - 1).astype(np.int64)
+            for rule in ("source", "push_pull"):
+                total, pt, _ = engine.count_dag_parts(orow, ocol, part, k, rule=rule)
+                ref, ref_pt = oracle.partition_totals(orow, ocol, part, k, rule)
+                assert total == ref == case["triangles"], (case["name"], k, rule)
+                assert np.array_equal(pt, ref_pt), (case["name"], k, rule)
+
+
+@pytest.mark.parametrize("k", [8, 5000])  # shared-memory table / global counters
+def test_partition_counts_seeded_from_files(engine, tmp_path, metis_writer, k):
+    rowptr, colidx = gen_csr(tc.GenSpec("rmat", scale=16, edge_factor=16, seed=3))
+    orow, ocol = oracle.orient(rowptr, colidx)
+    n = len(orow) - 1
+    # contiguous id blocks, as a locality-seeking partitioner would give, with a shuffled tail
+    part = (np.arange(n, dtype=np.int64) * k) // n
+    tail = np.random.default_rng(k).permutation(n)[: n // 4]
+    part[tail] = np.random.default_rng(k + 1).integers(0, k, len(tail))
+    prefix = str(tmp_path / "pgraph")
+    if k <= 8:  # the file path: write, assemble, count
+        metis_writer(prefix, orow, ocol, part, k)
+        orow2, ocol2, part2 = tc.assemble_metis(prefix, k)
+        assert np.array_equal(orow2, orow) and np.array_equal(ocol2, ocol) and np.array_equal(part2, part)
+    for rule in ("source", "push_pull"):
+        for arm in (None, 9):
+            total, pt, _ = engine.count_dag_parts(orow, ocol, part, k, rule=rule, force_arm=arm)
+            ref, ref_pt = oracle.partition_totals(orow, ocol, part, k, rule)
+            assert total == ref and np.array_equal(pt, ref_pt), (k, rule, arm)
+    total, _, _ = engine.count_dag(orow, ocol)
+    assert total == ref
+
+
+def test_partition_arguments_checked(engine, golden):
+    rowptr, colidx = csr_of(golden[0])
+    orow, ocol = oracle.orient(rowptr, colidx)
+    n = len(orow) - 1
+    part = np.zeros(n, np.int64)
+    for bad in (-1, 2):
+        p = part.copy()
+        p[n - 1] = bad
+        with pytest.raises(tc.TCError) as ei:
+            engine.count_dag_parts(orow, ocol, p, 2)
+        assert ei.value.status == 1 and "partition id" in str(ei.value)
+    with pytest.raises(tc.TCError):
+        engine.count_dag_parts(orow, ocol, part, 0)
+    with pytest.raises(ValueError):
+        engine.count_dag_parts(orow, ocol, part, 1, rule="owner")
+    with pytest.raises(ValueError):
+        engine.count_dag_parts(orow, ocol, part[:-1], 1)
+    # an unknown rule through the C ABI itself
+    import ctypes as C
+    from hetegeneous_parallel_programming_gb300 import _ffi
+    g = _ffi.Csr(n, len(ocol), orow.ctypes.data, ocol.ctypes.data, 0)
+    tot = C.c_uint64(0)
+    out = np.zeros(1, np.uint64)
+    assert engine._L.tc_count_dag_parts(engine._h, C.byref(g), part.ctypes.data, 1, 7, None, C.byref(tot),
+                                        out.ctypes.data, None) == 1
+    # the ctx stays usable
+    total, pt, _ = engine.count_dag_parts(orow, ocol, part, 1)
+    assert total == golden[0]["triangles"] and pt.tolist() == [total]

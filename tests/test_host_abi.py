@@ -151,3 +151,79 @@ def test_check_csr_rejects(rowptr, colidx, why):
     with pytest.raises(tc.TCError) as ei:
         tc.check_csr(np.array(rowptr), np.array(colidx), sorted_simple=True)
     assert ei.value.status == 2
+
+
+def _partitioned_dag(seed=4, n=600, k=4):
+    nn, s, d = tc.gen_edges_host(tc.GenSpec("rmat", scale=9, edge_factor=8, seed=seed))
+    r, c = oracle.csr_from_edges(nn, s, d)
+    orow, ocol = oracle.orient(r, c)
+    part = np.random.default_rng(seed).integers(0, k, len(orow) - 1).astype(np.int64)
+    return orow, ocol, part
+
+
+def test_metis_parts_load_and_assemble(tmp_path, metis_writer):
+    orow, ocol, part = _partitioned_dag()
+    (tmp_path / "metis").mkdir()
+    prefix = str(tmp_path / "metis" / "pgraph")
+    metis_writer(prefix, orow, ocol, part, 4)
+    deg = np.diff(orow)
+    for p in range(4):
+        mp = tc.load_metis_part(prefix + str(p))
+        own = np.flatnonzero(part == p)
+        assert mp["n"] == len(orow) - 1 and mp["n_real"] == len(own)
+        assert mp["nnz"] == int(deg[own].sum()) and mp["max_degree"] == int(deg.max())
+        assert np.array_equal(mp["vertex_list"], own) and np.array_equal(mp["part"], part)
+        sub_deg = np.diff(mp["rowptr"])
+        assert np.array_equal(sub_deg, np.where(part == p, deg, 0))
+    r, c, pt = tc.assemble_metis(prefix, 4)
+    assert np.array_equal(r, orow) and np.array_equal(c, ocol) and np.array_equal(pt, part)
+
+
+def test_metis_parts_inconsistent_rejected(tmp_path, metis_writer):
+    orow, ocol, part = _partitioned_dag(seed=5, k=3)
+    prefix = str(tmp_path / "pgraph")
+    metis_writer(prefix, orow, ocol, part, 3)
+    with pytest.raises(tc.TCError) as ei:  # a fourth file set does not exist
+        tc.assemble_metis(prefix, 4)
+    assert ei.value.status == 5
+    # a part table that differs between file sets
+    other = part.copy()
+    other[0] = (other[0] + 1) % 3
+    other.tofile(prefix + "1.part.bin")
+    with pytest.raises(tc.TCError) as ei:
+        tc.assemble_metis(prefix, 3)
+    assert ei.value.status == 2
+    # partition ids outside [0, num_parts): the same files read as two partitions
+    metis_writer(prefix, orow, ocol, part, 3)
+    with pytest.raises(tc.TCError) as ei:
+        tc.assemble_metis(prefix, 2)
+    assert ei.value.status == 2
+    # a vertex list that misses a vertex
+    vl = np.fromfile(prefix + "0.vertex_list.bin", np.int32)
+    vl[-1] = vl[0]
+    vl.tofile(prefix + "0.vertex_list.bin")
+    with pytest.raises(tc.TCError) as ei:
+        tc.assemble_metis(prefix, 3)
+    assert ei.value.status == 2
+    # a row with entries in a partition that does not own it
+    metis_writer(prefix, orow, ocol, part, 3)
+    deg = np.diff(orow)
+    u = int(np.flatnonzero((part != 0) & (deg > 0))[0])
+    rows = (part == 0) | (np.arange(len(deg)) == u)
+    np.concatenate([[0], np.cumsum(np.where(rows, deg, 0))]).astype(np.int64).tofile(prefix + "0.vertex.bin")
+    np.concatenate([ocol[orow[v]:orow[v + 1]] for v in np.flatnonzero(rows)]).astype(np.int32).tofile(
+        prefix + "0.edge.bin")
+    meta = (tmp_path / "pgraph0.meta.txt").read_text().split()
+    meta[2] = str(int(deg[rows].sum()))
+    (tmp_path / "pgraph0.meta.txt").write_text("\n".join(meta) + "\n")
+    assert tc.load_metis_part(prefix + "0")["nnz"] == int(deg[rows].sum())  # the file set itself reads
+    with pytest.raises(tc.TCError) as ei:
+        tc.assemble_metis(prefix, 3)
+    assert ei.value.status == 2 and "belongs to partition" in str(ei.value)
+    # a truncated vertex list against its meta file
+    metis_writer(prefix, orow, ocol, part, 3)
+    vl = np.fromfile(prefix + "2.vertex_list.bin", np.int32)
+    vl[:-1].tofile(prefix + "2.vertex_list.bin")
+    with pytest.raises(tc.TCError) as ei:
+        tc.load_metis_part(prefix + "2")
+    assert ei.value.status == 5

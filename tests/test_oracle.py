@@ -141,3 +141,19 @@ def test_batch_count_matches_individual(golden):
         base += len(c)
     totals = oracle.batch_count(vtx_off, np.concatenate(rowptr), np.concatenate(cols))
     assert totals.tolist() == [c["triangles"] for c in golden[:20]]
+
+
+def test_partition_totals_python_statement(golden):
+    """The per-PE partial counts (both credit rules) against the PE loops stated in Python."""
+    rng = np.random.default_rng(9)
+    for case in golden:
+        rowptr, colidx = csr_of(case)
+        orow, ocol = oracle.orient(rowptr, colidx)
+        n = len(orow) - 1
+        for k in (1, 2, 3):
+            part = rng.integers(0, k, n).astype(np.int64)
+            for rule in ("source", "push_pull"):
+                total, pt = oracle.partition_totals(orow, ocol, part, k, rule)
+                t2, pt2 = oracle.py_partition_totals(orow, ocol, part, k, rule)
+                assert pt.tolist() == pt2, (case["name"], k, rule)
+                assert total == t2 == case["triangles"]
