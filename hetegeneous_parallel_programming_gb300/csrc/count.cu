@@ -1149,10 +1149,13 @@ __device__ __forceinline__ uint32_t pull_test(const uint32_t *tb, int32_t base, 
 // edge and adds them to the edge's shared counter when it moves on to the
 // next edge.
 struct PullBatch {
-  int32_t gend[32];   // inclusive prefix sum of the edges' group counts
-  int32_t vlo[32];    // first valid entry of the edge in the batch's entry numbering
-  int32_t vhi[32];    // one past its last valid entry
-  long long vb[32];   // 16-byte block index of group g of the edge: vb + g
+  // per edge of the batch, one 16-byte record read in one load:
+  //   x: inclusive prefix sum of the edges' group counts
+  //   y: first valid entry of the edge in the batch's entry numbering
+  //   z: one past its last valid entry
+  //   w: 16-byte block of group g of the edge, counted from the block that
+  //      holds col[0]: w + g (fits 32 bits, m < 2^32)
+  int4 ed[32];
   uint32_t hits[32];  // PER_EDGE: triangles of each edge of the batch
 };
 
@@ -1196,14 +1199,12 @@ __device__ __forceinline__ void pull_run(const DevDag &g, const uint2 *__restric
     }
     const int G = __shfl_sync(TC_FULL_MASK, gincl, 31);
     const int gexcl = gincl - ng;
-    sb.gend[lane] = gincl;
-    sb.vlo[lane] = 4 * gexcl + off;
-    sb.vhi[lane] = 4 * gexcl + off + na;
-    sb.vb[lane] = (long long)(A >> 4) - gexcl;
+    const uintptr_t col_blk = reinterpret_cast<uintptr_t>(g.col) >> 4;
+    sb.ed[lane] = make_int4(gincl, 4 * gexcl + off, 4 * gexcl + off + na, (int)((A >> 4) - col_blk) - gexcl);
     if (PER_EDGE) sb.hits[lane] = 0u;
     __syncwarp();
-    int c = 0, cend = sb.gend[0], clo = sb.vlo[0], chi = sb.vhi[0];
-    long long cvb = sb.vb[0];
+    int c = 0;
+    int4 cur = sb.ed[0];
     uint32_t h = 0;
     int hc = 0;  // PER_EDGE: the edge h belongs to
     for (int gb = 0; gb < G; gb += 32 * PL_GUNROLL) {
@@ -1218,19 +1219,14 @@ __device__ __forceinline__ void pull_run(const DevDag &g, const uint2 *__restric
         lo[j] = 0;
         hi[j] = 0;
         if (gi < G) {
-          while (gi >= cend) {  // ends: gend[31] == G > gi
-            ++c;
-            cend = sb.gend[c];
-            clo = sb.vlo[c];
-            chi = sb.vhi[c];
-            cvb = sb.vb[c];
-          }
-          q[j] = __ldg(reinterpret_cast<const int4 *>((uintptr_t)(cvb + gi) << 4));
-          lo[j] = clo - 4 * gi;
-          hi[j] = chi - 4 * gi;
+          while (gi >= cur.x) cur = sb.ed[++c];  // ends: ed[31].x == G > gi
+          q[j] = __ldg(reinterpret_cast<const int4 *>((col_blk + (uintptr_t)(cur.w + gi)) << 4));
+          lo[j] = cur.y - 4 * gi;
+          hi[j] = cur.z - 4 * gi;
         }
         ce[j] = c;
-        if (TOP) gfirst[j] = (long long)((((uintptr_t)(cvb + gi)) << 4) - reinterpret_cast<uintptr_t>(g.col)) >> 2;
+        if (TOP)
+          gfirst[j] = (long long)(((col_blk + (uintptr_t)(cur.w + gi)) << 4) - reinterpret_cast<uintptr_t>(g.col)) >> 2;
       }
 #pragma unroll
       for (int j = 0; j < PL_GUNROLL; ++j) {
