@@ -1067,6 +1067,16 @@ constexpr int PL_ITEM_MIN = 256;   // smallest, near the end of the work
 constexpr int PL_UNROLL = 4;      // table build: list loads in flight per lane
 constexpr int PL_GUNROLL = 4;      // flattened probing: 16-byte loads in flight per lane
 constexpr int PL_GROUP_THREADS = 256;
+// Dense edges: an edge u->v whose source is a hub and whose row suffix holds
+// more than PL_DENSE_NUM / PL_DENSE_DEN entries per 32-bit word of v's
+// bitmap table is counted by ANDing u's hub bit row with the table, 32
+// candidates per word, instead of probing the suffix entry by entry.
+constexpr int PL_DENSE_NUM = 1;
+constexpr int PL_DENSE_DEN = 1;
+// Dense edges join two of the top PL_DENSE_HUB ids; their bit rows take
+// PL_DENSE_HUB^2 / 8 bytes (512 MB).
+constexpr int64_t PL_DENSE_HUB = 65536;
+constexpr int PL_DUNROLL = 2;  // dense edges: 16-byte word loads in flight per lane
 
 // One counting sort groups the PULL tiles' edges.  A target among the top
 // PL_HUB ids (ids are degree ranks) always fits the bitmap window, since all
@@ -1159,11 +1169,20 @@ struct PullBatch {
   uint32_t hits[32];  // PER_EDGE: triangles of each edge of the batch
 };
 
-template <bool BITMAP, bool PER_EDGE, bool TOP, bool LABEL>
+// Dense edges (DENSE, bitmap tables of hub targets only): the table's base is
+// hub0 + 128 * woff4, so its 16-byte word j lines up with word woff4 + j of
+// every hub bit row; tw4 16-byte words cover it.
+struct PullDense {
+  int32_t hub0;
+  int woff4, tw4;
+};
+
+template <bool BITMAP, bool PER_EDGE, bool TOP, bool LABEL, bool DENSE>
 __device__ __forceinline__ void pull_run(const DevDag &g, const uint2 *__restrict__ er, int64_t k, int64_t k2,
                                          bool have_b, const uint32_t *tb, int32_t base, int bits, int lane,
                                          PullBatch &sb, uint32_t *out, unsigned long long &acc,
-                                         unsigned long long *tile_cycles, unsigned long long build_share) {
+                                         unsigned long long *tile_cycles, unsigned long long build_share,
+                                         PullDense pd) {
   int64_t e_n = -1;
   int32_t r_n = 0;
   if (k + lane < k2) {
@@ -1187,6 +1206,11 @@ __device__ __forceinline__ void pull_run(const DevDag &g, const uint2 *__restric
       const int64_t re = g.rowptr[r + 1];
       a0 = g.restrict_after ? e + 1 : g.rowptr[r];
       na = (int)(re - a0);
+    }
+    bool dense = false;
+    if (DENSE) {  // counted by the word loop below instead of probed
+      dense = e >= 0 && r >= pd.hub0 && (int64_t)na * PL_DENSE_DEN > (int64_t)PL_DENSE_NUM * 4 * pd.tw4;
+      if (dense) na = 0;
     }
     const uintptr_t A = reinterpret_cast<uintptr_t>(g.col + a0);
     const int off = na > 0 ? (int)((A >> 2) & 3u) : 0;
@@ -1247,6 +1271,60 @@ __device__ __forceinline__ void pull_run(const DevDag &g, const uint2 *__restric
           }
       }
     }
+    // DENSE: the batch's dense edges, flattened over the lanes as (edge,
+    // 16-byte word) pairs, PL_DUNROLL word loads in flight per lane; the
+    // per-edge sums go to the edges' hit counters (they have no probe hits)
+    uint32_t dc = 0;
+    if (DENSE) {
+      const unsigned dm = __ballot_sync(TC_FULL_MASK, dense);
+      if (dm) {
+        if (PER_EDGE && h) {  // flush the probe hits before the records are reused
+          atomicAdd(&sb.hits[hc], h);
+          h = 0;
+        }
+        __syncwarp();
+        if (dense) sb.ed[__popc(dm & lanemask_lt())] = make_int4(r - pd.hub0, lane, 0, 0);
+        __syncwarp();
+        const int nd = __popc(dm), tw4 = pd.tw4;
+        const uint4 *t4 = reinterpret_cast<const uint4 *>(tb);
+        int d = lane / tw4, j = lane - d * tw4;  // pair lane + 32 i
+        int cd = d;
+        for (int f0 = 0; f0 < nd * tw4; f0 += 32 * PL_DUNROLL) {
+          uint4 a[PL_DUNROLL], b[PL_DUNROLL];
+          int du[PL_DUNROLL];
+#pragma unroll
+          for (int u = 0; u < PL_DUNROLL; ++u) {
+            du[u] = d;
+            a[u] = make_uint4(0u, 0u, 0u, 0u);
+            b[u] = a[u];
+            if (d < nd) {
+              a[u] = __ldg(g.hub_bits + (size_t)sb.ed[d].x * (size_t)g.hub_wpr4 + pd.woff4 + j);
+              b[u] = t4[j];
+            }
+            j += 32;
+            while (j >= tw4) {
+              j -= tw4;
+              ++d;
+            }
+          }
+#pragma unroll
+          for (int u = 0; u < PL_DUNROLL; ++u) {
+            const uint32_t x = __popc(a[u].x & b[u].x) + __popc(a[u].y & b[u].y) + __popc(a[u].z & b[u].z) +
+                               __popc(a[u].w & b[u].w);
+            if (PER_EDGE && du[u] != cd) {
+              if (dc) atomicAdd(&sb.hits[sb.ed[cd].y], dc);
+              cd = du[u];
+              dc = 0;
+            }
+            dc += x;
+          }
+        }
+        if (PER_EDGE) {
+          if (dc && cd < nd) atomicAdd(&sb.hits[sb.ed[cd].y], dc);
+          dc = 0;
+        }
+      }
+    }
     if (PER_EDGE) {
       if (h) atomicAdd(&sb.hits[hc], h);
       __syncwarp();
@@ -1256,7 +1334,7 @@ __device__ __forceinline__ void pull_run(const DevDag &g, const uint2 *__restric
         acc += cnt;
       }
     } else {
-      acc += h;
+      acc += h + dc;
     }
     if (tile_cycles) {  // share of this batch's time by the edge's probe count, plus the build share
       const unsigned tot = __reduce_add_sync(TC_FULL_MASK, (unsigned)(e >= 0 ? na + 1 : 0));
@@ -1297,6 +1375,7 @@ __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint2 
   __syncwarp();
   const int64_t np = (int64_t)*npull;
   const int64_t warps = (int64_t)gridDim.x * PL_WARPS;
+  const int32_t hub0 = (int32_t)(g.n - (g.n < PL_DENSE_HUB ? g.n : PL_DENSE_HUB));  // dense edges' hubs
   unsigned long long acc = 0;
   for (;;) {
     unsigned it = 0;
@@ -1320,9 +1399,21 @@ __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint2 
       }
       const int64_t bb = g.rowptr[v];
       const int nb = (int)(g.rowptr[v + 1] - bb);
-      const int32_t bmin = nb > 0 ? __ldg(g.col + bb) : 0;
-      const uint32_t span = nb > 0 ? (uint32_t)(__ldg(g.col + bb + nb - 1) - bmin) + 1u : 0u;
+      int32_t bmin = nb > 0 ? __ldg(g.col + bb) : 0;
+      uint32_t span = nb > 0 ? (uint32_t)(__ldg(g.col + bb + nb - 1) - bmin) + 1u : 0u;
       const bool bitmap = span <= (uint32_t)PL_WORDS * 32u;
+      // dense edges need the table aligned with the hub bit rows: the base goes
+      // down to a 128-id boundary counted from hub0 (a hub target's list lies
+      // in (v, n), so the window still fits)
+      PullDense pd{hub0, 0, 0};
+      const bool dense_run = MODE == 0 && g.hub_bits != nullptr && bitmap && nb > 0 && v >= hub0;
+      if (dense_run) {
+        const int32_t bmax = bmin + (int32_t)span - 1;
+        pd.woff4 = (bmin - hub0) >> 7;
+        bmin = hub0 + 128 * pd.woff4;
+        span = (uint32_t)(bmax - bmin) + 1u;
+        pd.tw4 = (int)((span + 127u) >> 7);
+      }
       if (!bitmap && nb > PL_WORDS / 2) {  // wide window and long list: warp pivot search per edge
         long long tq = tr0;
         for (int64_t q = k; q < k2; ++q) {
@@ -1387,24 +1478,30 @@ __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint2 
       constexpr bool LAB = MODE == 2;
       if (MODE == 1) {  // per-vertex counts: per-edge output plus the top-edge attribution
         if (bitmap)
-          pull_run<true, true, true, false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc,
-                                            tile_cycles, build_share);
+          pull_run<true, true, true, false, false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc,
+                                                   tile_cycles, build_share, pd);
         else
-          pull_run<false, true, true, false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc,
-                                             tile_cycles, build_share);
+          pull_run<false, true, true, false, false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc,
+                                                    tile_cycles, build_share, pd);
       } else if (out == nullptr) {  // total only
-        if (bitmap)
-          pull_run<true, false, false, LAB>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc, tile_cycles,
-                                build_share);
+        if (dense_run)
+          pull_run<true, false, false, false, MODE == 0>(g, er, k, k2, true, tb, bmin, bits, lane, s_batch[w], out,
+                                                         acc, tile_cycles, build_share, pd);
+        else if (bitmap)
+          pull_run<true, false, false, LAB, false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc,
+                                                   tile_cycles, build_share, pd);
         else
-          pull_run<false, false, false, LAB>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc, tile_cycles,
-                                 build_share);
+          pull_run<false, false, false, LAB, false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc,
+                                                    tile_cycles, build_share, pd);
+      } else if (dense_run) {
+        pull_run<true, true, false, false, MODE == 0>(g, er, k, k2, true, tb, bmin, bits, lane, s_batch[w], out, acc,
+                                                      tile_cycles, build_share, pd);
       } else if (bitmap) {
-        pull_run<true, true, false, LAB>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc, tile_cycles,
-                             build_share);
+        pull_run<true, true, false, LAB, false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc,
+                                                tile_cycles, build_share, pd);
       } else {
-        pull_run<false, true, false, LAB>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc, tile_cycles,
-                              build_share);
+        pull_run<false, true, false, LAB, false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc,
+                                                 tile_cycles, build_share, pd);
       }
       __syncwarp();
       // back to all zero: the touched word range with 16-byte stores, or the
@@ -1473,6 +1570,12 @@ static size_t count_sort_scratch_bytes(const tc_ctx *ctx, int64_t n, int64_t T) 
   return std::max(radix_sort_scratch_bytes(ctx, T > 0 ? T : 1), scan_scratch_bytes(ctx, pull_key_count(n, T, nullptr) + 1));
 }
 
+// Hub bit rows: one row per dense hub (the top min(n, PL_DENSE_HUB) ids), each
+// hub_wpr4(n) 16-byte words wide (one bit per hub id).
+static int64_t hub_rows(int64_t n) { return std::min<int64_t>(n, PL_DENSE_HUB); }
+static int hub_wpr4(int64_t n) { return (int)((hub_rows(n) + 127) / 128); }
+static int64_t hub_bits_words4(int64_t n) { return hub_rows(n) * hub_wpr4(n); }
+
 size_t count_scratch_bytes(const tc_ctx *ctx, int64_t n, int64_t m) {
   const int64_t T = (m + TILE_EDGES - 1) / TILE_EDGES;
   Sizer sz;
@@ -1488,6 +1591,7 @@ size_t count_scratch_bytes(const tc_ctx *ctx, int64_t n, int64_t m) {
   sz.take<unsigned long long>(TC_NUM_ARMS);
   sz.take<uint32_t>(pull_key_count(n, T, nullptr) + 1);
   sz.take<uint2>(m);
+  sz.take<uint4>(hub_bits_words4(n));
   return sz.used + count_sort_scratch_bytes(ctx, n, T) + 256;
 }
 
@@ -1506,6 +1610,7 @@ tc_status count_carve(const tc_ctx *ctx, int64_t n, int64_t m, Bump &bump, Count
   cb.arm_bytes = bump.take<unsigned long long>(TC_NUM_ARMS);
   cb.pull_pos = bump.take<uint32_t>(pull_key_count(n, T, nullptr) + 1);
   cb.pull_er = bump.take<uint2>(m);
+  cb.hub_bits = bump.take<uint4>(hub_bits_words4(n));
   cb.sort_scratch = bump.take<char>((int64_t)count_sort_scratch_bytes(ctx, n, T));
   return bump.overflow ? TC_ERR_OOM : TC_OK;
 }
@@ -1533,15 +1638,54 @@ static int64_t pull_key_count(int64_t n, int64_t T, PullKeys *pk) {
 // counted the keys), then count.  The scatter kernel runs over every tile
 // (each block skips tiles of other arms) since the number of PULL tiles is
 // known only on the device.
-static tc_status run_pull(tc_ctx *ctx, const DevDag &g, CountBufs &cb, uint32_t *out, int64_t T) {
+// Bit rows of the hubs' out-lists, one warp per hub row: the warp clears the
+// row, then ORs in its entries, one OR per distinct word (lanes matched by
+// word).  Every entry of a hub row is a hub (it ranks above its row).  Nothing
+// is done when no edge was grouped for the PULL arm.
+__global__ void hub_bits_kernel(DevDag g, int32_t hub0, int wpr4, const unsigned *__restrict__ npull,
+                                uint4 *__restrict__ bits) {
+  if (*npull == 0) return;
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < g.n - hub0; row += warps) {
+    uint4 *b4 = bits + row * wpr4;
+    for (int q = lane; q < wpr4; q += 32) b4[q] = make_uint4(0u, 0u, 0u, 0u);
+    __syncwarp();
+    uint32_t *b = reinterpret_cast<uint32_t *>(b4);
+    const int64_t e0 = g.rowptr[hub0 + row], e1 = g.rowptr[hub0 + row + 1];
+    for (int64_t e = e0 + lane; e - lane < e1; e += 32) {
+      const bool in = e < e1;
+      const int32_t w = in ? g.col[e] - hub0 : -1;
+      const bool ok = in && w >= 0;  // false only outside a relabelled DAG
+      const unsigned act = __ballot_sync(TC_FULL_MASK, ok);
+      if (ok) {
+        const unsigned peers = __match_any_sync(act, w >> 5);
+        const unsigned word = __reduce_or_sync(peers, 1u << (w & 31));
+        if (lane == __ffs(peers) - 1) atomicOr(b + (w >> 5), word);
+      }
+    }
+    __syncwarp();
+  }
+}
+
+static tc_status run_pull(tc_ctx *ctx, const DevDag &g_in, CountBufs &cb, uint32_t *out, int64_t T) {
   PullKeys pk;
-  const int64_t K = pull_key_count(g.n, T, &pk);
+  const int64_t K = pull_key_count(g_in.n, T, &pk);
   unsigned *pos = cb.pull_pos;
   const int gblocks = (int)std::min<int64_t>(T, (int64_t)ctx->num_sms * 8);
   TC_TRY(exclusive_scan_u32(ctx, cb.pull_pos, cb.pull_pos, K + 1, cb.sort_scratch));
-  pull_scatter_kernel<<<gblocks, PL_GROUP_THREADS, 0, ctx->stream>>>(g.col, g.src, cb.arm, g.m, pk, pos,
+  pull_scatter_kernel<<<gblocks, PL_GROUP_THREADS, 0, ctx->stream>>>(g_in.col, g_in.src, cb.arm, g_in.m, pk, pos,
                                                                      cb.pull_er);
   TC_CHECK_LAUNCH(ctx);
+  DevDag g = g_in;
+  // dense edges: plain counts of a relabelled DAG (rows hold higher ids only)
+  if (g.restrict_after && !g.top && !g.vlabel && g.m > 0) {
+    const int32_t hub0 = (int32_t)(g.n - hub_rows(g.n));
+    hub_bits_kernel<<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(g, hub0, hub_wpr4(g.n), pos + K, cb.hub_bits);
+    TC_CHECK_LAUNCH(ctx);
+    g.hub_bits = cb.hub_bits;
+    g.hub_wpr4 = hub_wpr4(g.n);
+  }
   // pos[K] (no edge has key K) still holds the number of grouped edges
   const int grid = ctx->num_sms * ctx->arm_blocks_per_sm[TC_ARM_PULL];
   if (g.top)

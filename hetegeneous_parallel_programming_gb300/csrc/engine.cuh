@@ -40,6 +40,10 @@ struct DevDag {
   const uint8_t *vlabel = nullptr;   // [n] labelled mode: vertex labels (relabelled ids; PULL arm only)
   int label = 0;                     // labelled mode: count common neighbours with this label
   int restrict_after = 0;
+  // PULL dense edges: bit rows of the DAG rows of the top hub ids, one row of
+  // hub_wpr4 16-byte words per hub (null: dense path off)
+  const uint4 *hub_bits = nullptr;
+  int hub_wpr4 = 0;
 };
 
 // Validation: sets VF_* bits in ctx->d_flags[0].
@@ -98,6 +102,7 @@ struct CountBufs {
   unsigned long long *arm_bytes;    // [TC_NUM_ARMS]
   uint32_t *pull_pos;     // [keys+1] PULL grouping: key counts, then group offsets
   uint2 *pull_er;         // [m] PULL grouping: (edge id, row) grouped by key (source block, target)
+  uint4 *hub_bits;        // [hub rows][hub words / 4] PULL dense edges: bit rows of the hubs' out-lists
   void *sort_scratch;
 };
 size_t count_scratch_bytes(const tc_ctx *ctx, int64_t n, int64_t m);

@@ -135,6 +135,27 @@ def test_pull_fallback_wide_long_lists(engine):
     assert np.array_equal(t, expect_t)
 
 
+def test_pull_dense_core(engine):
+    """A 3000-vertex core with edge probability 1/2 inside a sparse 200 000-vertex
+    graph: the core vertices are the top-ranked hubs and their row suffixes are
+    dense, so PULL counts most core edges by ANDing hub bit rows."""
+    rng = np.random.default_rng(5)
+    n, k = 200000, 3000
+    core = rng.choice(n, k, replace=False)
+    iu, ju = np.triu_indices(k, 1)
+    keep = rng.random(len(iu)) < 0.5
+    src = np.concatenate([core[iu[keep]], rng.integers(0, n, 400000)])
+    dst = np.concatenate([core[ju[keep]], rng.integers(0, n, 400000)])
+    rowptr, colidx = oracle.csr_from_edges(n, src, dst)
+    ref, ref_pe, _, _ = oracle.triangles(rowptr, colidx, per_edge=True)
+    for arm in (None, tc.ARM_NAMES.index("pull")):
+        total, pe, st = engine.count(rowptr, colidx, force_arm=arm, edge_counts=True)
+        assert total == ref and np.array_equal(pe, ref_pe), arm
+        total, _, _ = engine.count(rowptr, colidx, force_arm=arm)
+        assert total == ref, arm
+    assert st["tiles_per_arm"]["pull"] > 0
+
+
 def test_vertex_counts_golden(engine, golden):
     for case in golden:
         rowptr, colidx = csr_of(case)
