@@ -34,7 +34,7 @@ static tc_status check_csr_args(tc_ctx *ctx, const tc_csr *g) {
 }
 
 // Device copies of a caller CSR (no copy when already on the device).
-tc_status stage_csr(tc_ctx *ctx, const tc_csr *g, Bump &bump, DevCSR &d, uint64_t *h2d) {
+tc_status stage_csr(tc_ctx *ctx, const tc_csr *g, Bump &bump, DevCSR &d, uint64_t *h2d, int pieces) {
   d.n = g->n;
   d.nnz = g->nnz;
   if (g->on_device) {
@@ -47,19 +47,36 @@ tc_status stage_csr(tc_ctx *ctx, const tc_csr *g, Bump &bump, DevCSR &d, uint64_
   if (bump.overflow) return set_error(ctx, TC_ERR_OOM, "arena overflow staging the graph");
   TC_CHECK_CUDA(ctx, cudaMemcpyAsync(rp, g->rowptr, sizeof(int64_t) * (size_t)(g->n + 1), cudaMemcpyHostToDevice,
                                      ctx->stream));
-  if (g->nnz > 0)
+  if (pieces > 1) {
+    // piece k = blocks [k * per, (k + 1) * per) of the kept-count geometry
+    int G;
+    int64_t chunk;
+    orient_geometry(ctx, g->nnz, pieces, &G, &chunk);
+    const int per = (G + pieces - 1) / pieces;
+    TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->piece_ev[0], ctx->stream));
+    TC_CHECK_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->piece_ev[0], 0));
+    for (int k = 0; k < pieces; ++k) {
+      const int64_t e0 = std::min<int64_t>(g->nnz, (int64_t)k * per * chunk);
+      const int64_t e1 = std::min<int64_t>(g->nnz, (int64_t)(k + 1) * per * chunk);
+      if (e1 > e0)
+        TC_CHECK_CUDA(ctx, cudaMemcpyAsync(cl + e0, g->colidx + e0, sizeof(int32_t) * (size_t)(e1 - e0),
+                                           cudaMemcpyHostToDevice, ctx->copy_stream));
+      TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->piece_ev[k], ctx->copy_stream));
+    }
+  } else if (g->nnz > 0) {
     TC_CHECK_CUDA(ctx, cudaMemcpyAsync(cl, g->colidx, sizeof(int32_t) * (size_t)g->nnz, cudaMemcpyHostToDevice,
                                        ctx->stream));
+  }
   *h2d += sizeof(int64_t) * (size_t)(g->n + 1) + sizeof(int32_t) * (size_t)g->nnz;
   d.rowptr = rp;
   d.col = cl;
   return TC_OK;
 }
 
-void orient_sizes(const tc_ctx *ctx, int64_t n, int64_t nnz, bool perm, bool dagcol, Sizer &sz) {
+void orient_sizes(const tc_ctx *ctx, int64_t n, int64_t nnz, bool perm, bool dagcol, Sizer &sz, int pieces) {
   int G;
   int64_t chunk;
-  orient_geometry(ctx, nnz, &G, &chunk);
+  orient_geometry(ctx, nnz, pieces, &G, &chunk);
   const int64_t mmax = nnz;
   sz.take<uint64_t>(n); sz.take<uint64_t>(n);
   sz.take<int32_t>(n);
@@ -78,8 +95,9 @@ void orient_sizes(const tc_ctx *ctx, int64_t n, int64_t nnz, bool perm, bool dag
 }
 
 void orient_carve(const tc_ctx *ctx, int64_t n, int64_t nnz, bool perm, bool dagcol, Bump &bump,
-                         OrientBufs &b) {
-  orient_geometry(ctx, nnz, &b.G, &b.chunk);
+                         OrientBufs &b, int pieces) {
+  b.pieces = pieces;
+  orient_geometry(ctx, nnz, pieces, &b.G, &b.chunk);
   const int64_t mmax = nnz;
   b.vkeys0 = bump.take<uint64_t>(n);
   b.vkeys1 = bump.take<uint64_t>(n);
@@ -162,9 +180,12 @@ tc_status tc_ctx_create(int device, tc_ctx **out) {
   if (cudaGetDeviceProperties(&prop, device) != cudaSuccess)
     return fail(set_error(nullptr, TC_ERR_CUDA, "cudaGetDeviceProperties failed"));
   ctx->num_sms = prop.multiProcessorCount;
-  if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess)
+  if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) != cudaSuccess)
     return fail(set_error(nullptr, TC_ERR_CUDA, "stream creation failed"));
   for (auto &ev : ctx->ev)
+    if (cudaEventCreate(&ev) != cudaSuccess) return fail(set_error(nullptr, TC_ERR_CUDA, "event creation failed"));
+  for (auto &ev : ctx->piece_ev)
     if (cudaEventCreate(&ev) != cudaSuccess) return fail(set_error(nullptr, TC_ERR_CUDA, "event creation failed"));
   if (cudaMalloc((void **)&ctx->d_total, 256) != cudaSuccess || cudaMalloc((void **)&ctx->d_flags, 256) != cudaSuccess ||
       cudaMalloc((void **)&ctx->d_heads, 256) != cudaSuccess ||
@@ -191,8 +212,12 @@ void tc_ctx_destroy(tc_ctx *ctx) {
   cudaFree(ctx->d_mlp);
   if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
   if (ctx->batch_exec) cudaGraphExecDestroy(ctx->batch_exec);
+  if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
   for (auto &ev : ctx->ev)
     if (ev) cudaEventDestroy(ev);
+  for (auto &ev : ctx->piece_ev)
+    if (ev) cudaEventDestroy(ev);
+  if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   (void)cudaGetLastError();
   delete ctx;
@@ -222,20 +247,32 @@ tc_status tc_count(tc_ctx *ctx, const tc_csr *g, const tc_opts *opts_in, uint64_
   tc_stats st;
   memset(&st, 0, sizeof(st));
   const bool want_edges = edge_counts != nullptr;
+  // host input: the column array uploads in pieces behind the orientation's
+  // first passes (worth it once the upload takes milliseconds)
+  const int pieces = (!g->on_device && g->nnz >= (int64_t(1) << 24)) ? TC_MAX_PIECES : 1;
   // arena: staged input + orientation + counting + output staging
   Sizer sz;
   if (!g->on_device) { sz.take<int64_t>(g->n + 1); sz.take<int32_t>(g->nnz); }
-  orient_sizes(ctx, g->n, g->nnz, want_edges, false, sz);
+  orient_sizes(ctx, g->n, g->nnz, want_edges, false, sz, pieces);
   sz.used += count_scratch_bytes(ctx, g->n, g->nnz);
   if (want_edges && !g->on_device) sz.take<uint32_t>(g->nnz);
   TC_TRY(arena_reserve(ctx, sz.used));
   Bump bump{ctx->arena, ctx->arena_cap};
   TC_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->d_flags, 0, sizeof(unsigned) * 8, ctx->stream));
   TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[0], ctx->stream));
+  // every return waits for the pieces' uploads: none may outlive the call
+  // (the arena and the caller's host arrays are only borrowed)
+  struct UploadGuard {
+    tc_ctx *c;
+    bool on;
+    ~UploadGuard() {
+      if (on) cudaStreamSynchronize(c->copy_stream);
+    }
+  } upload_guard{ctx, pieces > 1};
   DevCSR d;
-  TC_TRY(stage_csr(ctx, g, bump, d, &st.h2d_bytes));
+  TC_TRY(stage_csr(ctx, g, bump, d, &st.h2d_bytes, pieces));
   OrientBufs ob;
-  orient_carve(ctx, d.n, d.nnz, want_edges, false, bump, ob);
+  orient_carve(ctx, d.n, d.nnz, want_edges, false, bump, ob, pieces);
   CountBufs cb;
   if (count_carve(ctx, d.n, d.nnz, bump, cb, o.record_tile_costs != 0) != TC_OK || bump.overflow)
     return set_error(ctx, TC_ERR_OOM, "arena overflow");
@@ -244,7 +281,8 @@ tc_status tc_count(tc_ctx *ctx, const tc_csr *g, const tc_opts *opts_in, uint64_
   int64_t m = 0;
   float ms_a = 0;
   TC_TRY(orient_front(ctx, d, o, ob, &m, &st.ms_validate, &ms_a));
-  st.ms_h2d = elapsed(ctx->ev[0], ctx->ev[1]);
+  // with pieces the upload ends at the last piece's event (it overlaps the orientation)
+  st.ms_h2d = elapsed(ctx->ev[0], pieces > 1 ? ctx->piece_ev[pieces - 1] : ctx->ev[1]);
   if (want_edges && edge_capacity < m)
     return set_error(ctx, TC_ERR_INVALID_ARG, "edge_counts holds %lld entries, %lld oriented edges",
                      (long long)edge_capacity, (long long)m);

@@ -12,6 +12,8 @@
 
 #define TC_FULL_MASK 0xffffffffu
 
+constexpr int TC_MAX_PIECES = 8;
+
 struct tc_ctx {
   int device = 0;
   int num_sms = 0;
@@ -32,6 +34,10 @@ struct tc_ctx {
   // events: [0..8) entry-point phases, [8] plan start, [9] count start,
   // [10 + a] end of arm a's kernel
   cudaEvent_t ev[10 + TC_NUM_ARMS] = {};
+  // host input of tc_count: the column array is uploaded in pieces on a
+  // second stream while the orientation starts (one event per piece)
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t piece_ev[TC_MAX_PIECES] = {};
   // learned selector
   float *d_mlp = nullptr;                 // TC_MLP_PARAM_COUNT floats
   bool mlp_loaded = false;

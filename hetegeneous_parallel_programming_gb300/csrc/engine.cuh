@@ -80,8 +80,14 @@ struct OrientBufs {
   int group_bits = 0;
   // check ids, sortedness and self loops inside the kept-count pass
   bool validate = false;
+  // column array arriving in `pieces` uploads (ctx->piece_ev): piece k is
+  // blocks [k * ceil(G / pieces), ...) of the entry-chunk geometry, and the
+  // kept-count pass runs piece by piece as they land
+  int pieces = 1;
 };
-void orient_geometry(const tc_ctx *ctx, int64_t nnz, int *G, int64_t *chunk);
+// Entry-chunk geometry: about 6 resident blocks per SM, times `pieces` when
+// the column array arrives in pieces (each piece then fills the GPU).
+void orient_geometry(const tc_ctx *ctx, int64_t nnz, int pieces, int *G, int64_t *chunk);
 tc_status orient_phase_a(tc_ctx *ctx, const DevCSR &g, OrientBufs &b);
 // out == nullptr: only the original-id DAG columns (b.dag_col) are written.
 tc_status orient_phase_b(tc_ctx *ctx, const DevCSR &g, OrientBufs &b, int64_t m, bool want_perm,
@@ -127,9 +133,13 @@ tc_status run_count(tc_ctx *ctx, const DevDag &dag, const tc_opts &opts, CountBu
 void count_stats(tc_ctx *ctx, tc_stats *st, bool timing);
 
 // Shared by the entry points (capi.cu, batch.cu).
-tc_status stage_csr(tc_ctx *ctx, const tc_csr *g, Bump &bump, DevCSR &d, uint64_t *h2d);
-void orient_sizes(const tc_ctx *ctx, int64_t n, int64_t nnz, bool perm, bool dagcol, Sizer &sz);
-void orient_carve(const tc_ctx *ctx, int64_t n, int64_t nnz, bool perm, bool dagcol, Bump &bump, OrientBufs &b);
+// pieces > 1 (host input only): rowptr is copied on the ctx stream, the
+// column array in `pieces` uploads on ctx->copy_stream, each recording
+// ctx->piece_ev[k]; the orientation's kept-count pass waits for them.
+tc_status stage_csr(tc_ctx *ctx, const tc_csr *g, Bump &bump, DevCSR &d, uint64_t *h2d, int pieces = 1);
+void orient_sizes(const tc_ctx *ctx, int64_t n, int64_t nnz, bool perm, bool dagcol, Sizer &sz, int pieces = 1);
+void orient_carve(const tc_ctx *ctx, int64_t n, int64_t nnz, bool perm, bool dagcol, Bump &bump, OrientBufs &b,
+                  int pieces = 1);
 tc_status orient_front(tc_ctx *ctx, const DevCSR &d, const tc_opts &o, OrientBufs &ob, int64_t *m, float *ms_validate,
                        float *ms_a);
 float elapsed(cudaEvent_t a, cudaEvent_t b);

@@ -14,9 +14,9 @@ namespace tc {
 constexpr int OR_THREADS = 256;
 constexpr int OR_PER = ENTRY_TILE / OR_THREADS;  // 8 entries per thread per tile
 
-void orient_geometry(const tc_ctx *ctx, int64_t nnz, int *G, int64_t *chunk) {
+void orient_geometry(const tc_ctx *ctx, int64_t nnz, int pieces, int *G, int64_t *chunk) {
   int64_t tiles = (nnz + ENTRY_TILE - 1) / ENTRY_TILE;
-  int64_t g = (int64_t)ctx->num_sms * 6;  // resident at once: 6 blocks of 256 per SM
+  int64_t g = (int64_t)ctx->num_sms * 6 * pieces;  // resident at once: 6 blocks of 256 per SM
   if (g > tiles) g = tiles;
   if (g < 1) g = 1;
   *chunk = ((tiles + g - 1) / g) * ENTRY_TILE;
@@ -118,12 +118,14 @@ __global__ void __launch_bounds__(OR_THREADS, 6) kept_count_kernel(const int64_t
                                                                int64_t nnz, int64_t chunk,
                                                                const int32_t *__restrict__ rank,
                                                                unsigned long long *__restrict__ kept,
-                                                               int64_t *__restrict__ bcount, unsigned *flags) {
+                                                               int64_t *__restrict__ bcount, unsigned *flags,
+                                                               int b_off) {
   __shared__ int rows[ENTRY_TILE];
   __shared__ int scan_tmp[32];
   __shared__ unsigned long long bsum;
   if (threadIdx.x == 0) bsum = 0;
-  const int64_t b = (int64_t)blockIdx.x * chunk, e_end = min(nnz, b + chunk);
+  const int blk = (int)blockIdx.x + b_off;  // block of the entry-chunk geometry
+  const int64_t b = (int64_t)blk * chunk, e_end = min(nnz, b + chunk);
   unsigned long long mine = 0;
   unsigned f = 0;
   const int lane = threadIdx.x & 31;
@@ -171,7 +173,7 @@ __global__ void __launch_bounds__(OR_THREADS, 6) kept_count_kernel(const int64_t
     if (lane == 0 && f) atomicOr(flags, f);
   }
   __syncthreads();
-  if (threadIdx.x == 0) bcount[blockIdx.x] = (int64_t)bsum;
+  if (threadIdx.x == 0) bcount[blk] = (int64_t)bsum;
 }
 
 
@@ -223,7 +225,7 @@ __global__ void classify_rows_kernel(const int64_t *__restrict__ len, int64_t n,
 
 tc_status orient_phase_a(tc_ctx *ctx, const DevCSR &g, OrientBufs &b) {
   const int bits = vertex_bits(g.n);
-  orient_geometry(ctx, g.nnz, &b.G, &b.chunk);
+  orient_geometry(ctx, g.nnz, b.pieces, &b.G, &b.chunk);
   const int gbits = b.vgroup ? b.group_bits : 0;
   if (2 * bits + gbits > 64) return set_error(ctx, TC_ERR_UNSUPPORTED, "rank key needs %d bits", 2 * bits + gbits);
   deg_key_kernel<<<grid_for(ctx, g.n, 256, 8), 256, 0, ctx->stream>>>(g.rowptr, g.n, bits, b.vgroup, b.vkeys0);
@@ -237,15 +239,22 @@ tc_status orient_phase_a(tc_ctx *ctx, const DevCSR &g, OrientBufs &b) {
   TC_CHECK_LAUNCH(ctx);
   TC_CHECK_CUDA(ctx, cudaMemsetAsync(b.kept, 0, sizeof(int64_t) * (size_t)(g.n + 1), ctx->stream));
   if (g.nnz > 0) {
-    if (b.validate)
-      kept_count_kernel<true><<<b.G, OR_THREADS, 0, ctx->stream>>>(g.rowptr, g.col, g.n, g.nnz, b.chunk, b.rank,
-                                                                   (unsigned long long *)b.kept, b.bcount,
-                                                                   ctx->d_flags);
-    else
-      kept_count_kernel<false><<<b.G, OR_THREADS, 0, ctx->stream>>>(g.rowptr, g.col, g.n, g.nnz, b.chunk, b.rank,
-                                                                    (unsigned long long *)b.kept, b.bcount,
-                                                                    ctx->d_flags);
-    TC_CHECK_LAUNCH(ctx);
+    // one launch per arriving piece of the column array (one piece when it
+    // is already on the device); each launch fills the GPU
+    const int per = (b.G + b.pieces - 1) / b.pieces;
+    for (int k = 0; k < b.pieces && k * per < b.G; ++k) {
+      const int blocks = per < b.G - k * per ? per : b.G - k * per;
+      if (b.pieces > 1) TC_CHECK_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->piece_ev[k], 0));
+      if (b.validate)
+        kept_count_kernel<true><<<blocks, OR_THREADS, 0, ctx->stream>>>(g.rowptr, g.col, g.n, g.nnz, b.chunk,
+                                                                        b.rank, (unsigned long long *)b.kept,
+                                                                        b.bcount, ctx->d_flags, k * per);
+      else
+        kept_count_kernel<false><<<blocks, OR_THREADS, 0, ctx->stream>>>(g.rowptr, g.col, g.n, g.nnz, b.chunk,
+                                                                         b.rank, (unsigned long long *)b.kept,
+                                                                         b.bcount, ctx->d_flags, k * per);
+      TC_CHECK_LAUNCH(ctx);
+    }
     TC_TRY(exclusive_scan_i64(ctx, b.bcount, b.bcount, b.G, b.sort_scratch, b.d_m));
   } else {
     TC_CHECK_CUDA(ctx, cudaMemsetAsync(b.d_m, 0, sizeof(int64_t), ctx->stream));

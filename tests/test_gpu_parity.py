@@ -135,6 +135,31 @@ def test_pull_fallback_wide_long_lists(engine):
     assert np.array_equal(t, expect_t)
 
 
+def test_host_input_uploaded_in_pieces(engine):
+    """Host input of >= 2^24 entries is uploaded in pieces behind the
+    orientation: a bad id in the last piece or an unsorted row in the first
+    is still caught, the call returns cleanly and the ctx counts the intact
+    graph exactly afterwards."""
+    rowptr, colidx = gen_csr(tc.GenSpec("rmat", scale=20, edge_factor=16, seed=4))
+    n = len(rowptr) - 1
+    assert len(colidx) >= 1 << 24
+    ref = oracle.triangles(rowptr, colidx)
+    bad = colidx.copy()
+    bad[-1] = n
+    with pytest.raises(tc.TCError) as ei:
+        engine.count(rowptr, bad)
+    assert ei.value.status == 2
+    bad = colidx.copy()
+    u = int(np.flatnonzero(np.diff(rowptr) >= 2)[0])
+    bad[rowptr[u]], bad[rowptr[u] + 1] = bad[rowptr[u] + 1], bad[rowptr[u]]
+    with pytest.raises(tc.TCError) as ei:
+        engine.count(rowptr, bad)
+    assert ei.value.status == 2
+    total, pe, st = engine.count(rowptr, colidx, edge_counts=True)
+    assert total == ref and int(pe.sum()) == ref
+    assert st["h2d_bytes"] == 8 * len(rowptr) + 4 * len(colidx)
+
+
 def test_pull_dense_core(engine):
     """A 3000-vertex core with edge probability 1/2 inside a sparse 200 000-vertex
     graph: the core vertices are the top-ranked hubs and their row suffixes are
