@@ -68,6 +68,7 @@ struct OrientBufs {
   int32_t *indeg;              // [n] DAG in-degree by relabelled id
   int32_t *mid_list, *big_list, *huge_list;  // [n] rows for the warp / block / global sorts
   unsigned *seg_counts;        // [3]
+  int32_t *rv = nullptr;       // [nnz] rank of every entry's target, written by the kept-count pass
   // phase B
   int32_t *ncol, *nsrc;        // [m]
   uint32_t *perm;              // [m] original slot of each relabelled edge (optional)

@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(OR_THREADS, 6) kept_count_kernel(const int64_t
                                                                const int32_t *__restrict__ rank,
                                                                unsigned long long *__restrict__ kept,
                                                                int64_t *__restrict__ bcount, unsigned *flags,
-                                                               int b_off) {
+                                                               int b_off, int32_t *__restrict__ rv_out) {
   __shared__ int rows[ENTRY_TILE];
   __shared__ int scan_tmp[32];
   __shared__ unsigned long long bsum;
@@ -142,6 +142,13 @@ __global__ void __launch_bounds__(OR_THREADS, 6) kept_count_kernel(const int64_t
     }
 #pragma unroll
     for (int k = 0; k < OR_PER; ++k) rv[k] = vv[k] >= 0 && (int64_t)vv[k] < n ? rank[vv[k]] : -1;
+    if (rv_out) {  // the placement streams these instead of gathering them again
+#pragma unroll
+      for (int k = 0; k < OR_PER; ++k) {
+        const int64_t e = t0 + k * OR_THREADS + threadIdx.x;
+        if (e < t1) rv_out[e] = rv[k];
+      }
+    }
 #pragma unroll
     for (int k = 0; k < OR_PER; ++k) {
       const int64_t e = t0 + k * OR_THREADS + threadIdx.x;
@@ -248,11 +255,11 @@ tc_status orient_phase_a(tc_ctx *ctx, const DevCSR &g, OrientBufs &b) {
       if (b.validate)
         kept_count_kernel<true><<<blocks, OR_THREADS, 0, ctx->stream>>>(g.rowptr, g.col, g.n, g.nnz, b.chunk,
                                                                         b.rank, (unsigned long long *)b.kept,
-                                                                        b.bcount, ctx->d_flags, k * per);
+                                                                        b.bcount, ctx->d_flags, k * per, b.rv);
       else
         kept_count_kernel<false><<<blocks, OR_THREADS, 0, ctx->stream>>>(g.rowptr, g.col, g.n, g.nnz, b.chunk,
                                                                          b.rank, (unsigned long long *)b.kept,
-                                                                         b.bcount, ctx->d_flags, k * per);
+                                                                         b.bcount, ctx->d_flags, k * per, b.rv);
       TC_CHECK_LAUNCH(ctx);
     }
     TC_TRY(exclusive_scan_i64(ctx, b.bcount, b.bcount, b.G, b.sort_scratch, b.d_m));
@@ -286,7 +293,8 @@ __global__ void __launch_bounds__(OR_THREADS, 6) place_kernel(const int64_t *__r
                                                           const int64_t *__restrict__ nrowptr,
                                                           int32_t *__restrict__ ncol, int32_t *__restrict__ nsrc,
                                                           uint32_t *__restrict__ perm,
-                                                          int32_t *__restrict__ dag_col) {
+                                                          int32_t *__restrict__ dag_col,
+                                                          const int32_t *__restrict__ rv_in) {
   __shared__ int rows[ENTRY_TILE];
   __shared__ int scan_tmp[32];
   __shared__ long long s_wbase[OR_THREADS / 32 + 1];
@@ -307,11 +315,14 @@ __global__ void __launch_bounds__(OR_THREADS, 6) place_kernel(const int64_t *__r
     for (int k = 0; k < OR_PER; ++k) {
       const int i = wbase + k * 32 + lane;
       const bool in = t0 + i < t1;
-      vv[k] = in ? col[t0 + i] : -1;
+      vv[k] = in && (DAGCOL || !rv_in) ? col[t0 + i] : -1;
       uu[k] = in ? rows[i] : -1;
+      if (rv_in) rv[k] = in ? rv_in[t0 + i] : -1;  // ranks of the targets, from the kept-count pass
     }
+    if (!rv_in) {
 #pragma unroll
-    for (int k = 0; k < OR_PER; ++k) rv[k] = vv[k] >= 0 && (int64_t)vv[k] < n ? rank[vv[k]] : -1;
+      for (int k = 0; k < OR_PER; ++k) rv[k] = vv[k] >= 0 && (int64_t)vv[k] < n ? rank[vv[k]] : -1;
+    }
     unsigned bal[OR_PER];
     int cnt = 0;
 #pragma unroll
@@ -597,7 +608,8 @@ tc_status orient_phase_b(tc_ctx *ctx, const DevCSR &g, OrientBufs &b, int64_t m,
   if (g.nnz > 0 && m > 0) {
 #define TC_PLACE(V, D, R)                                                                                        \
   place_kernel<V, D, R><<<b.G, OR_THREADS, 0, ctx->stream>>>(g.rowptr, g.col, g.n, g.nnz, b.chunk, b.rank, b.bcount, \
-                                                             b.orowptr, b.nrowptr, b.ncol, b.nsrc, b.perm, b.dag_col)
+                                                             b.orowptr, b.nrowptr, b.ncol, b.nsrc, b.perm, b.dag_col, \
+                                                             b.rv)
     if (!relabel) TC_PLACE(false, true, false);
     else if (want_perm && want_dag_cols) TC_PLACE(true, true, true);
     else if (want_perm) TC_PLACE(true, false, true);
