@@ -273,12 +273,15 @@ def engine_arm(args, rank, world, local_rank, dist):
     line = None
     if rank == 0:
         hbm, kind = peaks()
+        l2_gbs = eng.l2_bandwidth()
         arm = max(st["ms_arm"], key=lambda k: st["ms_arm"][k])
         achieved = st["alg_bytes_arm"][arm] / (st["ms_arm"][arm] * 1e-3) / 1e9 if st["ms_arm"][arm] > 0 else 0.0
-        traffic = None
+        traffic = l2_traffic = None
         if TRAFFIC.exists():
             tr = json.loads(TRAFFIC.read_text()).get(args.workload, {})
             traffic = tr.get(arm)
+            l2_traffic = tr.get(arm + "_l2")
+        arm_s = st["ms_arm"][arm] * 1e-3
         line = {
             "metric": "GTEPS on 1 GB300, learned vs plain selector (exact count); batched graphs/s",
             "value": round(world * m / (ms_best * 1e-3) / 1e9, 4),
@@ -319,6 +322,12 @@ def engine_arm(args, rank, world, local_rank, dist):
                                            if traffic and st["ms_arm"][arm] > 0 else None),
                          "dram_frac": (round(traffic / (st["ms_arm"][arm] * 1e-3) / 1e9 / hbm, 4)
                                        if traffic and st["ms_arm"][arm] > 0 else None),
+                         "l2": {"peak": round(l2_gbs, 1), "unit": "GB/s",
+                                "peak_kind": "measured here: tc_l2_bandwidth, 64 MB read 128 times with L1-bypassing loads",
+                                "traffic": l2_traffic,
+                                "achieved": round(l2_traffic / arm_s / 1e9, 1) if l2_traffic and arm_s > 0 else None,
+                                "frac": (round(l2_traffic / arm_s / 1e9 / l2_gbs, 4)
+                                         if l2_traffic and arm_s > 0 and l2_gbs > 0 else None)},
                          "count_phase": {"alg_bytes": int(st["alg_bytes"]),
                                          "achieved": round(st["alg_bytes"] / (st["ms_count"] * 1e-3) / 1e9, 1)
                                          if st["ms_count"] > 0 else None}},

@@ -495,6 +495,13 @@ class Engine:
                                             float(lr), float(weight_decay), int(seed), C.byref(loss)))
         return float(loss.value)
 
+    def l2_bandwidth(self, nbytes: int = 64 << 20, passes: int = 128) -> float:
+        """L2 read ceiling in GB/s: one kernel streams an L2-resident buffer
+        `passes` times with L1-bypassing 16-byte loads (tc_l2_bandwidth)."""
+        g = C.c_double(0.0)
+        self._chk(self._L.tc_l2_bandwidth(self._h, int(nbytes), int(passes), C.byref(g)))
+        return float(g.value)
+
     def set_selector_weights(self, params) -> None:
         params = np.ascontiguousarray(params, np.float32)
         self._chk(self._L.tc_selector_set_weights(self._h, _ptr(params), len(params)))

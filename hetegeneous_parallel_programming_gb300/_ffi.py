@@ -106,6 +106,7 @@ _SIGS = {
     "tc_count_labelled": (C.c_int, [P, C.POINTER(Csr), P, I32, C.POINTER(Opts), PU64, P, I64, C.POINTER(Stats)]),
     "tc_batch_count": (C.c_int, [P, C.POINTER(Batch), C.POINTER(Opts), P, C.POINTER(Stats)]),
     "tc_count_dag_noalloc": (C.c_int, [C.c_int, P, P, I64, I64, P, P, P]),
+    "tc_l2_bandwidth": (C.c_int, [P, I64, I32, C.POINTER(C.c_double)]),
     "tc_count_dag_parts": (C.c_int, [P, C.POINTER(Csr), P, I32, I32, C.POINTER(Opts), PU64, P, C.POINTER(Stats)]),
     "tc_count_edges": (C.c_int, [P, I64, I64, P, P, I32, C.POINTER(Opts), PU64, C.POINTER(Stats)]),
     "tc_tile_profile": (C.c_int, [P, C.POINTER(Csr), P, P, I64, PI64]),

@@ -156,9 +156,52 @@ tc_status orient_front(tc_ctx *ctx, const DevCSR &d, const tc_opts &o, OrientBuf
   return TC_OK;
 }
 
+// L2 read probe: every thread strides the buffer with 16-byte L2-only loads,
+// `passes` times; the XOR of what it read keeps the loads alive.
+__global__ void l2_read_kernel(const uint4 *__restrict__ buf, int64_t n4, int passes, unsigned *sink) {
+  uint32_t acc = 0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int p = 0; p < passes; ++p) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + 3 * stride < n4; i += 4 * stride) {
+      const uint4 a = __ldcg(buf + i), b = __ldcg(buf + i + stride), c = __ldcg(buf + i + 2 * stride),
+                  d = __ldcg(buf + i + 3 * stride);
+      acc ^= a.x ^ a.y ^ a.z ^ a.w ^ b.x ^ b.y ^ b.z ^ b.w ^ c.x ^ c.y ^ c.z ^ c.w ^ d.x ^ d.y ^ d.z ^ d.w;
+    }
+    for (; i < n4; i += stride) {
+      const uint4 a = __ldcg(buf + i);
+      acc ^= a.x ^ a.y ^ a.z ^ a.w;
+    }
+  }
+  if (acc == 0x9e3779b9u) atomicAdd(sink, 1u);  // practically never taken
+}
+
 }  // namespace tc
 
 extern "C" {
+
+tc_status tc_l2_bandwidth(tc_ctx *ctx, int64_t bytes, int32_t passes, double *gbs) {
+  if (!ctx || !gbs || bytes < 4096 || passes < 1)
+    return set_error(ctx, TC_ERR_INVALID_ARG, "need ctx, gbs, bytes >= 4096 and passes >= 1");
+  TC_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
+  const int64_t n4 = bytes / 16;
+  TC_TRY(arena_reserve(ctx, n4 * 16 + 256));
+  uint4 *buf = reinterpret_cast<uint4 *>(ctx->arena);
+  TC_CHECK_CUDA(ctx, cudaMemsetAsync(buf, 1, (size_t)n4 * 16, ctx->stream));
+  const int grid = ctx->num_sms * 8;
+  float best = 0.f;
+  for (int rep = 0; rep < 6; ++rep) {
+    TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[0], ctx->stream));
+    l2_read_kernel<<<grid, 256, 0, ctx->stream>>>(buf, n4, passes, ctx->d_flags + 7);
+    TC_CHECK_LAUNCH(ctx);
+    TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[1], ctx->stream));
+    TC_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    const float ms = elapsed(ctx->ev[0], ctx->ev[1]);
+    if (rep > 0 && (best == 0.f || ms < best)) best = ms;  // rep 0 warms up
+  }
+  *gbs = best > 0.f ? (double)n4 * 16.0 * passes / (best * 1e-3) / 1e9 : 0.0;
+  return TC_OK;
+}
 
 tc_status tc_ctx_create(int device, tc_ctx **out) {
   if (!out) return set_error(nullptr, TC_ERR_INVALID_ARG, "null out");

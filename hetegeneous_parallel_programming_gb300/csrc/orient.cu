@@ -544,17 +544,107 @@ __global__ void __launch_bounds__(256) seg_sort_warpsmem_kernel(const int64_t *_
   }
 }
 
+// Rows without payload whose ids span at most SEG_SMEM_MAX * 32 values are
+// sorted through a bitmap in the key buffer: one bit per entry (a row's ids
+// are distinct), a block prefix of the words' popcounts, then every thread
+// writes its words' set bits in order.
+constexpr int SEG_BITMAP_KEYS = SEG_SMEM_MAX / 256;  // keys per thread (256 threads)
+
 template <bool VALS>
 __global__ void __launch_bounds__(256) seg_sort_smem_kernel(const int64_t *__restrict__ nrowptr,
                                                            const int32_t *__restrict__ list, const unsigned *count,
                                                            int32_t *__restrict__ ncol, uint32_t *__restrict__ perm) {
   __shared__ int32_t skey[SEG_SMEM_MAX];
   __shared__ uint32_t sval[VALS ? SEG_SMEM_MAX : 1];
+  __shared__ int32_t s_red[2][8];
+  __shared__ int32_t s_wsum[8];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const unsigned cnt = *count;
   for (unsigned i = blockIdx.x; i < cnt; i += gridDim.x) {
     const int32_t r = list[i];
     const int64_t b = nrowptr[r];
     const int L = (int)(nrowptr[r + 1] - b);
+    if (!VALS) {
+      int32_t x[SEG_BITMAP_KEYS];
+      int32_t lo = 0x7fffffff, hi = -1;
+#pragma unroll
+      for (int j = 0; j < SEG_BITMAP_KEYS; ++j) {
+        const int k = (int)threadIdx.x + 256 * j;
+        x[j] = k < L ? ncol[b + k] : -1;
+        if (k < L) {
+          lo = min(lo, x[j]);
+          hi = max(hi, x[j]);
+        }
+      }
+      lo = __reduce_min_sync(TC_FULL_MASK, lo);
+      hi = __reduce_max_sync(TC_FULL_MASK, hi);
+      if (lane == 0) {
+        s_red[0][warp] = lo;
+        s_red[1][warp] = hi;
+      }
+      __syncthreads();
+      lo = s_red[0][0];
+      hi = s_red[1][0];
+#pragma unroll
+      for (int w = 1; w < 8; ++w) {
+        lo = min(lo, s_red[0][w]);
+        hi = max(hi, s_red[1][w]);
+      }
+      const int64_t span = (int64_t)hi - lo + 1;
+      if (span <= (int64_t)SEG_SMEM_MAX * 32) {  // uniform over the block
+        const int W = (int)((span + 31) >> 5);
+        uint32_t *bm = reinterpret_cast<uint32_t *>(skey);
+        for (int q = threadIdx.x; q < W; q += 256) bm[q] = 0u;
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < SEG_BITMAP_KEYS; ++j)
+          if ((int)threadIdx.x + 256 * j < L) {
+            const int d = x[j] - lo;
+            atomicOr(&bm[d >> 5], 1u << (d & 31));
+          }
+        __syncthreads();
+        // thread t owns words [t * per, (t + 1) * per)
+        const int per = (W + 255) / 256;
+        const int w0 = min(W, (int)threadIdx.x * per), w1 = min(W, w0 + per);
+        int c = 0;
+        for (int q = w0; q < w1; ++q) c += __popc(bm[q]);
+        int inc = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(TC_FULL_MASK, inc, o);
+          if (lane >= o) inc += y;
+        }
+        if (lane == 31) s_wsum[warp] = inc;
+        __syncthreads();
+        int pos = inc - c, total = 0;
+        for (int w = 0; w < 8; ++w) {
+          if (w < warp) pos += s_wsum[w];
+          total += s_wsum[w];
+        }
+        if (total != L) {  // duplicate ids (only without validation): keep them, sort by comparisons
+          __syncthreads();
+#pragma unroll
+          for (int j = 0; j < SEG_BITMAP_KEYS; ++j)
+            if ((int)threadIdx.x + 256 * j < L) skey[threadIdx.x + 256 * j] = x[j];
+          __syncthreads();
+          hybrid_flip_bitonic<VALS, true>(skey, sval, L, warp, blockDim.x >> 5, lane);
+          for (int k = threadIdx.x; k < L; k += blockDim.x) ncol[b + k] = skey[k];
+          __syncthreads();
+          continue;
+        }
+        for (int q = w0; q < w1; ++q) {
+          uint32_t bits = bm[q];
+          while (bits) {
+            const int t = __ffs(bits) - 1;
+            bits &= bits - 1;
+            ncol[b + pos++] = lo + 32 * q + t;
+          }
+        }
+        __syncthreads();
+        continue;
+      }
+      __syncthreads();  // s_red is read again by the next row
+    }
     for (int k = threadIdx.x; k < L; k += blockDim.x) {
       skey[k] = ncol[b + k];
       if (VALS) sval[k] = perm[b + k];

@@ -167,6 +167,16 @@ tc_status tc_count_labelled(tc_ctx *ctx, const tc_csr *g, const uint8_t *vertex_
                             const tc_opts *opts, uint64_t *total, uint32_t *edge_counts, int64_t edge_capacity,
                             tc_stats *stats);
 
+/* ---- measurement ---------------------------------------------------------- */
+
+/* L2 read ceiling of the ctx's GPU: one kernel reads a device buffer of
+ * `bytes` (small enough to stay in L2, e.g. 32 MB) `passes` times with
+ * 16-byte loads that bypass L1; *gbs = bytes * passes / kernel time (CUDA
+ * events on the ctx stream, best of 5 launches after a warm-up).  The
+ * roofline of the PULL arm, whose row suffixes and tables come mostly from
+ * L2, is reported against it beside the HBM copy bandwidth. */
+tc_status tc_l2_bandwidth(tc_ctx *ctx, int64_t bytes, int32_t passes, double *gbs);
+
 /* ---- allocation-free variant ------------------------------------------- */
 
 /* Size of the fixed device scratch array behind tc_count_dag_noalloc.  Every
