@@ -1095,8 +1095,14 @@ constexpr int PL_MAX_BLOCKS = 64;
 
 // pos[key] starts at the exclusive scan of the histogram; each edge takes the
 // next slot of its key's group and stores (edge id, row) there
+// Record of a grouped edge: (edge id, end of its row) when the DAG is
+// relabelled (the probed suffix is (e, rowptr[row + 1])), else (edge id,
+// row).  Edges are visited in order, so the row ends are read almost
+// sequentially here instead of at random in the probing kernel.
 __global__ void __launch_bounds__(PL_GROUP_THREADS) pull_scatter_kernel(const int32_t *__restrict__ col,
                                                                        const int32_t *__restrict__ src,
+                                                                       const int64_t *__restrict__ rowptr,
+                                                                       int row_end,
                                                                        const int32_t *__restrict__ arm, int64_t m,
                                                                        PullKeys pk,
                                                                        unsigned *__restrict__ pos,
@@ -1107,13 +1113,15 @@ __global__ void __launch_bounds__(PL_GROUP_THREADS) pull_scatter_kernel(const in
     const int64_t e1 = min(m, (t + 1) * TILE_EDGES);
     for (int64_t e = t * TILE_EDGES + threadIdx.x; e < e1; e += PL_GROUP_THREADS) {
       const unsigned slot = atomicAdd(pos + pk.key(e, __ldg(col + e)), 1u);
-      er[slot] = make_uint2((uint32_t)e, (uint32_t)__ldg(src + e));  // one 8-byte store
+      const int32_t r = __ldg(src + e);
+      const uint32_t y = row_end ? (uint32_t)__ldg(rowptr + r + 1) : (uint32_t)r;
+      er[slot] = make_uint2((uint32_t)e, y);  // one 8-byte store
     }
   }
 }
 
-// `er` holds the grouped (edge id, row) pairs; `npull` points at
-// their number.
+// `er` holds the grouped records (see pull_scatter_kernel); `npull` points
+// at their number.
 //
 // Each warp owns PL_WORDS words of shared memory, all zero between runs, and
 // a guard word after them that is never written.  A run of target v uses the
@@ -1175,6 +1183,7 @@ struct PullBatch {
 struct PullDense {
   int32_t hub0;
   int woff4, tw4;
+  int64_t hub_e0;  // first edge of the hub rows (rowptr[hub0])
 };
 
 template <bool BITMAP, bool PER_EDGE, bool TOP, bool LABEL, bool DENSE>
@@ -1184,32 +1193,36 @@ __device__ __forceinline__ void pull_run(const DevDag &g, const uint2 *__restric
                                          unsigned long long *tile_cycles, unsigned long long build_share,
                                          PullDense pd) {
   int64_t e_n = -1;
-  int32_t r_n = 0;
+  uint32_t y_n = 0;
   if (k + lane < k2) {
     const uint2 p = er[k + lane];
     e_n = p.x;
-    r_n = (int32_t)p.y;
+    y_n = p.y;
   }
   for (int64_t qb = k; qb < k2; qb += 32) {
     const long long t0 = clock64();
     const int64_t e = e_n;
-    const int32_t r = r_n;
+    const uint32_t y = y_n;  // relabelled DAG: end of the edge's row; else its row
     e_n = -1;
     if (qb + 32 + lane < k2) {  // prefetch for the next batch
       const uint2 p = er[qb + 32 + lane];
       e_n = p.x;
-      r_n = (int32_t)p.y;
+      y_n = p.y;
     }
     int64_t a0 = 0;
     int na = 0;
     if (e >= 0 && have_b) {
-      const int64_t re = g.rowptr[r + 1];
-      a0 = g.restrict_after ? e + 1 : g.rowptr[r];
-      na = (int)(re - a0);
+      if (g.restrict_after) {
+        a0 = e + 1;
+        na = (int)((int64_t)y - a0);
+      } else {
+        a0 = g.rowptr[y];
+        na = (int)(g.rowptr[y + 1] - a0);
+      }
     }
     bool dense = false;
-    if (DENSE) {  // counted by the word loop below instead of probed
-      dense = e >= 0 && r >= pd.hub0 && (int64_t)na * PL_DENSE_DEN > (int64_t)PL_DENSE_NUM * 4 * pd.tw4;
+    if (DENSE) {  // counted by the word loop below instead of probed; hub rows own edges [hub_e0, m)
+      dense = e >= pd.hub_e0 && (int64_t)na * PL_DENSE_DEN > (int64_t)PL_DENSE_NUM * 4 * pd.tw4;
       if (dense) na = 0;
     }
     const uintptr_t A = reinterpret_cast<uintptr_t>(g.col + a0);
@@ -1283,7 +1296,7 @@ __device__ __forceinline__ void pull_run(const DevDag &g, const uint2 *__restric
           h = 0;
         }
         __syncwarp();
-        if (dense) sb.ed[__popc(dm & lanemask_lt())] = make_int4(r - pd.hub0, lane, 0, 0);
+        if (dense) sb.ed[__popc(dm & lanemask_lt())] = make_int4(__ldg(g.src + e) - pd.hub0, lane, 0, 0);
         __syncwarp();
         const int nd = __popc(dm), tw4 = pd.tw4;
         const uint4 *t4 = reinterpret_cast<const uint4 *>(tb);
@@ -1376,6 +1389,7 @@ __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint2 
   const int64_t np = (int64_t)*npull;
   const int64_t warps = (int64_t)gridDim.x * PL_WARPS;
   const int32_t hub0 = (int32_t)(g.n - (g.n < PL_DENSE_HUB ? g.n : PL_DENSE_HUB));  // dense edges' hubs
+  const int64_t hub_e0 = g.hub_bits != nullptr ? g.rowptr[hub0] : g.m;
   unsigned long long acc = 0;
   for (;;) {
     unsigned it = 0;
@@ -1405,7 +1419,7 @@ __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint2 
       // dense edges need the table aligned with the hub bit rows: the base goes
       // down to a 128-id boundary counted from hub0 (a hub target's list lies
       // in (v, n), so the window still fits)
-      PullDense pd{hub0, 0, 0};
+      PullDense pd{hub0, 0, 0, hub_e0};
       const bool dense_run = MODE == 0 && g.hub_bits != nullptr && bitmap && nb > 0 && v >= hub0;
       if (dense_run) {
         const int32_t bmax = bmin + (int32_t)span - 1;
@@ -1674,7 +1688,8 @@ static tc_status run_pull(tc_ctx *ctx, const DevDag &g_in, CountBufs &cb, uint32
   unsigned *pos = cb.pull_pos;
   const int gblocks = (int)std::min<int64_t>(T, (int64_t)ctx->num_sms * 8);
   TC_TRY(exclusive_scan_u32(ctx, cb.pull_pos, cb.pull_pos, K + 1, cb.sort_scratch));
-  pull_scatter_kernel<<<gblocks, PL_GROUP_THREADS, 0, ctx->stream>>>(g_in.col, g_in.src, cb.arm, g_in.m, pk, pos,
+  pull_scatter_kernel<<<gblocks, PL_GROUP_THREADS, 0, ctx->stream>>>(g_in.col, g_in.src, g_in.rowptr,
+                                                                     g_in.restrict_after, cb.arm, g_in.m, pk, pos,
                                                                      cb.pull_er);
   TC_CHECK_LAUNCH(ctx);
   DevDag g = g_in;
