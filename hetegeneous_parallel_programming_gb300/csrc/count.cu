@@ -52,6 +52,10 @@ __device__ __forceinline__ int fixed_select(const PlanStats &s) {
   if (s.mean_in >= 256.f && s.mean_db >= 32.f && s.mean_da >= 8.f) return TC_ARM_PULL;
   if (s.nrows <= 16.f && s.mean_min >= 64.f && s.maxwin <= 16384.f) return TC_ARM_BITMAP;
   if (s.mean_min >= 64.f) return TC_ARM_BSEARCH_32;
+  // Lists of similar length (mean |log2 ratio| <= 2.5, e.g. small ER, RGG
+  // and R-MAT graphs): an even merge-path split beats searching the longer
+  // list; fitted to per-tile costs of R-MAT and of mixed small-graph batches.
+  if (s.alr <= 2.5f) return TC_ARM_MPATH_4;
   return TC_ARM_BSEARCH_4;
 }
 
