@@ -337,7 +337,7 @@ def engine_arm(args, rank, world, local_rank, dist):
             "clocks": clk.summary(),
         }
     if not args.no_batched:
-        bat = batched(args, eng, torch, dev, dist, rank)
+        bat = batched(args, eng, torch, dev, dist, rank, learned=have_weights)
         if line is not None:
             line.update(bat)
     if line is not None and not args.no_cpu_baseline:
@@ -366,7 +366,7 @@ def engine_arm(args, rank, world, local_rank, dist):
     eng.close()
 
 
-def batched(args, eng, torch, dev, dist, rank):
+def batched(args, eng, torch, dev, dist, rank, learned=False):
     import hetegeneous_parallel_programming_gb300 as tc
     t0 = time.time()
     vtx_off, rowptr, colidx = tc.gen_batch_host(args.batch_graphs, seed=1)
@@ -378,6 +378,13 @@ def batched(args, eng, torch, dev, dist, rank):
     torch.cuda.synchronize()
     call = lambda: eng.batch_count_device(G, d_off.data_ptr(), d_row.data_ptr(), d_col.data_ptr())
     ms, (totals, st) = timed(call, args.steps, args.warmup, eng, torch, dist)
+    ms_l = None
+    if learned:  # the learned selector on the same batch (reported beside the fixed rule)
+        call_l = lambda: eng.batch_count_device(G, d_off.data_ptr(), d_row.data_ptr(), d_col.data_ptr(),
+                                                selector="learned")
+        ms_l, (totals_l, _) = timed(call_l, args.steps, args.warmup, eng, torch, dist)
+        if list(map(int, totals_l)) != list(map(int, totals)):
+            raise SystemExit("learned and fixed batched counts disagree")
     # one launch sequence per graph (same engine, no batching)
     loc_rows = []
     for g in range(G):
@@ -401,7 +408,10 @@ def batched(args, eng, torch, dev, dist, rank):
     return {"batched": {"graphs": G, "graphs_per_s": round(G / (ms * 1e-3), 1), "ms_per_batch": round(ms, 3),
                         "per_graph_launch_graphs_per_s": round(G / (ms_pg * 1e-3), 1),
                         "speedup_vs_per_graph": round(ms_pg / ms, 2), "undirected_edges": len(colidx) // 2,
-                        "kernel_launches_per_batch": int(st["kernel_launches"])}}
+                        "kernel_launches_per_batch": int(st["kernel_launches"]),
+                        "selector": "fixed",
+                        "learned_graphs_per_s": round(G / (ms_l * 1e-3), 1) if ms_l else None,
+                        "learned_over_plain": round(ms / ms_l, 4) if ms_l else None}}
 
 
 def reference_arm(args, rank, world, local_rank):

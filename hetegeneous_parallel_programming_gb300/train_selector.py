@@ -15,8 +15,11 @@ device forward/backward/AdamW kernels (tc_selector_train).  Held-out graphs
 cost of the chosen arm per tile over the summed cost of the per-tile best
 arm, for the fixed-threshold selector and for the MLP.  Several candidates
 (seed x weight decay x epochs) are trained and the one with the lowest mean
-regret on the scale-21 and scale-22 held-out graphs is kept; the scale-20
-and scale-24 graphs (the latter is the benchmark graph) only report.
+regret on the scale-21 and scale-22 held-out graphs and a held-out batch is
+kept; the scale-20 and scale-24 graphs (the latter is the benchmark graph)
+and the benchmark's batch only report.  Mixed small-graph batches (ER /
+R-MAT / RGG, as the batched path counts them) can join the training set as
+disjoint unions (--batches, 2048 graphs each).
 
     python -m hetegeneous_parallel_programming_gb300.train_selector --out DIR
 """
@@ -48,6 +51,15 @@ def disjoint_union(graphs):
     return rowptr, colidx
 
 
+def batch_union(num_graphs: int, seed: int):
+    """A mixed small-graph batch (ER / R-MAT / RGG, n log-uniform in
+    [64, 16384], mean degree in [4, 64]) as one CSR of global ids."""
+    vtx_off, rowptr, colidx = tc.gen_batch_host(num_graphs, seed=seed)
+    gid = np.repeat(np.arange(len(vtx_off) - 1), np.diff(vtx_off))
+    shift = vtx_off[:-1][np.repeat(gid, np.diff(rowptr))]
+    return rowptr.astype(np.int64), (colidx.astype(np.int64) + shift).astype(np.int32)
+
+
 def regret(costs: np.ndarray, chosen: np.ndarray) -> float:
     """Summed cost of the chosen arms over the summed per-tile best cost."""
     best = costs.min(axis=1).sum()
@@ -64,6 +76,9 @@ def main():
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--no-union", action="store_true", help="profile each graph alone only")
     ap.add_argument("--save-heldout", action="store_true", help="also write the held-out graphs' tile profiles")
+    ap.add_argument("--batches", type=int, default=0,
+                    help="mixed small-graph batch unions (2048 graphs each) added to the training set; also "
+                         "adds a held-out batch to validation and the benchmark's batch to the report")
     args = ap.parse_args()
     out = Path(args.out)
     out.mkdir(parents=True, exist_ok=True)
@@ -96,6 +111,14 @@ def main():
         fixed.append(eng.plan_arms(ur, uc, selector="fixed"))
         union = {"n": int(len(ur) - 1), "nnz": int(len(uc)), "tiles": len(f)}
         del ur, uc
+    batches = []
+    for i in range(args.batches):
+        br, bc = batch_union(2048, seed=2000 + i)
+        f, k = eng.tile_profile(br, bc)
+        feats.append(f)
+        costs.append(k)
+        fixed.append(eng.plan_arms(br, bc, selector="fixed"))
+        batches.append({"graphs": 2048, "seed": 2000 + i, "tiles": len(f)})
     X = np.concatenate(feats)
     Y = np.concatenate(costs)
     # held out: other seeds and larger scales, and the benchmark graph itself
@@ -105,9 +128,16 @@ def main():
         r, cidx = rmat_graph(eng, scale, 0.57, 0.19, 0.19, seed=seed)
         f, k = eng.tile_profile(r, cidx)
         held_graphs.append((scale, seed, r, cidx, f, k))
+    # mixed small-graph batches of 4096 graphs: seed 3 validates, seed 1 (the
+    # benchmark's batch) only reports; "scale" 0 marks a batch
+    if args.batches:
+        for seed in (3, 1):
+            r, cidx = batch_union(4096, seed)
+            f, k = eng.tile_profile(r, cidx)
+            held_graphs.append((0, seed, r, cidx, f, k))
     t_prof = time.time() - t0
     t0 = time.time()
-    validation = [g for g in held_graphs if g[0] in (21, 22)]
+    validation = [g for g in held_graphs if g[0] in (21, 22) or (g[0] == 0 and g[1] == 3)]
     candidates = []
     best = None
     for ep in [int(x) for x in args.epochs.split(",")]:
@@ -129,10 +159,13 @@ def main():
     for scale, seed, r, cidx, f, k in held_graphs:
         learned = eng.plan_arms(r, cidx, selector="learned")
         fx = eng.plan_arms(r, cidx, selector="fixed")
+        name = f"s{scale}" if scale else f"batch{seed}"
         if args.save_heldout:
-            held_sets[f"s{scale}_features"] = f
-            held_sets[f"s{scale}_costs"] = k
-        held.append({"role": "validation" if scale in (21, 22) else "test","scale": scale, "seed": seed, "tiles": len(f),
+            held_sets[f"{name}_features"] = f
+            held_sets[f"{name}_costs"] = k
+        is_val = scale in (21, 22) or (scale == 0 and seed == 3)
+        held.append({"role": "validation" if is_val else "test", "graph": name, "scale": scale, "seed": seed,
+                     "tiles": len(f),
                      "regret_learned": regret(k, learned), "regret_fixed": regret(k, fx),
                      "cost_fixed_over_learned": float(k[np.arange(len(k)), fx].sum() /
                                                       k[np.arange(len(k)), learned].sum()),
@@ -144,7 +177,7 @@ def main():
     info = {"architecture": f"16 -> 64 -> 64 -> {tc.TC_NUM_ARMS}, ReLU; bf16 weights at inference, fp32 accumulate",
             "loss": loss, "chosen": best[2], "candidates": candidates, "lr": args.lr, "rows": int(len(X)),
             "profile_seconds": round(t_prof, 1), "train_seconds": round(t_train, 2),
-            "train_regret": train_regret, "held_out": held, "graphs": meta, "union": union,
+            "train_regret": train_regret, "held_out": held, "graphs": meta, "union": union, "batches": batches,
             "arms": tc.ARM_NAMES}
     (out / "selector_mlp.json").write_text(json.dumps(info, indent=1))
     np.savez_compressed(out / "selector_training_set.npz", features=X, costs=Y)
