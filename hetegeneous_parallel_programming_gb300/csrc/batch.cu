@@ -31,43 +31,6 @@ __global__ void group_fill_kernel(const int64_t *__restrict__ vtx_off, int64_t G
   }
 }
 
-// Local ids -> global ids; a local id outside its graph is flagged (and
-// clamped to the graph's first vertex so later kernels stay in bounds).
-__global__ void __launch_bounds__(BT_THREADS) globalize_kernel(const int64_t *__restrict__ rowptr,
-                                                              const int32_t *__restrict__ col, int64_t n, int64_t nnz,
-                                                              const int32_t *__restrict__ vgroup,
-                                                              const int64_t *__restrict__ vtx_off,
-                                                              int32_t *__restrict__ gcol, unsigned *flags) {
-  __shared__ int rows[ENTRY_TILE];
-  __shared__ int scan_tmp[32];
-  unsigned f = 0;
-  const int64_t tiles = (nnz + ENTRY_TILE - 1) / ENTRY_TILE;
-  for (int64_t t = blockIdx.x; t < tiles; t += gridDim.x) {
-    const int64_t t0 = t * ENTRY_TILE, t1 = min(nnz, t0 + ENTRY_TILE);
-    int64_t hint = -1;  // tiles of one block are not contiguous here
-    expand_rows<ENTRY_TILE>(rowptr, n, t0, t1, rows, scan_tmp, hint);
-    for (int k = threadIdx.x; k < t1 - t0; k += BT_THREADS) {
-      const int u = rows[k];
-      const int32_t v = col[t0 + k];
-      int64_t base = 0, size = 0;
-      if (u >= 0 && u < n) {
-        const int32_t gidx = vgroup[u];
-        base = vtx_off[gidx];
-        size = vtx_off[gidx + 1] - base;
-      }
-      if (v < 0 || (int64_t)v >= size) {
-        f |= VF_ID_RANGE;
-        gcol[t0 + k] = (int32_t)base;
-      } else {
-        gcol[t0 + k] = (int32_t)(base + v);
-      }
-    }
-    __syncthreads();
-  }
-  f = __reduce_or_sync(TC_FULL_MASK, f);
-  if ((threadIdx.x & 31) == 0 && f) atomicOr(flags, f);
-}
-
 // Graph g owns relabelled rows [vtx_off[g], vtx_off[g+1]) and so the edge
 // range [nrowptr[vtx_off[g]], nrowptr[vtx_off[g+1]]).
 __global__ void __launch_bounds__(BT_THREADS) graph_sum_kernel(const uint32_t *__restrict__ cnt,
@@ -122,7 +85,6 @@ tc_status tc_batch_count(tc_ctx *ctx, const tc_batch *b, const tc_opts *opts_in,
   const int gbits = bit_width_u64((uint64_t)(G > 1 ? G - 1 : 1));
   Sizer sz;
   if (!b->on_device) { sz.take<int64_t>(G + 1); sz.take<int64_t>(n + 1); sz.take<int32_t>(nnz); }
-  sz.take<int32_t>(nnz);
   sz.take<int32_t>(n);
   orient_sizes(ctx, n, nnz, false, false, sz);
   sz.used += count_scratch_bytes(ctx, n, nnz);
@@ -146,12 +108,12 @@ tc_status tc_batch_count(tc_ctx *ctx, const tc_batch *b, const tc_opts *opts_in,
     d_row = r1;
     d_col = c1;
   }
-  int32_t *gcol = bump.take<int32_t>(nnz);
   int32_t *vgroup = bump.take<int32_t>(n);
   OrientBufs ob;
   orient_carve(ctx, n, nnz, false, false, bump, ob);
   ob.vgroup = vgroup;
   ob.group_bits = gbits;
+  ob.vtx_off = d_off;
   CountBufs cb;
   if (count_carve(ctx, n, nnz, bump, cb, false) != TC_OK) return set_error(ctx, TC_ERR_OOM, "arena overflow");
   uint32_t *cnt = bump.take<uint32_t>(nnz);
@@ -161,16 +123,11 @@ tc_status tc_batch_count(tc_ctx *ctx, const tc_batch *b, const tc_opts *opts_in,
   TC_CHECK_CUDA(ctx, cudaMemsetAsync(vgroup, 0, sizeof(int32_t) * n, ctx->stream));
   group_fill_kernel<<<(int)std::min<int64_t>(G, 65535), 256, 0, ctx->stream>>>(d_off, G, n, vgroup, ctx->d_flags);
   TC_CHECK_LAUNCH(ctx);
-  if (nnz > 0) {
-    globalize_kernel<<<grid_for(ctx, nnz, ENTRY_TILE, 8), BT_THREADS, 0, ctx->stream>>>(d_row, d_col, n, nnz, vgroup,
-                                                                                        d_off, gcol, ctx->d_flags);
-    TC_CHECK_LAUNCH(ctx);
-  }
-  DevCSR d;
+  DevCSR d;  // local column ids: the kept-count pass adds each row's graph base (ob.vtx_off)
   d.n = n;
   d.nnz = nnz;
   d.rowptr = d_row;
-  d.col = gcol;
+  d.col = d_col;
   int64_t m = 0;
   float ms_a = 0;
   TC_TRY(orient_front(ctx, d, o, ob, &m, &st.ms_validate, &ms_a));

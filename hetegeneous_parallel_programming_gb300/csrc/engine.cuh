@@ -79,6 +79,11 @@ struct OrientBufs {
   // id), so every group owns the contiguous rank range of its vertices.
   const int32_t *vgroup = nullptr;
   int group_bits = 0;
+  // batched graphs whose column ids are local: the kept-count pass adds
+  // vtx_off[vgroup[u]] to every id of row u (and range-checks it); only the
+  // kept-count pass reads the column array then (the placement streams the
+  // target ranks it wrote)
+  const int64_t *vtx_off = nullptr;
   // check ids, sortedness and self loops inside the kept-count pass
   bool validate = false;
   // column array arriving in `pieces` uploads (ctx->piece_ev): piece k is

@@ -119,7 +119,9 @@ __global__ void __launch_bounds__(OR_THREADS, 6) kept_count_kernel(const int64_t
                                                                const int32_t *__restrict__ rank,
                                                                unsigned long long *__restrict__ kept,
                                                                int64_t *__restrict__ bcount, unsigned *flags,
-                                                               int b_off, int32_t *__restrict__ rv_out) {
+                                                               int b_off, int32_t *__restrict__ rv_out,
+                                                               const int32_t *__restrict__ vgroup,
+                                                               const int64_t *__restrict__ vtx_off) {
   __shared__ int rows[ENTRY_TILE];
   __shared__ int scan_tmp[32];
   __shared__ unsigned long long bsum;
@@ -139,6 +141,26 @@ __global__ void __launch_bounds__(OR_THREADS, 6) kept_count_kernel(const int64_t
     for (int k = 0; k < OR_PER; ++k) {
       const int64_t e = t0 + k * OR_THREADS + threadIdx.x;
       vv[k] = e < t1 ? col[e] : -1;
+    }
+    if (vtx_off) {  // batched graphs: local ids plus the base of the row's graph (always range-checked)
+#pragma unroll
+      for (int k = 0; k < OR_PER; ++k) {
+        const int64_t e = t0 + k * OR_THREADS + threadIdx.x;
+        if (e >= t1) continue;
+        const int u = rows[e - t0];
+        int64_t base = 0, size = 0;
+        if (u >= 0 && u < n) {
+          const int32_t gi = vgroup[u];
+          base = vtx_off[gi];
+          size = vtx_off[gi + 1] - base;
+        }
+        if (vv[k] < 0 || (int64_t)vv[k] >= size) {
+          f |= VF_ID_RANGE;
+          vv[k] = -1;
+        } else {
+          vv[k] = (int32_t)(base + vv[k]);
+        }
+      }
     }
 #pragma unroll
     for (int k = 0; k < OR_PER; ++k) rv[k] = vv[k] >= 0 && (int64_t)vv[k] < n ? rank[vv[k]] : -1;
@@ -161,7 +183,8 @@ __global__ void __launch_bounds__(OR_THREADS, 6) kept_count_kernel(const int64_t
         if (VALIDATE) {
           if (v < 0 || (int64_t)v >= n) f |= VF_ID_RANGE;
           else if (u == v) f |= VF_SELF_LOOP;
-          if (u >= 0 && u < n && e > 0 && e > rowptr[u] && col[e - 1] >= v) f |= VF_UNSORTED;
+          // stored ids (local ones in a batch) compare alike within a row
+          if (u >= 0 && u < n && e > 0 && e > rowptr[u] && col[e - 1] >= col[e]) f |= VF_UNSORTED;
         }
       }
       const unsigned km = __ballot_sync(TC_FULL_MASK, keep);
@@ -175,7 +198,7 @@ __global__ void __launch_bounds__(OR_THREADS, 6) kept_count_kernel(const int64_t
   }
   mine = warp_sum(mine);
   if (lane == 0 && mine) atomicAdd(&bsum, mine);
-  if (VALIDATE) {
+  if (VALIDATE || vtx_off) {  // batch ids are range-checked even without validation
     f = __reduce_or_sync(TC_FULL_MASK, f);
     if (lane == 0 && f) atomicOr(flags, f);
   }
@@ -255,11 +278,13 @@ tc_status orient_phase_a(tc_ctx *ctx, const DevCSR &g, OrientBufs &b) {
       if (b.validate)
         kept_count_kernel<true><<<blocks, OR_THREADS, 0, ctx->stream>>>(g.rowptr, g.col, g.n, g.nnz, b.chunk,
                                                                         b.rank, (unsigned long long *)b.kept,
-                                                                        b.bcount, ctx->d_flags, k * per, b.rv);
+                                                                        b.bcount, ctx->d_flags, k * per, b.rv,
+                                                                        b.vgroup, b.vtx_off);
       else
         kept_count_kernel<false><<<blocks, OR_THREADS, 0, ctx->stream>>>(g.rowptr, g.col, g.n, g.nnz, b.chunk,
                                                                          b.rank, (unsigned long long *)b.kept,
-                                                                         b.bcount, ctx->d_flags, k * per, b.rv);
+                                                                         b.bcount, ctx->d_flags, k * per, b.rv,
+                                                                         b.vgroup, b.vtx_off);
       TC_CHECK_LAUNCH(ctx);
     }
     TC_TRY(exclusive_scan_i64(ctx, b.bcount, b.bcount, b.G, b.sort_scratch, b.d_m));

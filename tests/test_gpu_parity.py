@@ -352,6 +352,26 @@ def test_batch_matches_per_graph(engine):
     assert np.array_equal(totals, ref) and np.array_equal(totals2, ref)
 
 
+def test_batch_local_ids_checked(engine):
+    """Batch column ids are local to their graph: an id equal to the graph's
+    size (still inside the union) or negative is rejected, with or without
+    validation, and the ctx then counts the intact batch."""
+    path = oracle.csr_from_edges(4, np.array([0, 1, 2], np.int32), np.array([1, 2, 3], np.int32))
+    tri = oracle.csr_from_edges(3, np.array([0, 1, 0], np.int32), np.array([1, 2, 2], np.int32))
+    vtx_off = np.array([0, 4, 7], np.int64)
+    rowptr = np.concatenate([path[0], tri[0][1:] + len(path[1])]).astype(np.int64)
+    colidx = np.concatenate([path[1], tri[1]]).astype(np.int32)
+    for bad_id in (4, -1):
+        bad = colidx.copy()
+        bad[0] = bad_id
+        for validate in (True, False):
+            with pytest.raises(tc.TCError) as ei:
+                engine.batch_count(vtx_off, rowptr, bad, validate=validate)
+            assert ei.value.status == 2, (bad_id, validate)
+    totals, _ = engine.batch_count(vtx_off, rowptr, colidx)
+    assert totals.tolist() == [0, 1]
+
+
 @pytest.mark.parametrize("rowptr,colidx", [
     ([0, 2, 1, 3], [1, 2, 0]),          # rowptr not monotone
     ([0, 1, 2, 2], [1, 3]),             # id out of range
