@@ -1190,7 +1190,7 @@ struct PullDense {
   int64_t hub_e0;  // first edge of the hub rows (rowptr[hub0])
 };
 
-template <bool BITMAP, bool PER_EDGE, bool TOP, bool LABEL, bool DENSE>
+template <bool BITMAP, bool PER_EDGE, bool TOP, bool DENSE>
 __device__ __forceinline__ void pull_run(const DevDag &g, const uint2 *__restrict__ er, int64_t k, int64_t k2,
                                          bool have_b, const uint32_t *tb, int32_t base, int bits, int lane,
                                          PullBatch &sb, uint32_t *out, unsigned long long &acc,
@@ -1281,7 +1281,6 @@ __device__ __forceinline__ void pull_run(const DevDag &g, const uint2 *__restric
         for (int t = 0; t < 4; ++t)
           if (t >= lo[j] && t < hi[j]) {
             uint32_t hit = pull_test<BITMAP>(tb, base, bits, xs[t]);
-            if (LABEL && hit) hit = g.vlabel[xs[t]] == g.label;  // the reference's labelled intersection
             h += hit;
             // the hit closes triangle (u, v, x): entry u->x joins its lowest and highest vertex
             if (TOP && hit) atomicAdd(g.top + gfirst[j] + t, 1u);
@@ -1424,7 +1423,7 @@ __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint2 
       // down to a 128-id boundary counted from hub0 (a hub target's list lies
       // in (v, n), so the window still fits)
       PullDense pd{hub0, 0, 0, hub_e0};
-      const bool dense_run = MODE == 0 && g.hub_bits != nullptr && bitmap && nb > 0 && v >= hub0;
+      const bool dense_run = MODE != 1 && g.hub_bits != nullptr && bitmap && nb > 0 && v >= hub0;
       if (dense_run) {
         const int32_t bmax = bmin + (int32_t)span - 1;
         pd.woff4 = (bmin - hub0) >> 7;
@@ -1474,6 +1473,9 @@ __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint2 
 #pragma unroll
         for (int u = 0; u < PL_UNROLL; ++u) {
           if (q0 + 32 * u + lane >= nb) continue;
+          // labelled counts: the table holds only N+(v)'s entries with the
+          // label, so every hit is a labelled one (no test per probe)
+          if (MODE == 2 && g.vlabel[x[u]] != g.label) continue;
           if (bitmap) {
             const uint32_t d = (uint32_t)(x[u] - bmin);
             if (d < span) atomicOr(&tb[d >> 5], 1u << (d & 31));  // false only for an unsorted list
@@ -1493,32 +1495,31 @@ __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint2 
       __syncwarp();
       const unsigned long long build_share =
           tile_cycles ? (unsigned long long)(clock64() - tr0) / (unsigned long long)(k2 - k) : 0ull;
-      constexpr bool LAB = MODE == 2;
       if (MODE == 1) {  // per-vertex counts: per-edge output plus the top-edge attribution
         if (bitmap)
-          pull_run<true, true, true, false, false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc,
+          pull_run<true, true, true, false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc,
                                                    tile_cycles, build_share, pd);
         else
-          pull_run<false, true, true, false, false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc,
+          pull_run<false, true, true, false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc,
                                                     tile_cycles, build_share, pd);
       } else if (out == nullptr) {  // total only
         if (dense_run)
-          pull_run<true, false, false, false, MODE == 0>(g, er, k, k2, true, tb, bmin, bits, lane, s_batch[w], out,
+          pull_run<true, false, false, MODE != 1>(g, er, k, k2, true, tb, bmin, bits, lane, s_batch[w], out,
                                                          acc, tile_cycles, build_share, pd);
         else if (bitmap)
-          pull_run<true, false, false, LAB, false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc,
+          pull_run<true, false, false, false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc,
                                                    tile_cycles, build_share, pd);
         else
-          pull_run<false, false, false, LAB, false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc,
+          pull_run<false, false, false, false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc,
                                                     tile_cycles, build_share, pd);
       } else if (dense_run) {
-        pull_run<true, true, false, false, MODE == 0>(g, er, k, k2, true, tb, bmin, bits, lane, s_batch[w], out, acc,
+        pull_run<true, true, false, MODE != 1>(g, er, k, k2, true, tb, bmin, bits, lane, s_batch[w], out, acc,
                                                       tile_cycles, build_share, pd);
       } else if (bitmap) {
-        pull_run<true, true, false, LAB, false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc,
+        pull_run<true, true, false, false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc,
                                                 tile_cycles, build_share, pd);
       } else {
-        pull_run<false, true, false, LAB, false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc,
+        pull_run<false, true, false, false>(g, er, k, k2, nb > 0, tb, bmin, bits, lane, s_batch[w], out, acc,
                                                  tile_cycles, build_share, pd);
       }
       __syncwarp();
@@ -1697,8 +1698,9 @@ static tc_status run_pull(tc_ctx *ctx, const DevDag &g_in, CountBufs &cb, uint32
                                                                      cb.pull_er);
   TC_CHECK_LAUNCH(ctx);
   DevDag g = g_in;
-  // dense edges: plain counts of a relabelled DAG (rows hold higher ids only)
-  if (g.restrict_after && !g.top && !g.vlabel && g.m > 0) {
+  // dense edges: plain and labelled counts of a relabelled DAG (rows hold
+  // higher ids only; labelled tables hold only the labelled entries)
+  if (g.restrict_after && !g.top && g.m > 0) {
     const int32_t hub0 = (int32_t)(g.n - hub_rows(g.n));
     hub_bits_kernel<<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(g, hub0, hub_wpr4(g.n), pos + K, cb.hub_bits);
     TC_CHECK_LAUNCH(ctx);
