@@ -87,7 +87,7 @@ void orient_sizes(const tc_ctx *ctx, int64_t n, int64_t nnz, bool perm, bool dag
   scr = std::max(scr, scan_scratch_bytes(ctx, G));
   sz.take<char>((int64_t)scr);
   sz.take<int64_t>(n + 1); sz.take<int64_t>(n + 1); sz.take<int64_t>(n + 1);
-  sz.take<int32_t>(n);
+  sz.take<int2>(n);
   sz.take<int32_t>(n); sz.take<int32_t>(n); sz.take<int32_t>(n); sz.take<unsigned>(3);
   sz.take<int32_t>(nnz);
   sz.take<int32_t>(mmax); sz.take<int32_t>(mmax);
@@ -112,7 +112,7 @@ void orient_carve(const tc_ctx *ctx, int64_t n, int64_t nnz, bool perm, bool dag
   b.orowptr = bump.take<int64_t>(n + 1);
   b.nrowptr = bump.take<int64_t>(n + 1);
   b.dnew = bump.take<int64_t>(n + 1);
-  b.indeg = bump.take<int32_t>(n);
+  b.dv = bump.take<int2>(n);
   b.mid_list = bump.take<int32_t>(n);
   b.big_list = bump.take<int32_t>(n);
   b.huge_list = bump.take<int32_t>(n);

@@ -137,7 +137,15 @@ __global__ void __launch_bounds__(PLAN_THREADS) plan_kernel(DevDag g, int64_t T,
     const int64_t rb = g.rowptr[r], re = g.rowptr[r + 1];
     const int64_t a0 = g.restrict_after ? e + 1 : rb;
     const float da = (float)(re - a0);
-    const float db = (float)(g.rowptr[s + 1] - g.rowptr[s]);
+    float db, ins;  // target's out-degree and DAG in-degree: one 8-byte gather on a relabelled DAG
+    if (g.dv) {
+      const int2 q = __ldg(g.dv + s);
+      db = (float)q.x;
+      ins = (float)q.y;
+    } else {
+      db = (float)(g.rowptr[s + 1] - g.rowptr[s]);
+      ins = g.indeg ? (float)g.indeg[s] : 0.f;
+    }
     sda += da;
     sdb += db;
     const float mn = fminf(da, db), mx = fmaxf(da, db);
@@ -145,12 +153,12 @@ __global__ void __launch_bounds__(PLAN_THREADS) plan_kernel(DevDag g, int64_t T,
     smax += mx;
     const float lr = flog2p1(da) - flog2p1(db);
     salr += fabsf(lr);
-    if (g.indeg) sin += (float)g.indeg[s];  // how many edges share this target's list
+    sin += ins;  // how many edges share this target's list
     const int bin = mn < 2.f ? 0 : mn < 8.f ? 1 : mn < 32.f ? 2 : mn < 128.f ? 3 : mn < 512.f ? 4 : 5;
 #pragma unroll
     for (int k = 0; k < 6; ++k) bins[k] += (bin == k) ? 1.f : 0.f;
     work += (unsigned long long)(da + db);
-    alg += 4ULL * (unsigned long long)((re - rb) + (g.rowptr[s + 1] - g.rowptr[s])) + 4ULL;
+    alg += 4ULL * (unsigned long long)((re - rb) + (int64_t)db) + 4ULL;
     if (e == e0 || g.src[e - 1] != r) {
       ++nrows;
       maxdr = max(maxdr, (long long)(re - rb));

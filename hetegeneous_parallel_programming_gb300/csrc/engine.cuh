@@ -34,7 +34,8 @@ struct DevDag {
   const int32_t *col = nullptr;      // [m]
   const int32_t *src = nullptr;      // [m] row of each edge
   const uint32_t *perm = nullptr;    // [m] output slot of each edge (null: identity)
-  const int32_t *indeg = nullptr;    // [n] in-degree of each vertex in the DAG
+  const int32_t *indeg = nullptr;    // [n] in-degree of each vertex in the DAG (caller-oriented DAGs)
+  const int2 *dv = nullptr;          // [n] (out-degree, in-degree) of each vertex (relabelled DAGs)
   uint32_t *top = nullptr;           // [m] per-vertex mode: triangles in which edge e joins the
                                      // lowest and the highest vertex (PULL arm only)
   const uint8_t *vlabel = nullptr;   // [n] labelled mode: vertex labels (relabelled ids; PULL arm only)
@@ -65,7 +66,7 @@ struct OrientBufs {
   int64_t *orowptr;            // [n+1] original-order DAG row pointers
   int64_t *nrowptr;            // [n+1] relabelled row pointers
   int64_t *dnew;               // [n+1] relabelled row lengths
-  int32_t *indeg;              // [n] DAG in-degree by relabelled id
+  int2 *dv;                    // [n] (out-degree, in-degree) per relabelled vertex
   int32_t *mid_list, *big_list, *huge_list;  // [n] rows for the warp / block / global sorts
   unsigned *seg_counts;        // [3]
   int32_t *rv = nullptr;       // [nnz] rank of every entry's target, written by the kept-count pass

@@ -207,16 +207,17 @@ __global__ void __launch_bounds__(OR_THREADS, 6) kept_count_kernel(const int64_t
 }
 
 
-// Relabelled out-degree and DAG in-degree (symmetric degree minus kept
-// out-degree) of every vertex.
+// Relabelled out-degree (for the row pointers, and with the DAG in-degree,
+// the symmetric degree minus the kept out-degree, as one 8-byte pair the
+// tile planner gathers per edge target) of every vertex.
 __global__ void dnew_kernel(const int64_t *__restrict__ kept, const int32_t *__restrict__ rank,
                             const int64_t *__restrict__ rowptr, int64_t n, int64_t *__restrict__ dnew,
-                            int32_t *__restrict__ indeg) {
+                            int2 *__restrict__ dv) {
   for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
     const int32_t r = rank[u];
     const int64_t k = kept[u];
     dnew[r] = k;
-    indeg[r] = (int32_t)(rowptr[u + 1] - rowptr[u] - k);
+    dv[r] = make_int2((int32_t)k, (int32_t)(rowptr[u + 1] - rowptr[u] - k));
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) dnew[n] = 0;
 }
@@ -294,7 +295,7 @@ tc_status orient_phase_a(tc_ctx *ctx, const DevCSR &g, OrientBufs &b) {
   // original-order DAG rowptr, relabelled rowptr, and the row classes
   TC_TRY(exclusive_scan_i64(ctx, b.kept, b.orowptr, g.n + 1, b.sort_scratch, nullptr));
   dnew_kernel<<<grid_for(ctx, g.n, 256, 8), 256, 0, ctx->stream>>>(b.kept, b.rank, g.rowptr, g.n, b.dnew,
-                                                                    b.indeg);
+                                                                    b.dv);
   TC_CHECK_LAUNCH(ctx);
   TC_TRY(exclusive_scan_i64(ctx, b.dnew, b.nrowptr, g.n + 1, b.sort_scratch, nullptr));
   TC_CHECK_CUDA(ctx, cudaMemsetAsync(b.seg_counts, 0, sizeof(unsigned) * 3, ctx->stream));
@@ -743,7 +744,8 @@ tc_status orient_phase_b(tc_ctx *ctx, const DevCSR &g, OrientBufs &b, int64_t m,
   out->col = b.ncol;
   out->src = b.nsrc;
   out->perm = want_perm ? b.perm : nullptr;
-  out->indeg = b.indeg;
+  out->indeg = nullptr;
+  out->dv = b.dv;
   out->restrict_after = 1;
   return TC_OK;
 }
