@@ -20,7 +20,7 @@ TC_MLP_PARAM_COUNT = (TC_MLP_FEATURES * TC_MLP_HIDDEN + TC_MLP_HIDDEN + TC_MLP_H
                       TC_MLP_HIDDEN + TC_MLP_HIDDEN * TC_NUM_ARMS + TC_NUM_ARMS)
 TILE_EDGES = 4096
 
-ARM_NAMES = ["bsearch4", "bsearch32", "merge8", "merge32", "hash", "bitmap", "gallop4", "mpath4", "flat", "pull"]
+ARM_NAMES = ["bsearch4", "bsearch32", "merge8", "merge32", "hash", "bitmap", "gallop4", "mpath2", "flat", "pull"]
 
 SELECT_FIXED, SELECT_LEARNED, SELECT_FORCE = 0, 1, 2
 GEN_ER, GEN_RMAT, GEN_RGG, GEN_CHUNG_LU = 0, 1, 2, 3

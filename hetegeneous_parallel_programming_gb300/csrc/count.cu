@@ -55,7 +55,7 @@ __device__ __forceinline__ int fixed_select(const PlanStats &s) {
   // Lists of similar length (mean |log2 ratio| <= 2.5, e.g. small ER, RGG
   // and R-MAT graphs): an even merge-path split beats searching the longer
   // list; fitted to per-tile costs of R-MAT and of mixed small-graph batches.
-  if (s.alr <= 2.5f) return TC_ARM_MPATH_4;
+  if (s.alr <= 2.5f) return TC_ARM_MPATH_2;
   return TC_ARM_BSEARCH_4;
 }
 
@@ -1563,7 +1563,7 @@ static ArmKernel arm_kernel(int arm) {
     case TC_ARM_MERGE_32: return merge_kernel<32>;
     case TC_ARM_HASH: return hash_kernel;
     case TC_ARM_GALLOP_4: return gallop_kernel<4>;
-    case TC_ARM_MPATH_4: return mpath_kernel<4>;
+    case TC_ARM_MPATH_2: return mpath_kernel<2>;
     case TC_ARM_FLAT: return flat_kernel;
     default: return bitmap_kernel;
   }

@@ -68,7 +68,7 @@ typedef enum tc_arm {
   TC_ARM_HASH = 4,         /* warp hash of the row's out-list, flattened probes */
   TC_ARM_BITMAP = 5,       /* block bitmap of the row's id window + probes    */
   TC_ARM_GALLOP_4 = 6,     /* 4 lanes per edge, each gallops a run of keys    */
-  TC_ARM_MPATH_4 = 7,      /* 4 lanes per edge split the merge path evenly    */
+  TC_ARM_MPATH_2 = 7,      /* 2 lanes per edge split the merge path evenly    */
   TC_ARM_FLAT = 8,         /* warp walks 32 edges' lookup lists as one run    */
   TC_ARM_PULL = 9,         /* edges grouped by target: hash N+(v) once, probe
                               every in-edge's row suffix against it           */
