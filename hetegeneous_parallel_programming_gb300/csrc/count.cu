@@ -1074,8 +1074,8 @@ __device__ __forceinline__ uint32_t attr_search_count(const int32_t *__restrict_
 constexpr int PL_THREADS = 128;
 constexpr int PL_WARPS = PL_THREADS / 32;
 constexpr int PL_WORDS = 2048;  // per warp: a 65536-id bitmap or a 2048-slot hash table
-constexpr int PL_ITEM = 2048;      // largest work chunk (grouped entries)
-constexpr int PL_ITEM_MIN = 256;   // smallest, near the end of the work
+constexpr int PL_ITEM = 512;       // largest work chunk (grouped entries)
+constexpr int PL_ITEM_MIN = 128;   // smallest, near the end of the work
 constexpr int PL_UNROLL = 4;      // table build: list loads in flight per lane
 constexpr int PL_GUNROLL = 4;      // flattened probing: 16-byte loads in flight per lane
 constexpr int PL_GROUP_THREADS = 256;
