@@ -40,8 +40,8 @@ struct PlanStats {
 
 __device__ __forceinline__ float flog2p1(float x) { return __log2f(1.0f + x); }
 
-// Fixed degree-threshold selector: the engine's fallback and the judge of the
-// learned one.
+// Fixed degree-threshold selector: the engine's default, its fallback, and
+// the baseline the learned selector is measured against.
 __device__ __forceinline__ int fixed_select(const PlanStats &s) {
   // Thresholds fitted to per-tile arm costs recorded on R-MAT scale 16-20
   // graphs (the learned selector's training set).  The bitmap is cleared per

@@ -76,7 +76,7 @@ typedef enum tc_arm {
 } tc_arm;
 
 typedef enum tc_selector {
-  TC_SELECT_FIXED = 0,     /* degree-threshold selector (fallback and judge)  */
+  TC_SELECT_FIXED = 0,     /* degree thresholds: default, fallback, baseline  */
   TC_SELECT_LEARNED = 1,   /* MLP cost model loaded into the ctx              */
   TC_SELECT_FORCE = 2      /* every tile uses opts.force_arm                  */
 } tc_selector;
