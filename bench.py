@@ -207,6 +207,16 @@ def engine_arm(args, rank, world, local_rank, dist):
         if have_weights:
             eng.set_selector_weights(w)
 
+    # the project's autotuner picks the PULL work-chunk size for this graph
+    # (counts it with each candidate before the timed region)
+    tune = None
+    if not args.no_autotune:
+        t0 = time.time()
+        best_item, tune_ms = eng.autotune_pull(rowptr.data_ptr(), (colidx.data_ptr(), nnz),
+                                               candidates=(256, 512, 1024), reps=2, on_device_n=n)
+        tune = {"pull_chunk": best_item, "ms_per_candidate": {str(k): round(v, 3) for k, v in tune_ms.items()}}
+        log(f"[rank {rank}] autotune: PULL chunk {best_item} {tune['ms_per_candidate']} ({time.time() - t0:.1f}s)")
+
     per_edge = torch.empty(m if args.per_edge else 1, dtype=torch.int32, device=dev)
 
     def step(sel):
@@ -331,6 +341,7 @@ def engine_arm(args, rank, world, local_rank, dist):
                          "count_phase": {"alg_bytes": int(st["alg_bytes"]),
                                          "achieved": round(st["alg_bytes"] / (st["ms_count"] * 1e-3) / 1e9, 1)
                                          if st["ms_count"] > 0 else None}},
+            "autotune": tune,
             "gpu_launches": int(st["kernel_launches"]) * args.steps,
             "per_edge_counts": per_edge_check,
             "per_vertex_counts": per_vertex,
@@ -467,6 +478,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--per-edge", action="store_true", help="also write per-edge local counts every step")
     ap.add_argument("--no-per-vertex", action="store_true", help="skip the per-vertex triangle count timing")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default PULL work-chunk size")
     ap.add_argument("--force-arm", default=None, help="run every tile on this arm (profiling)")
     ap.add_argument("--ref-step-seconds", type=float, default=4.0)
     args = ap.parse_args()

@@ -495,6 +495,35 @@ class Engine:
                                             float(lr), float(weight_decay), int(seed), C.byref(loss)))
         return float(loss.value)
 
+    def set_pull_chunks(self, item: int, item_min: int) -> None:
+        """PULL work-chunk sizes (largest, smallest) used by later calls."""
+        self._chk(self._L.tc_set_pull_chunks(self._h, int(item), int(item_min)))
+
+    def get_pull_chunks(self) -> tuple[int, int]:
+        a, b = C.c_int32(0), C.c_int32(0)
+        self._chk(self._L.tc_get_pull_chunks(self._h, C.byref(a), C.byref(b)))
+        return int(a.value), int(b.value)
+
+    def autotune_pull(self, rowptr, colidx, candidates=(256, 512, 1024, 2048), reps: int = 3, *,
+                      selector: str = "fixed", on_device_n: int = 0):
+        """Counts the graph with each candidate PULL chunk size and keeps the
+        fastest in this engine: (best, {candidate: ms}).  rowptr/colidx are
+        host arrays, or device pointers when on_device_n (the vertex count)
+        is given, with colidx then the entry count paired as (ptr, nnz)."""
+        if on_device_n:
+            (rp_ptr, cl_ptr, nnz) = rowptr, colidx[0], colidx[1]
+            g = _ffi.Csr(int(on_device_n), int(nnz), int(rp_ptr), int(cl_ptr), 1)
+        else:
+            rowptr, colidx = _i64(rowptr), _i32(colidx)
+            g = _ffi.Csr(len(rowptr) - 1, len(colidx), _ptr(rowptr).value, _ptr(colidx).value, 0)
+        cands = np.ascontiguousarray(candidates, np.int32)
+        ms = np.zeros(len(cands), np.float32)
+        best = C.c_int32(0)
+        o = _opts(selector, None, True)
+        self._chk(self._L.tc_autotune_pull(self._h, C.byref(g), C.byref(o), _ptr(cands), len(cands), int(reps),
+                                           ms.ctypes.data_as(C.POINTER(C.c_float)), C.byref(best)))
+        return int(best.value), {int(c): float(t) for c, t in zip(cands, ms)}
+
     def l2_bandwidth(self, nbytes: int = 64 << 20, passes: int = 128) -> float:
         """L2 read ceiling in GB/s: one kernel streams an L2-resident buffer
         `passes` times with L1-bypassing 16-byte loads (tc_l2_bandwidth)."""

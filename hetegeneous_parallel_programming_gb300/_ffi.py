@@ -107,6 +107,9 @@ _SIGS = {
     "tc_batch_count": (C.c_int, [P, C.POINTER(Batch), C.POINTER(Opts), P, C.POINTER(Stats)]),
     "tc_count_dag_noalloc": (C.c_int, [C.c_int, P, P, I64, I64, P, P, P]),
     "tc_l2_bandwidth": (C.c_int, [P, I64, I32, C.POINTER(C.c_double)]),
+    "tc_set_pull_chunks": (C.c_int, [P, I32, I32]),
+    "tc_get_pull_chunks": (C.c_int, [P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "tc_autotune_pull": (C.c_int, [P, C.POINTER(Csr), C.POINTER(Opts), P, I32, I32, PF, C.POINTER(C.c_int32)]),
     "tc_count_dag_parts": (C.c_int, [P, C.POINTER(Csr), P, I32, I32, C.POINTER(Opts), PU64, P, C.POINTER(Stats)]),
     "tc_count_edges": (C.c_int, [P, I64, I64, P, P, I32, C.POINTER(Opts), PU64, C.POINTER(Stats)]),
     "tc_tile_profile": (C.c_int, [P, C.POINTER(Csr), P, P, I64, PI64]),

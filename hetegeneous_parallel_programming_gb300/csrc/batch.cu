@@ -133,9 +133,10 @@ tc_status tc_batch_count(tc_ctx *ctx, const tc_batch *b, const tc_opts *opts_in,
   TC_TRY(orient_front(ctx, d, o, ob, &m, &st.ms_validate, &ms_a));
   // Back half (relabel sort -> count -> per-graph sums -> D2H), replayed as
   // a CUDA graph when the batch shape and buffers repeat.
-  const int64_t key[12] = {n, nnz, m, G, o.selector, o.force_arm, (int64_t)(uintptr_t)ctx->arena,
+  const int64_t key[14] = {n, nnz, m, G, o.selector, o.force_arm, (int64_t)(uintptr_t)ctx->arena,
                            (int64_t)ctx->arena_cap, (int64_t)(uintptr_t)d_col, (int64_t)(uintptr_t)d_row,
-                           (int64_t)(uintptr_t)d_off, (int64_t)ctx->mlp_loaded};
+                           (int64_t)(uintptr_t)d_off, (int64_t)ctx->mlp_loaded, ctx->pull_item,
+                           ctx->pull_item_min};
   const bool same = ctx->batch_exec && memcmp(key, ctx->batch_key, sizeof(key)) == 0;
   TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[4], ctx->stream));
   if (!same) {

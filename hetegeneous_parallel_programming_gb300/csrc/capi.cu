@@ -180,6 +180,67 @@ __global__ void l2_read_kernel(const uint4 *__restrict__ buf, int64_t n4, int pa
 
 extern "C" {
 
+tc_status tc_set_pull_chunks(tc_ctx *ctx, int32_t item, int32_t item_min) {
+  if (!ctx) return set_error(ctx, TC_ERR_INVALID_ARG, "null ctx");
+  if (item_min < 32 || item_min > item || item > 65536)
+    return set_error(ctx, TC_ERR_INVALID_ARG, "need 32 <= item_min <= item <= 65536 (got %d, %d)", (int)item_min,
+                     (int)item);
+  ctx->pull_item = item;
+  ctx->pull_item_min = item_min;
+  return TC_OK;
+}
+
+tc_status tc_get_pull_chunks(const tc_ctx *ctx, int32_t *item, int32_t *item_min) {
+  if (!ctx || !item || !item_min) return set_error(nullptr, TC_ERR_INVALID_ARG, "null argument");
+  *item = ctx->pull_item;
+  *item_min = ctx->pull_item_min;
+  return TC_OK;
+}
+
+tc_status tc_autotune_pull(tc_ctx *ctx, const tc_csr *g, const tc_opts *opts, const int32_t *candidates,
+                           int32_t ncand, int32_t reps, float *ms, int32_t *best) {
+  if (!ctx || !candidates || ncand < 1 || reps < 1)
+    return set_error(ctx, TC_ERR_INVALID_ARG, "need ctx, candidates, ncand >= 1 and reps >= 1");
+  for (int32_t i = 0; i < ncand; ++i)
+    if (candidates[i] < 32 || candidates[i] > 65536)
+      return set_error(ctx, TC_ERR_INVALID_ARG, "candidate %d outside [32, 65536]", (int)candidates[i]);
+  const int old_item = ctx->pull_item, old_min = ctx->pull_item_min;
+  auto restore = [&](tc_status st) {
+    ctx->pull_item = old_item;
+    ctx->pull_item_min = old_min;
+    return st;
+  };
+  float best_ms = 0.f;
+  int32_t best_item = old_item;
+  uint64_t first_total = 0;
+  for (int32_t i = 0; i < ncand; ++i) {
+    ctx->pull_item = candidates[i];
+    ctx->pull_item_min = std::max(32, candidates[i] / 4);
+    float cand_ms = 0.f;
+    for (int32_t r = 0; r <= reps; ++r) {  // r == 0 warms up
+      uint64_t total = 0;
+      tc_stats st;
+      const tc_status s = tc_count(ctx, g, opts, &total, nullptr, 0, &st);
+      if (s != TC_OK) return restore(s);
+      if (i == 0 && r == 0) first_total = total;
+      if (total != first_total)
+        return restore(set_error(ctx, TC_ERR_INVALID_GRAPH,
+                                 "chunk size %d counted %llu triangles, %llu with the first candidate",
+                                 (int)candidates[i], (unsigned long long)total, (unsigned long long)first_total));
+      if (r > 0 && (cand_ms == 0.f || st.ms_total < cand_ms)) cand_ms = st.ms_total;
+    }
+    if (ms) ms[i] = cand_ms;
+    if (i == 0 || cand_ms < best_ms) {
+      best_ms = cand_ms;
+      best_item = candidates[i];
+    }
+  }
+  ctx->pull_item = best_item;
+  ctx->pull_item_min = std::max(32, best_item / 4);
+  if (best) *best = best_item;
+  return TC_OK;
+}
+
 tc_status tc_l2_bandwidth(tc_ctx *ctx, int64_t bytes, int32_t passes, double *gbs) {
   if (!ctx || !gbs || bytes < 4096 || passes < 1)
     return set_error(ctx, TC_ERR_INVALID_ARG, "need ctx, gbs, bytes >= 4096 and passes >= 1");

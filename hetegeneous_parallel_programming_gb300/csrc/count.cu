@@ -1074,8 +1074,6 @@ __device__ __forceinline__ uint32_t attr_search_count(const int32_t *__restrict_
 constexpr int PL_THREADS = 128;
 constexpr int PL_WARPS = PL_THREADS / 32;
 constexpr int PL_WORDS = 2048;  // per warp: a 65536-id bitmap or a 2048-slot hash table
-constexpr int PL_ITEM = 512;       // largest work chunk (grouped entries)
-constexpr int PL_ITEM_MIN = 128;   // smallest, near the end of the work
 constexpr int PL_UNROLL = 4;      // table build: list loads in flight per lane
 constexpr int PL_GUNROLL = 4;      // flattened probing: 16-byte loads in flight per lane
 constexpr int PL_GROUP_THREADS = 256;
@@ -1371,13 +1369,15 @@ __device__ __forceinline__ void pull_run(const DevDag &g, const uint2 *__restric
   }
 }
 
-// Work is taken in chunks of grouped entries that shrink from PL_ITEM to
-// PL_ITEM_MIN as the remaining work falls, so the last chunks end together.
-__device__ __forceinline__ unsigned pull_next_chunk(unsigned *head, int64_t np, int64_t warps, int64_t *end) {
+// Work is taken in chunks of grouped entries that shrink from `item` to
+// `item_min` as the remaining work falls, so the last chunks end together
+// (the ctx's pull_item / pull_item_min; 512 and 128 unless tuned).
+__device__ __forceinline__ unsigned pull_next_chunk(unsigned *head, int64_t np, int64_t warps, int item,
+                                                    int item_min, int64_t *end) {
   const int64_t seen = (int64_t)*(volatile unsigned *)head;
   const int64_t left = np - seen;
   int64_t chunk = left / warps;
-  chunk = chunk >= PL_ITEM ? PL_ITEM : chunk <= PL_ITEM_MIN ? PL_ITEM_MIN : chunk;
+  chunk = chunk >= item ? item : chunk <= item_min ? item_min : chunk;
   const unsigned start = atomicAdd(head, (unsigned)chunk);
   *end = min(np, (int64_t)start + chunk);
   return start;
@@ -1390,7 +1390,7 @@ template <int MODE>
 __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint2 *__restrict__ er,
                                                          const unsigned *__restrict__ npull,
                                                          unsigned *head, uint32_t *out, unsigned long long *total,
-                                                         unsigned long long *tile_cycles) {
+                                                         unsigned long long *tile_cycles, int item, int item_min) {
   __shared__ __align__(16) uint32_t tab[PL_WARPS][PL_ROW];
   __shared__ PullBatch s_batch[PL_WARPS];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -1405,7 +1405,7 @@ __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint2 
   for (;;) {
     unsigned it = 0;
     int64_t p1 = 0;
-    if (lane == 0) it = pull_next_chunk(head, np, warps, &p1);
+    if (lane == 0) it = pull_next_chunk(head, np, warps, item, item_min, &p1);
     it = __shfl_sync(TC_FULL_MASK, it, 0);
     p1 = __shfl_sync(TC_FULL_MASK, (long long)p1, 0);
     if ((int64_t)it >= np) break;
@@ -1719,13 +1719,16 @@ static tc_status run_pull(tc_ctx *ctx, const DevDag &g_in, CountBufs &cb, uint32
   const int grid = ctx->num_sms * ctx->arm_blocks_per_sm[TC_ARM_PULL];
   if (g.top)
     pull_kernel<1><<<grid, PL_THREADS, 0, ctx->stream>>>(g, cb.pull_er, pos + K, ctx->d_heads + TC_ARM_PULL, out,
-                                                        ctx->d_total, cb.tile_cycles);
+                                                        ctx->d_total, cb.tile_cycles, ctx->pull_item,
+                                                        ctx->pull_item_min);
   else if (g.vlabel)
     pull_kernel<2><<<grid, PL_THREADS, 0, ctx->stream>>>(g, cb.pull_er, pos + K, ctx->d_heads + TC_ARM_PULL, out,
-                                                        ctx->d_total, cb.tile_cycles);
+                                                        ctx->d_total, cb.tile_cycles, ctx->pull_item,
+                                                        ctx->pull_item_min);
   else
     pull_kernel<0><<<grid, PL_THREADS, 0, ctx->stream>>>(g, cb.pull_er, pos + K,
-                                                    ctx->d_heads + TC_ARM_PULL, out, ctx->d_total, cb.tile_cycles);
+                                                    ctx->d_heads + TC_ARM_PULL, out, ctx->d_total, cb.tile_cycles, ctx->pull_item,
+                                                        ctx->pull_item_min);
   TC_CHECK_LAUNCH(ctx);
   return TC_OK;
 }

@@ -45,10 +45,14 @@ struct tc_ctx {
   int arm_blocks_per_sm[TC_NUM_ARMS] = {};
   int arm_units_per_sm[TC_NUM_ARMS] = {};   // independent workers (warps or blocks) per SM
   int64_t launches = 0;                   // kernels launched by the current call
+  // PULL work chunks (grouped entries a warp takes at a time): largest and
+  // smallest; tc_set_pull_chunks / tc_autotune_pull change them
+  int pull_item = 512;
+  int pull_item_min = 128;
   // captured back half of the batched pipeline (batch.cu), keyed by shape,
   // options and the buffers it reads
   cudaGraphExec_t batch_exec = nullptr;
-  int64_t batch_key[12] = {};
+  int64_t batch_key[14] = {};
   int64_t batch_launches = 0;
   char err[1024] = {0};
 };

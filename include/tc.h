@@ -167,6 +167,25 @@ tc_status tc_count_labelled(tc_ctx *ctx, const tc_csr *g, const uint8_t *vertex_
                             const tc_opts *opts, uint64_t *total, uint32_t *edge_counts, int64_t edge_capacity,
                             tc_stats *stats);
 
+/* ---- tuning --------------------------------------------------------------- */
+
+/* Work-chunk sizes of the PULL arm: a warp takes up to `item` grouped edges
+ * at a time, shrinking to `item_min` as the launch runs out of work
+ * (defaults 512 and 128; 32 <= item_min <= item <= 65536).  Results do not
+ * depend on them; speed does, per graph. */
+tc_status tc_set_pull_chunks(tc_ctx *ctx, int32_t item, int32_t item_min);
+tc_status tc_get_pull_chunks(const tc_ctx *ctx, int32_t *item, int32_t *item_min);
+
+/* Autotuner for the PULL work chunks: counts g (the tc_count contract) with
+ * each of the ncand candidate chunk sizes (item_min = max(32, item / 4)),
+ * `reps` times each after one warm-up call, and keeps the candidate with the
+ * lowest device time (CUDA events on the ctx stream, best of reps) in the
+ * ctx.  ms[i] (optional, ncand entries) receives candidate i's time, *best
+ * (optional) the chosen size.  Every candidate's total must agree, else
+ * TC_ERR_INVALID_GRAPH is returned and the ctx keeps its previous sizes. */
+tc_status tc_autotune_pull(tc_ctx *ctx, const tc_csr *g, const tc_opts *opts, const int32_t *candidates,
+                           int32_t ncand, int32_t reps, float *ms, int32_t *best);
+
 /* ---- measurement ---------------------------------------------------------- */
 
 /* L2 read ceiling of the ctx's GPU: one kernel reads a device buffer of

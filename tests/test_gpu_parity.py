@@ -160,6 +160,33 @@ def test_host_input_uploaded_in_pieces(engine):
     assert st["h2d_bytes"] == 8 * len(rowptr) + 4 * len(colidx)
 
 
+def test_pull_chunk_sizes_and_autotune(engine):
+    """PULL work-chunk sizes change speed, never counts; the autotuner keeps
+    the fastest candidate; the batched path's captured graph follows a change."""
+    rowptr, colidx = gen_csr(tc.GenSpec("rmat", scale=16, edge_factor=16, seed=6))
+    ref = oracle.triangles(rowptr, colidx)
+    old = engine.get_pull_chunks()
+    assert old == (512, 128)
+    vtx_off = np.array([0, len(rowptr) - 1], np.int64)
+    try:
+        for item, item_min in ((32, 32), (4096, 64), (512, 128)):
+            engine.set_pull_chunks(item, item_min)
+            assert engine.count(rowptr, colidx, force_arm=tc.ARM_NAMES.index("pull"))[0] == ref, item
+            assert engine.batch_count(vtx_off, rowptr, colidx)[0].tolist() == [ref], item
+        best, ms = engine.autotune_pull(rowptr, colidx, candidates=(128, 512, 2048), reps=1)
+        assert best in (128, 512, 2048) and sorted(ms) == [128, 512, 2048]
+        assert all(t > 0 for t in ms.values()) and ms[best] == min(ms.values())
+        assert engine.get_pull_chunks() == (best, max(32, best // 4))
+        assert engine.count(rowptr, colidx)[0] == ref
+        for bad in ((16, 16), (100, 200), (1 << 17, 64)):
+            with pytest.raises(tc.TCError):
+                engine.set_pull_chunks(*bad)
+        with pytest.raises(tc.TCError):
+            engine.autotune_pull(rowptr, colidx, candidates=(8,))
+    finally:
+        engine.set_pull_chunks(*old)
+
+
 def test_pull_dense_core(engine):
     """A 3000-vertex core with edge probability 1/2 inside a sparse 200 000-vertex
     graph: the core vertices are the top-ranked hubs and their row suffixes are
