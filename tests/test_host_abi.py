@@ -227,3 +227,14 @@ def test_metis_parts_inconsistent_rejected(tmp_path, metis_writer):
     with pytest.raises(tc.TCError) as ei:
         tc.load_metis_part(prefix + "2")
     assert ei.value.status == 5
+
+
+def test_selector_batch_union_is_the_disjoint_union():
+    """The trainer's small-graph batch union: a valid simple symmetric CSR in
+    global ids whose triangles are the batch's per-graph triangles."""
+    from hetegeneous_parallel_programming_gb300.train_selector import batch_union
+    rowptr, colidx = batch_union(24, seed=5)
+    tc.check_csr(rowptr, colidx, sorted_simple=True)
+    vtx_off, lrow, lcol = tc.gen_batch_host(24, seed=5)
+    assert np.array_equal(rowptr, lrow)
+    assert oracle.triangles(rowptr, colidx) == int(oracle.batch_count(vtx_off, lrow, lcol).sum())
