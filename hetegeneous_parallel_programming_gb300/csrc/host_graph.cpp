@@ -572,88 +572,103 @@ tc_status tc_load_metis_part(const char *prefix, tc_metis_part *out) {
   return TC_OK;
 }
 
+// Two passes over the file sets, one set in memory at a time: the first
+// checks every set and records the lengths of its own rows, the second
+// copies those rows.  Memory: the part table, the result and one set.
 tc_status tc_assemble_metis(const char *prefix, int32_t num_parts, int64_t *n_out, int64_t *nnz_out,
                             int64_t **rowptr_out, int32_t **colidx_out, int64_t **part_out) {
   if (!prefix || num_parts < 1 || !n_out || !nnz_out || !rowptr_out || !colidx_out) {
     set_global_error("tc_assemble_metis: bad arguments");
     return TC_ERR_INVALID_ARG;
   }
-  std::vector<tc_metis_part> parts((size_t)num_parts);
-  for (tc_metis_part &q : parts) memset(&q, 0, sizeof(q));
-  auto fail = [&](tc_status s) {
-    for (tc_metis_part &q : parts) tc_metis_part_free(&q);
-    return s;
-  };
-  for (int32_t k = 0; k < num_parts; ++k) {
-    const std::string pk = std::string(prefix) + std::to_string(k);
-    tc_status st = tc_load_metis_part(pk.c_str(), &parts[(size_t)k]);
-    if (st != TC_OK) return fail(st);
-  }
-  const int64_t n = parts[0].n;
-  const int64_t *part = parts[0].part;
-  int64_t owned = 0;
-  for (int32_t k = 0; k < num_parts; ++k) {
-    const tc_metis_part &q = parts[(size_t)k];
-    if (q.n != n || memcmp(q.part, part, sizeof(int64_t) * (size_t)n) != 0) {
-      set_global_error("%s%d: vertex count or part table differs from %s0", prefix, (int)k, prefix);
-      return fail(TC_ERR_INVALID_GRAPH);
-    }
-    owned += q.n_real;
-  }
-  for (int64_t v = 0; v < n; ++v) {
-    if (part[v] < 0 || part[v] >= num_parts) {
-      set_global_error("%s0.part.bin: vertex %lld in partition %lld, outside [0, %d)", prefix, (long long)v,
-                       (long long)part[v], (int)num_parts);
-      return fail(TC_ERR_INVALID_GRAPH);
-    }
-  }
-  if (owned != n) {
-    set_global_error("the vertex lists hold %lld vertices, the graph %lld", (long long)owned, (long long)n);
-    return fail(TC_ERR_INVALID_GRAPH);
-  }
-  // each vertex_list is its partition's vertices in ascending order
-  std::vector<int64_t> seen((size_t)num_parts, 0);
-  for (int64_t v = 0; v < n; ++v) {
-    const tc_metis_part &q = parts[(size_t)part[v]];
-    const int64_t i = seen[(size_t)part[v]]++;
-    if (i >= q.n_real || q.vertex_list[i] != v) {
-      set_global_error("%s%lld.vertex_list.bin does not list partition %lld's vertices in order (vertex %lld)", prefix,
-                       (long long)part[v], (long long)part[v], (long long)v);
-      return fail(TC_ERR_INVALID_GRAPH);
-    }
-  }
-  // rows: owned rows from their partition, every other row empty
-  int64_t *rowptr = (int64_t *)malloc(sizeof(int64_t) * (size_t)(n + 1));
-  if (!rowptr) { set_global_error("host allocation failed"); return fail(TC_ERR_OOM); }
-  rowptr[0] = 0;
-  for (int64_t v = 0; v < n; ++v) {
-    for (int32_t k = 0; k < num_parts; ++k) {
-      const tc_metis_part &q = parts[(size_t)k];
-      if (k != part[v] && q.rowptr[v + 1] != q.rowptr[v]) {
-        free(rowptr);
-        set_global_error("%s%d: row %lld holds entries but vertex %lld belongs to partition %lld", prefix, (int)k,
-                         (long long)v, (long long)v, (long long)part[v]);
-        return fail(TC_ERR_INVALID_GRAPH);
+  auto name = [&](int32_t k) { return std::string(prefix) + std::to_string(k); };
+  tc_metis_part q;
+  memset(&q, 0, sizeof(q));
+  std::vector<int64_t> part, len, owned;
+  int64_t n = 0;
+  tc_status st = TC_OK;
+  for (int32_t k = 0; k < num_parts && st == TC_OK; ++k) {  // pass 1: checks and row lengths
+    st = tc_load_metis_part(name(k).c_str(), &q);
+    if (st != TC_OK) break;
+    if (k == 0) {
+      n = q.n;
+      part.assign(q.part, q.part + n);
+      len.assign((size_t)n, 0);
+      owned.assign((size_t)num_parts, 0);
+      for (int64_t v = 0; v < n; ++v) {
+        if (part[(size_t)v] < 0 || part[(size_t)v] >= num_parts) {
+          set_global_error("%s0.part.bin: vertex %lld in partition %lld, outside [0, %d)", prefix, (long long)v,
+                           (long long)part[(size_t)v], (int)num_parts);
+          st = TC_ERR_INVALID_GRAPH;
+          break;
+        }
+        ++owned[(size_t)part[(size_t)v]];
       }
+    } else if (q.n != n || memcmp(q.part, part.data(), sizeof(int64_t) * (size_t)n) != 0) {
+      set_global_error("%s%d: vertex count or part table differs from %s0", prefix, (int)k, prefix);
+      st = TC_ERR_INVALID_GRAPH;
     }
-    const tc_metis_part &o = parts[(size_t)part[v]];
-    rowptr[v + 1] = rowptr[v] + (o.rowptr[v + 1] - o.rowptr[v]);
+    if (st == TC_OK && q.n_real != owned[(size_t)k]) {
+      set_global_error("%s%d.vertex_list.bin lists %lld vertices, the part table gives partition %d %lld", prefix,
+                       (int)k, (long long)q.n_real, (int)k, (long long)owned[(size_t)k]);
+      st = TC_ERR_INVALID_GRAPH;
+    }
+    int64_t own_entries = 0;
+    for (int64_t i = 0; st == TC_OK && i < q.n_real; ++i) {
+      const int64_t v = q.vertex_list[i];
+      if (part[(size_t)v] != k || (i > 0 && q.vertex_list[i - 1] >= v)) {
+        set_global_error("%s%d.vertex_list.bin does not list partition %d's vertices in order (entry %lld)", prefix,
+                         (int)k, (int)k, (long long)i);
+        st = TC_ERR_INVALID_GRAPH;
+        break;
+      }
+      len[(size_t)v] = q.rowptr[v + 1] - q.rowptr[v];
+      own_entries += len[(size_t)v];
+    }
+    // rows are monotone, so the own rows hold every entry exactly when all
+    // other rows are empty
+    if (st == TC_OK && own_entries != q.nnz) {
+      set_global_error("%s%d: rows of vertices outside partition %d hold entries", prefix, (int)k, (int)k);
+      st = TC_ERR_INVALID_GRAPH;
+    }
+    tc_metis_part_free(&q);
   }
+  if (st != TC_OK) return st;
+  int64_t *rowptr = (int64_t *)malloc(sizeof(int64_t) * (size_t)(n + 1));
+  if (!rowptr) { set_global_error("host allocation failed"); return TC_ERR_OOM; }
+  rowptr[0] = 0;
+  for (int64_t v = 0; v < n; ++v) rowptr[v + 1] = rowptr[v] + len[(size_t)v];
   const int64_t nnz = rowptr[n];
   int32_t *col = (int32_t *)malloc(sizeof(int32_t) * (size_t)std::max<int64_t>(nnz, 1));
   int64_t *part_copy = part_out ? (int64_t *)malloc(sizeof(int64_t) * (size_t)n) : nullptr;
   if (!col || (part_out && !part_copy)) {
     free(rowptr); free(col); free(part_copy);
     set_global_error("host allocation failed");
-    return fail(TC_ERR_OOM);
+    return TC_ERR_OOM;
   }
-#pragma omp parallel for schedule(dynamic, 4096)
-  for (int64_t v = 0; v < n; ++v) {
-    const tc_metis_part &o = parts[(size_t)part[v]];
-    memcpy(col + rowptr[v], o.colidx + o.rowptr[v], sizeof(int32_t) * (size_t)(rowptr[v + 1] - rowptr[v]));
+  for (int32_t k = 0; k < num_parts && st == TC_OK; ++k) {  // pass 2: the own rows' columns
+    st = tc_load_metis_part(name(k).c_str(), &q);
+    if (st != TC_OK) break;
+    if (q.n != n || q.n_real != owned[(size_t)k]) {  // the file set changed between the passes
+      set_global_error("%s%d changed while it was read", prefix, (int)k);
+      st = TC_ERR_IO;
+    }
+    for (int64_t i = 0; st == TC_OK && i < q.n_real; ++i) {
+      const int64_t v = q.vertex_list[i];
+      if (v < 0 || v >= n || part[(size_t)v] != k || q.rowptr[v + 1] - q.rowptr[v] != len[(size_t)v]) {
+        set_global_error("%s%d changed while it was read", prefix, (int)k);
+        st = TC_ERR_IO;
+        break;
+      }
+      memcpy(col + rowptr[v], q.colidx + q.rowptr[v], sizeof(int32_t) * (size_t)len[(size_t)v]);
+    }
+    tc_metis_part_free(&q);
   }
-  if (part_copy) memcpy(part_copy, part, sizeof(int64_t) * (size_t)n);
-  fail(TC_OK);
+  if (st != TC_OK) {
+    free(rowptr); free(col); free(part_copy);
+    return st;
+  }
+  if (part_copy) memcpy(part_copy, part.data(), sizeof(int64_t) * (size_t)n);
   *n_out = n;
   *nnz_out = nnz;
   *rowptr_out = rowptr;

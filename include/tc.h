@@ -391,9 +391,10 @@ void tc_metis_part_free(tc_metis_part *p);
  * row v comes from the partition that owns v.  Checks that every file set
  * has the same n and part table, that part values lie in [0, num_parts),
  * that each vertex_list is exactly the partition's vertices in ascending
- * order, that only owned rows hold entries and that the row lengths add
- * up.  rowptr/colidx are released with tc_csr_free, part (optional, int64[n])
- * with tc_host_free. */
+ * order and that only owned rows hold entries.  The sets are read one at a
+ * time, twice (checks and row lengths, then the rows): memory is the result
+ * plus one set.  rowptr/colidx are released with tc_csr_free, part
+ * (optional, int64[n]) with tc_host_free. */
 tc_status tc_assemble_metis(const char *prefix, int32_t num_parts, int64_t *n, int64_t *nnz, int64_t **rowptr,
                             int32_t **colidx, int64_t **part);
 void tc_host_free(void *p);

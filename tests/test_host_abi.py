@@ -219,7 +219,7 @@ def test_metis_parts_inconsistent_rejected(tmp_path, metis_writer):
     assert tc.load_metis_part(prefix + "0")["nnz"] == int(deg[rows].sum())  # the file set itself reads
     with pytest.raises(tc.TCError) as ei:
         tc.assemble_metis(prefix, 3)
-    assert ei.value.status == 2 and "belongs to partition" in str(ei.value)
+    assert ei.value.status == 2 and "outside partition 0 hold entries" in str(ei.value)
     # a truncated vertex list against its meta file
     metis_writer(prefix, orow, ocol, part, 3)
     vl = np.fromfile(prefix + "2.vertex_list.bin", np.int32)
