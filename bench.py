@@ -358,7 +358,7 @@ def engine_arm(args, rank, world, local_rank, dist):
         dt = run_cpu_sample(rh, ch, orow, ocol, step_k)
         line["cpu_baseline"] = {"value": round(m_sample / dt / 1e9, 5), "unit": "GTEPS",
                                 "cores": oracle.max_threads(), "kind": "port",
-                                "sample": f"every {step_k}th vertex's rows: {m_sample} oriented edges, orientation "
+                                "sample": f"rows of one vertex in {step_k}: {m_sample} oriented edges, orientation "
                                           f"+ merge count, {dt:.1f}s"}
         # reference-style GPU kernel (restated warp_vertex) on the original-id DAG
         try:
@@ -459,7 +459,7 @@ def reference_arm(args, rank, world, local_rank):
             "dtype": "int32/uint64", "data": f"synthetic ({workload_desc(wl)}, same graph as the engine arm)",
             "config": {"workload": workload_desc(wl), "n": n, "undirected_edges": nnz // 2},
             "cpu_baseline": {"value": round(v, 5), "unit": "GTEPS", "cores": cores, "kind": "port",
-                             "sample": f"every {step_k}th vertex's rows ({m_sample} oriented edges): orientation "
+                             "sample": f"rows of one vertex in {step_k} ({m_sample} oriented edges): orientation "
                                        f"(graph.cc:252-298) + merge count (graph.cc:376-391), C/OpenMP"},
             "e2e": {"value": round(v, 5), "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)

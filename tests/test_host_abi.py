@@ -238,3 +238,40 @@ def test_selector_batch_union_is_the_disjoint_union():
     vtx_off, lrow, lcol = tc.gen_batch_host(24, seed=5)
     assert np.array_equal(rowptr, lrow)
     assert oracle.triangles(rowptr, colidx) == int(oracle.batch_count(vtx_off, lrow, lcol).sum())
+
+
+def _bench(args, env=None):
+    import json
+    import os
+    import subprocess
+    import sys
+    e = dict(os.environ, CUDA_VISIBLE_DEVICES="")
+    e.update(env or {})
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py")] + args, env=e, capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.strip()]
+    return [json.loads(ln) for ln in lines]
+
+
+def test_bench_reference_arm_line():
+    """The reference arm times the oracle's orientation + merge count on the
+    host cores and prints one line with the engine arm's metric and unit."""
+    (line,) = _bench(["--impl", "reference", "--workload", "er16k", "--steps", "3", "--warmup", "3",
+                      "--ref-step-seconds", "0.2"])
+    assert line["impl"] == "reference"
+    assert line["unit"] == "GTEPS" and line["higher_is_better"] is True and line["value"] > 0
+    assert (line["n_gpus"], line["steps"], line["warmup"]) == (1, 3, 3)
+    assert line["config"]["n"] == 16384 and line["config"]["workload"].startswith("Erdos-Renyi")
+    cb = line["cpu_baseline"]
+    assert cb["value"] == line["value"] and cb["kind"] == "port" and cb["cores"] >= 1
+    assert "graph.cc:252-298" in cb["sample"] and "graph.cc:376-391" in cb["sample"]
+    assert line["e2e"] == {"value": line["value"], "unit": "GTEPS", "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
+    assert line["vs_baseline"] is None
+
+
+def test_bench_reference_arm_other_ranks_silent():
+    """Under torchrun only rank 0 runs the CPU path; the others exit 0 with no line."""
+    assert _bench(["--impl", "reference", "--workload", "er16k", "--steps", "1", "--warmup", "1"],
+                  env={"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"}) == []
