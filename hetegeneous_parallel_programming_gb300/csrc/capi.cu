@@ -310,6 +310,7 @@ void tc_ctx_destroy(tc_ctx *ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);  // pieced uploads write the arena
   cudaFree(ctx->arena);
   cudaFree(ctx->aux);
   cudaFree(ctx->d_total);
@@ -318,7 +319,6 @@ void tc_ctx_destroy(tc_ctx *ctx) {
   cudaFree(ctx->d_mlp);
   if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
   if (ctx->batch_exec) cudaGraphExecDestroy(ctx->batch_exec);
-  if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
   for (auto &ev : ctx->ev)
     if (ev) cudaEventDestroy(ev);
   for (auto &ev : ctx->piece_ev)
