@@ -6,10 +6,14 @@ imports it.  Wraps oracle/_build/libtc_oracle.so (tc_oracle.c, a plain C +
 OpenMP restatement of the reference CPU path) and adds pure-Python helpers
 for tiny graphs.
 
-Parity status: "parity unpinned" against the reference binary (its device
-intersection lives in the un-vendored GraphMiner tree and it ships no golden
-counts); pinned instead to networkx, analytic answers and brute force via
-the fixtures in tests/golden/.
+Parity status: pinned to the reference's own graph.cc.  oracle/_ref is
+that file compiled unchanged (oracle/build_ref.sh, oracle/ref.py); the
+restatement gives the same oriented arrays, per-edge, total and labelled
+counts as it (tests/test_ref_pin.py), and the fixtures it produced are
+committed in tests/golden/reference_outputs.json.  The reference's device
+intersection (GraphMiner's intersect_num) is not vendored; its CPU merge
+(graph.cc:376-391) is what both compute.  Also pinned to networkx, analytic
+answers and brute force (tests/golden/triangles.json).
 """
 from __future__ import annotations
 
@@ -22,6 +26,7 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 SO = HERE / "_build" / "libtc_oracle.so"
+GEN_HEADER = HERE.parent / "hetegeneous_parallel_programming_gb300" / "csrc" / "tc_gen_common.h"
 _lib = None
 
 
@@ -33,7 +38,8 @@ def build() -> Path:
 def lib() -> C.CDLL:
     global _lib
     if _lib is None:
-        if not SO.exists() or SO.stat().st_mtime < (HERE / "tc_oracle.c").stat().st_mtime:
+        srcs = [HERE / "tc_oracle.c", HERE / "build_oracle.sh", GEN_HEADER]
+        if not SO.exists() or any(SO.stat().st_mtime < f.stat().st_mtime for f in srcs if f.exists()):
             build()
         h = C.CDLL(str(SO))
         P, I64 = C.c_void_p, C.c_int64
@@ -55,6 +61,10 @@ def lib() -> C.CDLL:
         h.oracle_csr_from_edges.argtypes = [I64, I64, P, P, P, P]
         h.oracle_batch_count.restype = None
         h.oracle_batch_count.argtypes = [I64, P, P, P, P]
+        h.oracle_gen_num_samples.restype = I64
+        h.oracle_gen_num_samples.argtypes = [C.c_int32, I64, C.c_int32, C.c_double, C.c_double]
+        h.oracle_gen_edges.restype = I64
+        h.oracle_gen_edges.argtypes = [C.c_int32, I64, C.c_int32] + [C.c_double] * 6 + [C.c_uint64, P, P, I64]
         h.oracle_max_threads.restype = C.c_int
         h.oracle_set_threads.argtypes = [C.c_int]
         _lib = h
@@ -176,6 +186,26 @@ def csr_from_edges(n: int, src, dst):
     if nnz < 0:
         raise ValueError("bad edge list")
     return rowptr, colidx[:nnz].copy()
+
+
+GEN_KINDS = {"er": 0, "rmat": 1, "chung_lu": 3}
+
+
+def gen_edges(kind: str, n: int = 0, scale: int = 0, avg_degree: float = 0.0, edge_factor: float = 16.0,
+              a: float = 0.57, b: float = 0.19, c: float = 0.19, gamma: float = 2.1, seed: int = 0):
+    """The engine's seeded samples (ER, R-MAT, Chung-Lu) drawn without the
+    engine: (n, src, dst).  R-MAT has n = 2^scale."""
+    k = GEN_KINDS[kind]
+    if k == 1:
+        n = 1 << scale
+    M = int(lib().oracle_gen_num_samples(k, int(n), int(scale), float(avg_degree), float(edge_factor)))
+    src = np.empty(max(M, 1), np.int32)
+    dst = np.empty(max(M, 1), np.int32)
+    got = lib().oracle_gen_edges(k, int(n), int(scale), float(avg_degree), float(edge_factor), float(a), float(b),
+                                 float(c), float(gamma), int(seed), _p(src), _p(dst), M)
+    if got != M:
+        raise ValueError("bad generator parameters")
+    return int(n), src[:M], dst[:M]
 
 
 def batch_count(vtx_off, rowptr, colidx):

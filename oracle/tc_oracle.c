@@ -18,12 +18,14 @@
  *   - symmetrise / dedup / self-loop removal: the clean input the reference
  *     assumes (main.cc:17, graph.cc:329); restated as sort + unique per row.
  *
- * Parity status: the reference's own device intersection (GraphMiner's
- * intersect_num) is not vendored and the reference ships no golden counts,
- * so the oracle cannot be pinned to reference outputs ("parity unpinned"
- * against the reference binary).  It is pinned instead to networkx 3.6.1
- * triangle counts, to analytic answers (K_n, K_{a,b}, wheels, grids) and to
- * exhaustive enumeration on small graphs, all committed under tests/golden.
+ * Parity status: pinned to the reference's own code.  oracle/build_ref.sh
+ * compiles the reference's successful_push_pull/graph.cc unchanged into
+ * oracle/_ref; tests/test_ref_pin.py checks that this file gives the same
+ * oriented arrays, per-edge, total and labelled counts on the golden and
+ * seeded graphs, and tests/golden/reference_outputs.json keeps what the
+ * reference produced.  It is also pinned to networkx 3.6.1 triangle counts,
+ * analytic answers (K_n, K_{a,b}, wheels, grids) and exhaustive enumeration
+ * (tests/golden/triangles.json).
  *
  * Build: oracle/build_oracle.sh -> oracle/_build/libtc_oracle.so (gcc -O2 -fopenmp).
  */
@@ -259,3 +261,67 @@ void oracle_batch_count(int64_t num_graphs, const int64_t *vtx_off, const int64_
 
 int oracle_max_threads(void) { return omp_get_max_threads(); }
 void oracle_set_threads(int t) { if (t > 0) omp_set_num_threads(t); }
+
+/* ---- seeded generators, for CPU-only callers --------------------------------
+ * The same samples as the engine's tc_gen_edges_host (kinds 0 ER, 1 R-MAT,
+ * 3 Chung-Lu), from the shared counter-based sampling functions of
+ * tc_gen_common.h, with the per-workload parameters (sample count, R-MAT
+ * quadrant thresholds, Chung-Lu cumulative weights) derived here, so a
+ * process that only times the CPU path need not load the engine library.
+ * tests/test_ref_pin.py checks that both produce identical samples. */
+#include <math.h>
+#include "tc_gen_common.h"
+
+int64_t oracle_gen_num_samples(int32_t kind, int64_t n, int32_t scale, double avg_degree, double edge_factor) {
+  if (kind == 1) return (int64_t)floor(edge_factor * (double)((int64_t)1 << scale));
+  if (kind == 0 || kind == 3) return (int64_t)floor((double)n * avg_degree / 2.0);
+  return -1;
+}
+
+/* Writes the samples into src/dst (capacity entries); returns their number,
+ * or -1 for an unknown kind or too small a buffer. */
+int64_t oracle_gen_edges(int32_t kind, int64_t n, int32_t scale, double avg_degree, double edge_factor, double a,
+                         double b, double c, double gamma, uint64_t seed, int32_t *src, int32_t *dst,
+                         int64_t capacity) {
+  const int64_t M = oracle_gen_num_samples(kind, n, scale, avg_degree, edge_factor);
+  if (M < 0 || M > capacity) return -1;
+  if (kind == 0) {
+    const uint64_t key = tc_stream_key(seed, TC_SID_ER);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < M; ++i) tc_er_sample(key, (uint64_t)n, (uint64_t)i, &src[i], &dst[i]);
+  } else if (kind == 1) {
+    const double s = 4294967296.0;  /* cumulative quadrant probabilities in 2^-32 units */
+    const uint64_t t1 = (uint64_t)floor(a * s), t2 = (uint64_t)floor((a + b) * s),
+                   t3 = (uint64_t)floor((a + b + c) * s);
+    const uint64_t key = tc_stream_key(seed, TC_SID_RMAT);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < M; ++i) tc_rmat_sample(key, scale, t1, t2, t3, (uint64_t)i, &src[i], &dst[i]);
+  } else {
+    /* expected degree of vertex i proportional to (i+1)^(-1/(gamma-1)),
+     * scaled to mean avg_degree, capped at sqrt(n * avg_degree), in 20-bit
+     * fixed point (at least 1), accumulated */
+    uint64_t *cum = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)n);
+    double *w = (double *)malloc(sizeof(double) * (size_t)n);
+    if (!cum || !w) { free(cum); free(w); return -1; }
+    const double alpha = 1.0 / (gamma - 1.0);
+    double sum = 0.0;
+    for (int64_t i = 0; i < n; ++i) {
+      w[i] = pow((double)(i + 1), -alpha);
+      sum += w[i];
+    }
+    const double scl = avg_degree * (double)n / sum, cap = sqrt((double)n * avg_degree);
+    uint64_t acc = 0;
+    for (int64_t i = 0; i < n; ++i) {
+      const double d = fmin(w[i] * scl, cap);
+      uint64_t fx = (uint64_t)llround(d * 1048576.0);
+      acc += fx ? fx : 1;
+      cum[i] = acc;
+    }
+    free(w);
+    const uint64_t key = tc_stream_key(seed, TC_SID_CL);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < M; ++i) tc_cl_sample(key, cum, n, (uint64_t)i, &src[i], &dst[i]);
+    free(cum);
+  }
+  return M;
+}
