@@ -162,6 +162,31 @@ def timed(fn, steps, warmup, eng, torch, dist):
     return ms, out
 
 
+def timed_steps(fn, steps, warmup, eng, torch, dist):
+    """As timed(), plus every step's own device time (a pair of CUDA events
+    around each call) for the median and spread."""
+    for _ in range(warmup):
+        fn()
+    s = torch.cuda.ExternalStream(eng.stream)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev[0].record(s)
+    out = None
+    for i in range(steps):
+        out = fn()
+        ev[i + 1].record(s)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    per = [ev[i].elapsed_time(ev[i + 1]) for i in range(steps)]
+    ms = ev[0].elapsed_time(ev[steps]) / steps
+    from hetegeneous_parallel_programming_gb300 import shard
+    ms, _ = shard.aggregate(ms, 0.0, dist, device="cuda")
+    return ms, out, per
+
+
 def cpu_sample(rowptr_h, colidx_h, target_s: float):
     """Oracle (C/OpenMP) on every k-th row, sized for ~target_s seconds."""
     from oracle import oracle
@@ -276,9 +301,9 @@ def engine_arm(args, rank, world, local_rank, dist):
     # e2e through the public API with pinned host buffers (H2D + D2H inside)
     rowptr_h = rowptr.cpu().pin_memory()
     colidx_h = colidx.cpu().pin_memory()
-    ms_e2e, (tot_e2e, st_e2e) = timed(lambda: eng.count_host_ptr(n, nnz, rowptr_h.data_ptr(), colidx_h.data_ptr(),
-                                                                 selector=best),
-                                      max(1, min(args.steps, 5)), 1, eng, torch, dist)
+    ms_e2e, (tot_e2e, st_e2e), e2e_steps = timed_steps(
+        lambda: eng.count_host_ptr(n, nnz, rowptr_h.data_ptr(), colidx_h.data_ptr(), selector=best),
+        args.steps, args.warmup, eng, torch, dist)
     assert tot_e2e == total
     line = None
     if rank == 0:
@@ -321,7 +346,10 @@ def engine_arm(args, rank, world, local_rank, dist):
             "ms_arm": {k: round(v, 3) for k, v in st["ms_arm"].items()},
             "e2e": {"value": round(world * m / (ms_e2e * 1e-3) / 1e9, 4), "unit": "GTEPS",
                     "h2d_bytes_per_step": int(st_e2e["h2d_bytes"]), "d2h_bytes_per_step": int(st_e2e["d2h_bytes"]),
-                    "ms_per_step": round(ms_e2e, 3)},
+                    "ms_per_step": round(ms_e2e, 3), "steps": len(e2e_steps),
+                    "ms_median": round(statistics.median(e2e_steps), 3),
+                    "ms_min": round(min(e2e_steps), 3), "ms_max": round(max(e2e_steps), 3),
+                    "ms_h2d_in_call": round(st_e2e["ms_h2d"], 3)},
             "roofline": {"bound": "hbm", "kernel": f"arm:{arm}", "achieved": round(achieved, 1), "peak": hbm,
                          "unit": "GB/s", "frac": round(achieved / hbm, 4), "traffic": traffic,
                          "peak_kind": f"{kind} copy bandwidth",
@@ -352,14 +380,36 @@ def engine_arm(args, rank, world, local_rank, dist):
         if line is not None:
             line.update(bat)
     if line is not None and not args.no_cpu_baseline:
-        rh, ch = rowptr_h.numpy(), colidx_h.numpy()
+        # the full CPU oracle on the whole graph (no row sampling): it checks
+        # the total and every per-edge count, and its time is the CPU baseline
         from oracle import oracle
-        orow, ocol, step_k, m_sample, _ = cpu_sample(rh, ch, args.cpu_seconds)
-        dt = run_cpu_sample(rh, ch, orow, ocol, step_k)
-        line["cpu_baseline"] = {"value": round(m_sample / dt / 1e9, 5), "unit": "GTEPS",
+        rh, ch = rowptr_h.numpy(), colidx_h.numpy()
+        pe_dev = torch.empty(max(m, 1), dtype=torch.int32, device=dev)
+        tot_pe, _ = eng.count_device(n, nnz, rowptr.data_ptr(), colidx.data_ptr(), selector=best,
+                                     edge_counts_ptr=pe_dev.data_ptr(), edge_capacity=m)
+        pe_eng = pe_dev[:m].cpu().numpy().view(np.uint32)
+        del pe_dev
+        t0 = time.time()
+        orow, ocol = oracle.orient(rh, ch)
+        tot_o, pe_o = oracle.count(orow, ocol, per_edge=True)
+        dt = time.time() - t0
+        verified = {"against": "the full CPU oracle (C/OpenMP restatement of graph.cc:252-298 + graph.cc:376-391, "
+                               "pinned to the reference's own graph.cc), every oriented edge, no sampling",
+                    "total": tot_o == total, "per_edge": bool(tot_pe == tot_o and np.array_equal(pe_o, pe_eng)),
+                    "learned_total": (results["learned"][1][0] == tot_o) if have_weights else None,
+                    "e2e_total": tot_e2e == tot_o}
+        del pe_eng, pe_o
+        if "batched" in line:
+            verified["batch_totals"] = line["batched"].pop("verified_against_oracle")
+        line["verified"] = verified
+        log(f"[rank {rank}] oracle: T={tot_o} in {dt:.1f}s; verified {verified}")
+        if not all(v for k, v in verified.items() if k != "against" and v is not None):
+            raise SystemExit(f"engine and oracle disagree: {verified}")
+        line["cpu_baseline"] = {"value": round(m / dt / 1e9, 5), "unit": "GTEPS",
                                 "cores": oracle.max_threads(), "kind": "port",
-                                "sample": f"rows of one vertex in {step_k}: {m_sample} oriented edges, orientation "
-                                          f"+ merge count, {dt:.1f}s"}
+                                "sample": f"the whole graph, no sampling: orientation (graph.cc:252-298) + merge "
+                                          f"count of all {m} oriented edges (graph.cc:376-391) with per-edge "
+                                          f"counts, {dt:.1f}s"}
         # reference-style GPU kernel (restated warp_vertex) on the original-id DAG
         try:
             from baseline import build_ref
@@ -413,38 +463,44 @@ def batched(args, eng, torch, dev, dist, rank, learned=False):
             ne = int(rowptr[a + nn]) - e0
             out.append(eng.count_device(nn, ne, loc_rows[g].data_ptr(), base + 4 * e0)[0])
         return out
-    ms_pg, totals_pg = timed(per_graph, 1, 0, eng, torch, dist)
+    pg_steps, pg_warmup = 3, 1
+    ms_pg, totals_pg = timed(per_graph, pg_steps, pg_warmup, eng, torch, dist)
     if list(map(int, totals)) != totals_pg:
         raise SystemExit("batched and per-graph counts disagree")
+    from oracle import oracle  # every graph's total against the CPU oracle
+    ok = bool(np.array_equal(np.asarray(totals, np.uint64), oracle.batch_count(vtx_off, rowptr, colidx)))
+    if not ok:
+        raise SystemExit("batched counts disagree with the CPU oracle")
     return {"batched": {"graphs": G, "graphs_per_s": round(G / (ms * 1e-3), 1), "ms_per_batch": round(ms, 3),
                         "per_graph_launch_graphs_per_s": round(G / (ms_pg * 1e-3), 1),
+                        "per_graph_timing": f"{pg_warmup} warm-up + {pg_steps} timed passes over the {G} graphs",
                         "speedup_vs_per_graph": round(ms_pg / ms, 2), "undirected_edges": len(colidx) // 2,
                         "kernel_launches_per_batch": int(st["kernel_launches"]),
                         "selector": "fixed",
                         "learned_graphs_per_s": round(G / (ms_l * 1e-3), 1) if ms_l else None,
-                        "learned_over_plain": round(ms / ms_l, 4) if ms_l else None}}
+                        "learned_over_plain": round(ms / ms_l, 4) if ms_l else None,
+                        "verified_against_oracle": ok}}
+
+
+def host_graph(wl):
+    """The workload's symmetric CSR built on the host by the oracle alone
+    (same seeded samples as the engine's generator; no engine library)."""
+    from oracle import oracle
+    kw = {k: v for k, v in wl.items() if k != "kind"}
+    n, s, d = oracle.gen_edges(wl["kind"], **kw)
+    rh, ch = oracle.csr_from_edges(n, s, d)
+    return n, rh, ch
 
 
 def reference_arm(args, rank, world, local_rank):
     if rank != 0:
         return
-    import hetegeneous_parallel_programming_gb300 as tc
     from oracle import oracle
     wl = WORKLOADS[args.workload]
-    spec = tc.GenSpec(**wl)
-    try:
-        import torch
-        if not torch.cuda.is_available():
-            raise RuntimeError
-        torch.cuda.set_device(local_rank)
-        eng = tc.Engine(local_rank)
-        n, nnz, rowptr, colidx = make_graph(eng, wl, torch, torch.device("cuda", local_rank))
-        rh, ch = rowptr.cpu().numpy(), colidx.cpu().numpy()
-        eng.close()
-    except Exception:
-        n, s, d = tc.gen_edges_host(spec)
-        rh, ch = oracle.csr_from_edges(n, s, d)
-        nnz = len(ch)
+    t0 = time.time()
+    n, rh, ch = host_graph(wl)
+    nnz = len(ch)
+    log(f"reference arm: host graph n={n} nnz={nnz} ({time.time() - t0:.1f}s)")
     orow, ocol, step_k, m_sample, _ = cpu_sample(rh, ch, args.ref_step_seconds)
     for _ in range(args.warmup):
         run_cpu_sample(rh, ch, orow, ocol, step_k)
@@ -456,7 +512,8 @@ def reference_arm(args, rank, world, local_rank):
             "metric": "GTEPS on 1 GB300, learned vs plain selector (exact count); batched graphs/s",
             "value": round(v, 5), "unit": "GTEPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(sec * 1e3, 2), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "int32/uint64", "data": f"synthetic ({workload_desc(wl)}, same graph as the engine arm)",
+            "dtype": "int32/uint64",
+            "data": f"synthetic ({workload_desc(wl)}, same graph as the engine arm, drawn on the host cores)",
             "config": {"workload": workload_desc(wl), "n": n, "undirected_edges": nnz // 2},
             "cpu_baseline": {"value": round(v, 5), "unit": "GTEPS", "cores": cores, "kind": "port",
                              "sample": f"rows of one vertex in {step_k} ({m_sample} oriented edges): orientation "
@@ -474,8 +531,8 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="rmat24")
     ap.add_argument("--batch-graphs", type=int, default=4096)
     ap.add_argument("--no-batched", action="store_true")
-    ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true",
+                    help="skip the full CPU oracle run (its check of every count and its timing)")
     ap.add_argument("--per-edge", action="store_true", help="also write per-edge local counts every step")
     ap.add_argument("--no-per-vertex", action="store_true", help="skip the per-vertex triangle count timing")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default PULL work-chunk size")

@@ -11,6 +11,7 @@ a GPU the calls raise.
 from __future__ import annotations
 
 import ctypes as C
+from pathlib import Path
 from dataclasses import dataclass
 from typing import Optional, Sequence
 
@@ -358,6 +359,36 @@ class Engine:
             out = out[:len(colidx)]
         return int(tot.value), out, st.as_dict()
 
+    def count_dag_range(self, rowptr, colidx, row_begin: int, row_end: int, *, selector: str = "fixed",
+                        force_arm=None, edge_counts: bool = False, validate: bool = True):
+        """One shard of count_dag: the edges of rows [row_begin, row_end) of an
+        oriented graph, counted against the whole graph.  Returns (partial
+        total, per-edge counts of the range or None, stats dict)."""
+        rowptr, colidx = _i64(rowptr), _i32(colidx)
+        g = _ffi.Csr(len(rowptr) - 1, len(colidx), _ptr(rowptr).value, _ptr(colidx).value, 0)
+        o = _opts(selector, force_arm, validate)
+        tot = C.c_uint64(0)
+        st = _ffi.Stats()
+        rb, re = int(row_begin), int(row_end)
+        width = int(rowptr[re] - rowptr[rb]) if 0 <= rb <= re < len(rowptr) else 0
+        out = np.empty(max(width, 1), np.uint32) if edge_counts else None
+        self._chk(self._L.tc_count_dag_range(self._h, C.byref(g), rb, re, C.byref(o), C.byref(tot), _ptr(out),
+                                             width if edge_counts else 0, C.byref(st)))
+        if out is not None:
+            out = out[:width]
+        return int(tot.value), out, st.as_dict()
+
+    def count_dag_range_device(self, n: int, nnz: int, rowptr_ptr: int, colidx_ptr: int, row_begin: int,
+                               row_end: int, *, selector: str = "fixed", validate: bool = True):
+        """count_dag_range on a device-resident oriented graph: (partial total, stats dict)."""
+        g = _ffi.Csr(int(n), int(nnz), int(rowptr_ptr), int(colidx_ptr), 1)
+        o = _opts(selector, None, validate)
+        tot = C.c_uint64(0)
+        st = _ffi.Stats()
+        self._chk(self._L.tc_count_dag_range(self._h, C.byref(g), int(row_begin), int(row_end), C.byref(o),
+                                             C.byref(tot), None, 0, C.byref(st)))
+        return int(tot.value), st.as_dict()
+
     def count_dag_parts(self, rowptr, colidx, part, num_parts: int, *, rule: str = "source",
                         selector: str = "fixed", force_arm=None, validate: bool = True):
         """Per-partition partial counts of an oriented graph split by part
@@ -534,6 +565,19 @@ class Engine:
     def set_selector_weights(self, params) -> None:
         params = np.ascontiguousarray(params, np.float32)
         self._chk(self._L.tc_selector_set_weights(self._h, _ptr(params), len(params)))
+
+    def load_shipped_selector(self) -> bool:
+        """Loads the shipped MLP cost-model weights (data/selector_mlp.npz)
+        for selector="learned"; False when the file is absent or holds
+        weights for another arm set."""
+        path = Path(__file__).resolve().parent / "data" / "selector_mlp.npz"
+        if not path.exists():
+            return False
+        w = np.load(path)["params"].astype(np.float32)
+        if w.size != TC_MLP_PARAM_COUNT:
+            return False
+        self.set_selector_weights(w)
+        return True
 
     def get_selector_weights(self) -> np.ndarray:
         out = np.zeros(TC_MLP_PARAM_COUNT, np.float32)

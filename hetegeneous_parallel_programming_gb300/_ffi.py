@@ -102,6 +102,8 @@ _SIGS = {
     "tc_orient": (C.c_int, [P, C.POINTER(Csr), P, P, I64, PI64]),
     "tc_count": (C.c_int, [P, C.POINTER(Csr), C.POINTER(Opts), PU64, P, I64, C.POINTER(Stats)]),
     "tc_count_dag": (C.c_int, [P, C.POINTER(Csr), C.POINTER(Opts), PU64, P, I64, C.POINTER(Stats)]),
+    "tc_count_dag_range": (C.c_int, [P, C.POINTER(Csr), I64, I64, C.POINTER(Opts), PU64, P, I64,
+                                     C.POINTER(Stats)]),
     "tc_count_vertices": (C.c_int, [P, C.POINTER(Csr), C.POINTER(Opts), PU64, P, C.POINTER(Stats)]),
     "tc_count_labelled": (C.c_int, [P, C.POINTER(Csr), P, I32, C.POINTER(Opts), PU64, P, I64, C.POINTER(Stats)]),
     "tc_batch_count": (C.c_int, [P, C.POINTER(Batch), C.POINTER(Opts), P, C.POINTER(Stats)]),

@@ -595,8 +595,15 @@ struct PartReq {
   uint64_t *totals;
 };
 
+// Rows [row_begin, row_end) of an oriented graph counted against the whole
+// graph (tc_count_dag_range).
+struct RangeReq {
+  int64_t row_begin, row_end;
+};
+
 static tc_status count_dag_impl(tc_ctx *ctx, const tc_csr *dag_in, const tc_opts *opts_in, uint64_t *total,
-                                uint32_t *edge_counts, int64_t edge_capacity, tc_stats *stats, const PartReq *pr) {
+                                uint32_t *edge_counts, int64_t edge_capacity, tc_stats *stats, const PartReq *pr,
+                                const RangeReq *rr = nullptr) {
   if (!ctx || !total) return set_error(ctx, TC_ERR_INVALID_ARG, "null ctx or total");
   TC_TRY(check_csr_args(ctx, dag_in));
   tc_opts o;
@@ -607,18 +614,38 @@ static tc_status count_dag_impl(tc_ctx *ctx, const tc_csr *dag_in, const tc_opts
   tc_stats st;
   memset(&st, 0, sizeof(st));
   const int64_t m = dag_in->nnz;
+  // The counted edges: all of them, or the entries of a row range
+  // [e0, e1) = [rowptr[row_begin], rowptr[row_end]).
+  int64_t e0 = 0, e1 = m;
+  if (rr) {
+    if (rr->row_begin < 0 || rr->row_begin > rr->row_end || rr->row_end > dag_in->n)
+      return set_error(ctx, TC_ERR_INVALID_ARG, "row range [%lld, %lld) outside [0, %lld]", (long long)rr->row_begin,
+                       (long long)rr->row_end, (long long)dag_in->n);
+    if (dag_in->on_device) {
+      TC_CHECK_CUDA(ctx, cudaMemcpy(&e0, dag_in->rowptr + rr->row_begin, sizeof(int64_t), cudaMemcpyDeviceToHost));
+      TC_CHECK_CUDA(ctx, cudaMemcpy(&e1, dag_in->rowptr + rr->row_end, sizeof(int64_t), cudaMemcpyDeviceToHost));
+    } else {
+      e0 = dag_in->rowptr[rr->row_begin];
+      e1 = dag_in->rowptr[rr->row_end];
+    }
+    if (e0 < 0 || e0 > e1 || e1 > m)
+      return set_error(ctx, TC_ERR_INVALID_GRAPH, "row pointers of the range [%lld, %lld) are not within [0, nnz]",
+                       (long long)rr->row_begin, (long long)rr->row_end);
+  }
+  const int64_t m_out = e1 - e0;
   const bool want_edges = edge_counts != nullptr;
-  if (want_edges && edge_capacity < m)
+  if (want_edges && edge_capacity < m_out)
     return set_error(ctx, TC_ERR_INVALID_ARG, "edge_counts holds %lld entries, %lld edges", (long long)edge_capacity,
-                     (long long)m);
+                     (long long)m_out);
   // partitioned sums need per-edge counts on the device
   const bool dev_edges = want_edges || pr != nullptr;
   Sizer sz;
   if (!dag_in->on_device) { sz.take<int64_t>(dag_in->n + 1); sz.take<int32_t>(m); }
   sz.take<int32_t>(m);
   sz.take<int32_t>(dag_in->n);
+  if (rr) sz.take<int64_t>(dag_in->n + 1);
   sz.used += count_scratch_bytes(ctx, dag_in->n, m);
-  if (dev_edges && !(want_edges && dag_in->on_device)) sz.take<uint32_t>(m);
+  if (dev_edges && !(want_edges && dag_in->on_device)) sz.take<uint32_t>(m_out);
   if (pr) {
     if (!dag_in->on_device) sz.take<int64_t>(dag_in->n);
     sz.take<unsigned long long>(pr->num_parts);
@@ -630,11 +657,12 @@ static tc_status count_dag_impl(tc_ctx *ctx, const tc_csr *dag_in, const tc_opts
   TC_TRY(stage_csr(ctx, dag_in, bump, d, &st.h2d_bytes));
   int32_t *src = bump.take<int32_t>(m);
   int32_t *indeg = bump.take<int32_t>(dag_in->n);
+  int64_t *range_rowptr = rr ? bump.take<int64_t>(dag_in->n + 1) : nullptr;
   CountBufs cb;
   if (count_carve(ctx, dag_in->n, m, bump, cb, o.record_tile_costs != 0) != TC_OK || bump.overflow)
     return set_error(ctx, TC_ERR_OOM, "arena overflow");
   uint32_t *d_out = nullptr;
-  if (dev_edges) d_out = (want_edges && dag_in->on_device) ? edge_counts : bump.take<uint32_t>(m);
+  if (dev_edges) d_out = (want_edges && dag_in->on_device) ? edge_counts : bump.take<uint32_t>(m_out);
   const int64_t *d_part = nullptr;
   unsigned long long *d_pt = nullptr;
   if (pr) {
@@ -664,13 +692,17 @@ static tc_status count_dag_impl(tc_ctx *ctx, const tc_csr *dag_in, const tc_opts
   TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[4], ctx->stream));
   TC_TRY(launch_expand_src(ctx, d.rowptr, d.n, m, src));
   TC_TRY(launch_indeg(ctx, d.col, d.n, m, indeg));
+  // A row range is counted in place: its edges are entries [e0, e1) of the
+  // column array, so the count runs on col + e0 with row pointers shifted by
+  // -e0 (every row's list, inside the range or not, stays where it is).
+  if (rr) TC_TRY(launch_shift_rowptr(ctx, d.rowptr, d.n, e0, range_rowptr));
   TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[5], ctx->stream));
   DevDag dag;
   dag.n = d.n;
-  dag.m = m;
-  dag.rowptr = d.rowptr;
-  dag.col = d.col;
-  dag.src = src;
+  dag.m = m_out;
+  dag.rowptr = rr ? range_rowptr : d.rowptr;
+  dag.col = d.col + e0;
+  dag.src = src + e0;
   dag.perm = nullptr;
   dag.indeg = indeg;
   dag.restrict_after = 0;
@@ -678,10 +710,10 @@ static tc_status count_dag_impl(tc_ctx *ctx, const tc_csr *dag_in, const tc_opts
   TC_TRY(run_count(ctx, dag, o, cb, d_out, true));
   if (pr) TC_TRY(launch_part_sums(ctx, dag, d_out, d_part, pr->num_parts, pr->rule, d_pt));
   TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[6], ctx->stream));
-  if (want_edges && !dag_in->on_device && m > 0) {
-    TC_CHECK_CUDA(ctx, cudaMemcpyAsync(edge_counts, d_out, sizeof(uint32_t) * (size_t)m, cudaMemcpyDeviceToHost,
+  if (want_edges && !dag_in->on_device && m_out > 0) {
+    TC_CHECK_CUDA(ctx, cudaMemcpyAsync(edge_counts, d_out, sizeof(uint32_t) * (size_t)m_out, cudaMemcpyDeviceToHost,
                                        ctx->stream));
-    st.d2h_bytes += sizeof(uint32_t) * (size_t)m;
+    st.d2h_bytes += sizeof(uint32_t) * (size_t)m_out;
   }
   if (pr) {
     TC_CHECK_CUDA(ctx, cudaMemcpyAsync(pr->totals, d_pt, sizeof(uint64_t) * (size_t)pr->num_parts,
@@ -704,8 +736,8 @@ static tc_status count_dag_impl(tc_ctx *ctx, const tc_csr *dag_in, const tc_opts
   st.ms_orient = elapsed(ctx->ev[4], ctx->ev[5]);
   st.ms_d2h = elapsed(ctx->ev[6], ctx->ev[7]);
   st.ms_total = elapsed(ctx->ev[0], ctx->ev[7]);
-  st.m = m;
-  st.tiles = (m + TILE_EDGES - 1) / TILE_EDGES;
+  st.m = m_out;
+  st.tiles = (m_out + TILE_EDGES - 1) / TILE_EDGES;
   st.kernel_launches = ctx->launches;
   if (stats) *stats = st;
   return TC_OK;
@@ -714,6 +746,13 @@ static tc_status count_dag_impl(tc_ctx *ctx, const tc_csr *dag_in, const tc_opts
 tc_status tc_count_dag(tc_ctx *ctx, const tc_csr *dag_in, const tc_opts *opts_in, uint64_t *total,
                        uint32_t *edge_counts, int64_t edge_capacity, tc_stats *stats) {
   return count_dag_impl(ctx, dag_in, opts_in, total, edge_counts, edge_capacity, stats, nullptr);
+}
+
+tc_status tc_count_dag_range(tc_ctx *ctx, const tc_csr *dag, int64_t row_begin, int64_t row_end,
+                             const tc_opts *opts, uint64_t *total, uint32_t *edge_counts, int64_t edge_capacity,
+                             tc_stats *stats) {
+  const RangeReq rr{row_begin, row_end};
+  return count_dag_impl(ctx, dag, opts, total, edge_counts, edge_capacity, stats, nullptr, &rr);
 }
 
 tc_status tc_count_dag_parts(tc_ctx *ctx, const tc_csr *dag, const int64_t *part, int32_t num_parts, int32_t rule,

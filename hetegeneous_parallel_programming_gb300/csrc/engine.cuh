@@ -102,6 +102,7 @@ tc_status orient_phase_b(tc_ctx *ctx, const DevCSR &g, OrientBufs &b, int64_t m,
 
 // Row of every entry of a CSR (for counting a caller-oriented DAG).
 tc_status launch_expand_src(tc_ctx *ctx, const int64_t *rowptr, int64_t n, int64_t m, int32_t *src);
+tc_status launch_shift_rowptr(tc_ctx *ctx, const int64_t *rowptr, int64_t n, int64_t shift, int64_t *out);
 
 // Counting.
 struct CountBufs {

@@ -781,6 +781,20 @@ tc_status launch_indeg(tc_ctx *ctx, const int32_t *col, int64_t n, int64_t m, in
   return TC_OK;
 }
 
+// out[i] = rowptr[i] - shift: row pointers of a row range counted in place,
+// relative to the range's first entry (tc_count_dag_range).
+__global__ void shift_rowptr_kernel(const int64_t *__restrict__ rowptr, int64_t n, int64_t shift,
+                                    int64_t *__restrict__ out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = rowptr[i] - shift;
+}
+
+tc_status launch_shift_rowptr(tc_ctx *ctx, const int64_t *rowptr, int64_t n, int64_t shift, int64_t *out) {
+  shift_rowptr_kernel<<<grid_for(ctx, n + 1, 256, 8), 256, 0, ctx->stream>>>(rowptr, n, shift, out);
+  TC_CHECK_LAUNCH(ctx);
+  return TC_OK;
+}
+
 tc_status launch_expand_src(tc_ctx *ctx, const int64_t *rowptr, int64_t n, int64_t m, int32_t *src) {
   if (m <= 0) return TC_OK;
   expand_src_kernel<<<grid_for(ctx, m, ENTRY_TILE, 8), OR_THREADS, 0, ctx->stream>>>(rowptr, n, m, src);

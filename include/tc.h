@@ -146,6 +146,21 @@ tc_status tc_count(tc_ctx *ctx, const tc_csr *g, const tc_opts *opts, uint64_t *
 tc_status tc_count_dag(tc_ctx *ctx, const tc_csr *dag, const tc_opts *opts, uint64_t *total,
                        uint32_t *edge_counts, int64_t edge_capacity, tc_stats *stats);
 
+/* One shard of tc_count_dag: the edges of rows [row_begin, row_end) of an
+ * oriented graph, each counted against the whole graph (every row's list is
+ * read where it lies), so *total is the sum over u in the range, v in
+ * N+(u), of |N+(u) n N+(v)|.  Contiguous row ranges that cover [0, n) give
+ * partial counts that add up to tc_count_dag's total, with no exchange but
+ * that one sum.  It replaces the reference's split of the rows over GPUs
+ * (vertex u to device u % device_count, multigpu.cu:827-843) and its host
+ * gather of the per-device counts (multigpu.cu:930-941).  edge_counts
+ * (optional, edge_capacity >= rowptr[row_end] - rowptr[row_begin]) receives
+ * the range's per-edge counts in input order.  Validation, when enabled,
+ * checks the whole graph. */
+tc_status tc_count_dag_range(tc_ctx *ctx, const tc_csr *dag, int64_t row_begin, int64_t row_end,
+                             const tc_opts *opts, uint64_t *total, uint32_t *edge_counts, int64_t edge_capacity,
+                             tc_stats *stats);
+
 /* Triangles through every vertex of a symmetric graph: vertex_counts[u]
  * (n entries, input ids, memory kind of g->on_device) = number of triangles
  * that contain u, and *total = number of triangles.  The per-vertex counts

@@ -12,6 +12,11 @@ from reference_fixtures import digest, fixtures, golden_inputs, seeded_inputs
 
 pytestmark = pytest.mark.gpu
 
+
+@pytest.fixture(autouse=True)
+def _shipped_selector(engine):
+    assert engine.load_shipped_selector()
+
 ARMS = list(range(tc.TC_NUM_ARMS))
 
 

@@ -275,3 +275,17 @@ def test_bench_reference_arm_other_ranks_silent():
     """Under torchrun only rank 0 runs the CPU path; the others exit 0 with no line."""
     assert _bench(["--impl", "reference", "--workload", "er16k", "--steps", "1", "--warmup", "1"],
                   env={"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"}) == []
+
+
+def test_bench_reference_arm_does_not_load_the_engine():
+    """The reference arm draws its graph with the oracle on the host, so the
+    engine library is never mapped into its process."""
+    import subprocess
+    import sys
+    code = ("import sys, runpy; sys.argv = ['bench.py', '--impl', 'reference', '--workload', 'er16k', "
+            "'--steps', '1', '--warmup', '0', '--ref-step-seconds', '0.1']; "
+            "runpy.run_path('bench.py', run_name='__main__'); "
+            "print('ENGINE_MAPPED', 'libtc.so' in open('/proc/self/maps').read())")
+    r = subprocess.run([sys.executable, "-c", code], cwd=str(ROOT), capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert "ENGINE_MAPPED False" in r.stdout

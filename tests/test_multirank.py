@@ -29,7 +29,13 @@ def _worker(rank, world, port, rowptr, colidx, expect, q):
         orow, ocol = oracle.orient(rowptr, colidx)
         ranges = shard.balanced_row_ranges(orow, ocol, world)
         r0, r1 = ranges[rank]
-        local = int(oracle.lib().oracle_count_rows(len(orow) - 1, oracle._p(orow), oracle._p(ocol), r0, r1, 1, None))
+        if torch.cuda.is_available():  # the engine counts the shard (tc_count_dag_range)
+            import hetegeneous_parallel_programming_gb300 as tc
+            with tc.Engine(0) as eng:
+                local = eng.count_dag_range(orow, ocol, r0, r1)[0]
+        else:  # no GPU here: the oracle stands in for the engine's shard count
+            local = int(oracle.lib().oracle_count_rows(len(orow) - 1, oracle._p(orow), oracle._p(ocol), r0, r1, 1,
+                                                       None))
         total = shard.allreduce_total(local, dist)
         ms, units = shard.aggregate(10.0 + rank, 100.0 * (rank + 1), dist)
         q.put((rank, total, ms, units, ranges))
