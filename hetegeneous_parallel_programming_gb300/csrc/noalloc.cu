@@ -18,6 +18,8 @@
 #include <algorithm>
 #include <mutex>
 
+#include <cuda.h>
+
 #include "engine.cuh"
 
 namespace tc {
@@ -170,6 +172,35 @@ __global__ void __launch_bounds__(NA_THREADS) noalloc_hash_kernel(const int64_t 
 
 static std::mutex g_na_mu;
 static void *g_na_ptr[64] = {};
+static unsigned long long g_na_ctx[64] = {};  // context the cached address belongs to
+
+// Identity of the calling thread's current context (unique for the life of
+// the process, so a context created after cudaDeviceReset gets a new one);
+// 0 when the driver does not report it.  The driver calls are reached through
+// the runtime's entry-point query, so the library does not link libcuda.
+static unsigned long long current_ctx_id() {
+  typedef CUresult (*GetCurrent)(CUcontext *);
+  typedef CUresult (*GetId)(CUcontext, unsigned long long *);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static bool resolved = false;
+  if (!resolved) {
+    void *a = nullptr, *b = nullptr;
+    cudaDriverEntryPointQueryResult qa, qb;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) == cudaSuccess &&
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) == cudaSuccess &&
+        qa == cudaDriverEntryPointSuccess && qb == cudaDriverEntryPointSuccess) {
+      get_current = (GetCurrent)a;
+      get_id = (GetId)b;
+    }
+    (void)cudaGetLastError();
+    resolved = true;
+  }
+  CUcontext c = nullptr;
+  unsigned long long id = 0;
+  if (get_current && get_id && get_current(&c) == CUDA_SUCCESS && c && get_id(c, &id) == CUDA_SUCCESS) return id;
+  return 0;
+}
 
 }  // namespace tc
 
@@ -190,7 +221,9 @@ extern "C" tc_status tc_count_dag_noalloc(int device, const int64_t *rowptr, con
     (void)cudaGetLastError();
     return set_error(nullptr, TC_ERR_NO_DEVICE, "no CUDA device");
   }
-  if (prev != device && cudaSetDevice(device) != cudaSuccess) {
+  // cudaSetDevice also makes the device's primary context current (the
+  // context the runtime launches into), which the set-up below relies on.
+  if (cudaSetDevice(device) != cudaSuccess) {
     (void)cudaGetLastError();
     return set_error(nullptr, TC_ERR_INVALID_ARG, "cannot make device %d current", device);
   }
@@ -198,16 +231,21 @@ extern "C" tc_status tc_count_dag_noalloc(int device, const int64_t *rowptr, con
   void *scratch = nullptr;
   {
     // Set-up, once per device with that device current: the device address of
-    // the static array (its host-side name is only a stand-in).
+    // the static array (its host-side name is only a stand-in).  The address
+    // belongs to the device's current context; a new context (after
+    // cudaDeviceReset) has the array elsewhere, so the set-up runs again.
     std::lock_guard<std::mutex> lk(g_na_mu);
-    if (!g_na_ptr[device]) {
+    const unsigned long long ctx_id = current_ctx_id();
+    if (!g_na_ptr[device] || g_na_ctx[device] != ctx_id) {
       void *p = nullptr;
       cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
       if (e != cudaSuccess) {
         (void)cudaGetLastError();
+        g_na_ptr[device] = nullptr;
         st = set_error(nullptr, TC_ERR_CUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
       } else {
         g_na_ptr[device] = p;
+        g_na_ctx[device] = ctx_id;
       }
     }
     scratch = g_na_ptr[device];

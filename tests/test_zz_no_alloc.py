@@ -5,7 +5,9 @@ It exists for callers that may not allocate device memory while counting
 them, latency-bound loops that cannot take cudaMalloc's implicit sync).  The
 test calls it through the C ABI on device buffers the test owns and checks
 its total and per-edge counts against the allocating entry point
-tc_count_dag, bit for bit (integer counts), on two calls in a row: the
+tc_count_dag and the CPU oracle, bit for bit (integer counts), on graphs
+whose oriented rows are short (the kernel's hash path) and longer than 512
+entries (its per-edge warp search), on two calls in a row: the
 second call reuses the static scratch the first one left behind.  This file
 sorts last so that a run stopping at the first failure has already run every
 other test.
@@ -23,6 +25,10 @@ pytestmark = pytest.mark.gpu
 
 
 def _dag(spec):
+    if spec == "hubs":  # hubs and a 700-clique: oriented rows of up to 700 entries
+        from reference_fixtures import MAKER
+        rowptr, colidx = MAKER.hubs(20000, 4)
+        return oracle.orient(rowptr, colidx)
     n, s, d = tc.gen_edges_host(spec)
     rowptr, colidx = oracle.csr_from_edges(n, s, d)
     return oracle.orient(rowptr, colidx)
@@ -37,13 +43,19 @@ def _noalloc(orow_d, ocol_d, n, m, total_d, counts_d):
 
 
 @pytest.mark.parametrize("spec", [tc.GenSpec("rmat", scale=16, edge_factor=16, seed=3),
-                                  tc.GenSpec("er", n=20000, avg_degree=24, seed=4)])
+                                  tc.GenSpec("er", n=20000, avg_degree=24, seed=4),
+                                  "hubs"])
 def test_noalloc_matches_allocating_entry_point(spec):
     import torch
     orow, ocol = _dag(spec)
     n, m = len(orow) - 1, len(ocol)
+    if spec == "hubs":  # rows longer than 512 entries take the kernel's per-edge warp search
+        assert int(np.diff(orow).max()) > 512
     with tc.Engine(0) as eng:
         ref_total, ref_pe, _ = eng.count_dag(orow, ocol, edge_counts=True)
+    # the allocating entry point and the CPU oracle agree, so both pin the variant
+    o_total, o_pe = oracle.count(orow, ocol, per_edge=True)
+    assert ref_total == o_total and np.array_equal(ref_pe, o_pe)
     orow_d = torch.from_numpy(orow).cuda()
     ocol_d = torch.from_numpy(ocol).cuda()
     total_d = torch.full((1,), -1, dtype=torch.int64, device="cuda")
