@@ -45,7 +45,8 @@ class Stats(C.Structure):
                 ("ms_d2h", C.c_float), ("ms_total", C.c_float), ("m", C.c_int64), ("tiles", C.c_int64),
                 ("tiles_per_arm", C.c_int64 * TC_NUM_ARMS), ("kernel_launches", C.c_int64),
                 ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64), ("ms_arm", C.c_float * TC_NUM_ARMS),
-                ("alg_bytes_arm", C.c_uint64 * TC_NUM_ARMS), ("alg_bytes", C.c_uint64)]
+                ("alg_bytes_arm", C.c_uint64 * TC_NUM_ARMS), ("alg_bytes", C.c_uint64),
+                ("ms_pull_kernel", C.c_float), ("pull_edges", C.c_uint64)]
 
     _PER_ARM = ("tiles_per_arm", "ms_arm", "alg_bytes_arm")
 

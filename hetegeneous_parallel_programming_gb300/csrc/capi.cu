@@ -135,8 +135,9 @@ float elapsed(cudaEvent_t a, cudaEvent_t b) {
 
 // Validation + phase A + read back m and the flags (which the caller zeroed
 // before any kernel that may set them).
-tc_status orient_front(tc_ctx *ctx, const DevCSR &d, const tc_opts &o, OrientBufs &ob, int64_t *m,
-                              float *ms_validate, float *ms_a) {
+// The orientation's first half up to the host's read of m and the flags
+// (the copies are queued, not waited for); graph-capturable.
+tc_status orient_front_launch(tc_ctx *ctx, const DevCSR &d, const tc_opts &o, OrientBufs &ob) {
   TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[1], ctx->stream));
   // row pointers here; the column checks ride on the kept-count pass
   if (o.validate) TC_TRY(launch_validate_rowptr(ctx, d));
@@ -147,6 +148,23 @@ tc_status orient_front(tc_ctx *ctx, const DevCSR &d, const tc_opts &o, OrientBuf
   TC_CHECK_CUDA(ctx, cudaMemcpyAsync(&ctx->h_pinned[0], ob.d_m, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
   TC_CHECK_CUDA(ctx, cudaMemcpyAsync(&ctx->h_pinned[1], ctx->d_flags, sizeof(unsigned) * 2, cudaMemcpyDeviceToHost,
                                      ctx->stream));
+  return TC_OK;
+}
+
+// Waits for orient_front_launch's copies: the validation flags and m.
+tc_status orient_front_finish(tc_ctx *ctx, int64_t *m, float *ms_validate, float *ms_a) {
+  TC_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  const unsigned flags = (unsigned)(ctx->h_pinned[1] & 0xffffffffu);
+  if (flags) return set_error(ctx, TC_ERR_INVALID_GRAPH, "%s", flag_text(flags));
+  *m = (int64_t)ctx->h_pinned[0];
+  *ms_validate = elapsed(ctx->ev[1], ctx->ev[2]);
+  *ms_a = elapsed(ctx->ev[2], ctx->ev[3]);
+  return TC_OK;
+}
+
+tc_status orient_front(tc_ctx *ctx, const DevCSR &d, const tc_opts &o, OrientBufs &ob, int64_t *m,
+                              float *ms_validate, float *ms_a) {
+  TC_TRY(orient_front_launch(ctx, d, o, ob));
   TC_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   const unsigned flags = (unsigned)(ctx->h_pinned[1] & 0xffffffffu);
   if (flags) return set_error(ctx, TC_ERR_INVALID_GRAPH, "%s", flag_text(flags));
@@ -177,6 +195,16 @@ __global__ void l2_read_kernel(const uint4 *__restrict__ buf, int64_t n4, int pa
 }
 
 }  // namespace tc
+
+// A bounded device-side wait that gave up (VF_TIMEOUT, read back with the
+// total into h_pinned[3]) fails the call.  The kernels that wait count the
+// affected edges without the staged copy, so the total is still exact, but
+// a wait that runs out points at a device that is not making progress.
+static tc_status check_wait_flags(tc_ctx *ctx) {
+  if ((unsigned)(ctx->h_pinned[3] & 0xffffffffu) & VF_TIMEOUT)
+    return set_error(ctx, TC_ERR_TIMEOUT, "a bounded device wait gave up (bulk copy not completed)");
+  return TC_OK;
+}
 
 extern "C" {
 
@@ -319,6 +347,7 @@ void tc_ctx_destroy(tc_ctx *ctx) {
   cudaFree(ctx->d_mlp);
   if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
   if (ctx->batch_exec) cudaGraphExecDestroy(ctx->batch_exec);
+  if (ctx->batch_front_exec) cudaGraphExecDestroy(ctx->batch_front_exec);
   for (auto &ev : ctx->ev)
     if (ev) cudaEventDestroy(ev);
   for (auto &ev : ctx->piece_ev)
@@ -406,9 +435,12 @@ tc_status tc_count(tc_ctx *ctx, const tc_csr *g, const tc_opts *opts_in, uint64_
   }
   TC_CHECK_CUDA(ctx, cudaMemcpyAsync(&ctx->h_pinned[2], ctx->d_total, sizeof(unsigned long long),
                                      cudaMemcpyDeviceToHost, ctx->stream));
+  TC_CHECK_CUDA(ctx, cudaMemcpyAsync(&ctx->h_pinned[3], ctx->d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                                     ctx->stream));
   st.d2h_bytes += sizeof(unsigned long long);
   TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[7], ctx->stream));
   TC_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  TC_TRY(check_wait_flags(ctx));
   *total = ctx->h_pinned[2];
   count_stats(ctx, &st, true);
   st.ms_orient = ms_a + elapsed(ctx->ev[4], ctx->ev[5]);
@@ -493,9 +525,12 @@ tc_status tc_count_labelled(tc_ctx *ctx, const tc_csr *g, const uint8_t *vertex_
   }
   TC_CHECK_CUDA(ctx, cudaMemcpyAsync(&ctx->h_pinned[2], ctx->d_total, sizeof(unsigned long long),
                                      cudaMemcpyDeviceToHost, ctx->stream));
+  TC_CHECK_CUDA(ctx, cudaMemcpyAsync(&ctx->h_pinned[3], ctx->d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                                     ctx->stream));
   st.d2h_bytes += sizeof(unsigned long long);
   TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[7], ctx->stream));
   TC_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  TC_TRY(check_wait_flags(ctx));
   *total = ctx->h_pinned[2];
   count_stats(ctx, &st, true);
   st.ms_orient = ms_a + elapsed(ctx->ev[4], ctx->ev[5]);
@@ -571,9 +606,12 @@ tc_status tc_count_vertices(tc_ctx *ctx, const tc_csr *g, const tc_opts *opts_in
   }
   TC_CHECK_CUDA(ctx, cudaMemcpyAsync(&ctx->h_pinned[2], ctx->d_total, sizeof(unsigned long long),
                                      cudaMemcpyDeviceToHost, ctx->stream));
+  TC_CHECK_CUDA(ctx, cudaMemcpyAsync(&ctx->h_pinned[3], ctx->d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                                     ctx->stream));
   st.d2h_bytes += sizeof(unsigned long long);
   TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[7], ctx->stream));
   TC_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  TC_TRY(check_wait_flags(ctx));
   *total = ctx->h_pinned[2];
   count_stats(ctx, &st, true);
   st.ms_orient = ms_a + elapsed(ctx->ev[4], ctx->ev[5]);
@@ -724,11 +762,14 @@ static tc_status count_dag_impl(tc_ctx *ctx, const tc_csr *dag_in, const tc_opts
   }
   TC_CHECK_CUDA(ctx, cudaMemcpyAsync(&ctx->h_pinned[2], ctx->d_total, sizeof(unsigned long long),
                                      cudaMemcpyDeviceToHost, ctx->stream));
+  TC_CHECK_CUDA(ctx, cudaMemcpyAsync(&ctx->h_pinned[3], ctx->d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                                     ctx->stream));
   st.d2h_bytes += sizeof(unsigned long long);
   TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[7], ctx->stream));
   TC_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   if (pr && (ctx->h_pinned[1] & VF_PART_RANGE))
     return set_error(ctx, TC_ERR_INVALID_ARG, "%s", flag_text(VF_PART_RANGE));
+  TC_TRY(check_wait_flags(ctx));
   *total = ctx->h_pinned[2];
   count_stats(ctx, &st, true);
   st.ms_h2d = elapsed(ctx->ev[0], ctx->ev[1]);

@@ -455,6 +455,160 @@ __global__ void __launch_bounds__(CT_THREADS) bsearch_kernel(DevDag g, const uin
   flush_total(acc, total);
 }
 
+// ---- BSEARCH_32 with the search list staged by bulk copies ----------------------
+//
+// One warp per edge, as in the reference's warp_intersect (graph_gpu.h:228-252):
+// lanes take keys of the shorter list and binary-search them in the longer
+// one.  Here the longer list is first copied into the warp's shared memory by
+// one bulk asynchronous copy (cp.async.bulk, the TMA unit's non-tensor form)
+// completing an mbarrier, so every search step reads shared memory instead of
+// making a dependent trip to L2; the copy of the warp's next edge is issued
+// before the current edge is searched, so it overlaps that search.  The copy
+// covers the 16-byte blocks that hold the list (at most 3 entries either
+// side; an aligned block holding a list entry lies in that entry's memory
+// page), and the search skips to the list's offset in the buffer.  Lists
+// longer than a buffer are searched in place (pivot search).  A wait that
+// gives up (it should never) sets VF_TIMEOUT and the warp counts its
+// remaining edges in place, after waiting (bounded) for its copies in flight.
+// 1: BSEARCH_32 searches the longer list in place (pivot search), for
+// measuring the staged version against it.
+#ifndef TC_BS32_PIVOT
+#define TC_BS32_PIVOT 0
+#endif
+constexpr int BT_STAGE = 512;         // entries per staging buffer (static shared memory stays under 48 KB)
+constexpr int BT_WARPS = CT_THREADS / 32;
+constexpr uint32_t BT_WAIT_LIMIT = 1u << 22;
+
+struct BtEdge {
+  const int32_t *keys;   // shorter list (global)
+  const int32_t *list;   // longer list (global)
+  int nk, nl;
+  int off;               // list's first entry in the staging buffer (staged only)
+  bool staged;
+};
+
+// Issues the copy of edge e's longer list into buf (lane 0), or marks it to be
+// searched in place.
+__device__ __forceinline__ BtEdge bt_issue(const DevDag &g, int64_t e, int32_t *buf, uint64_t *bar, bool stage_ok,
+                                           int lane) {
+  int32_t s;
+  const EdgeLists L = edge_lists(g, e, s);
+  BtEdge b;
+  const bool a_short = L.na <= L.nb;
+  b.keys = a_short ? L.a : L.b;
+  b.nk = a_short ? L.na : L.nb;
+  b.list = a_short ? L.b : L.a;
+  b.nl = a_short ? L.nb : L.na;
+  b.off = 0;
+  b.staged = false;
+  // staging pays when the searches touch more of the list than the copy
+  // moves: about nk * log2(nl) probes of a 32-byte sector each against 4*nl
+  // bytes copied
+  if (!stage_ok || b.nk <= 0 || b.nl <= 32 || b.nl > BT_STAGE ||
+      8 * b.nk * (32 - __clz(b.nl)) < b.nl)
+    return b;
+  const uintptr_t a0 = reinterpret_cast<uintptr_t>(b.list);
+  const uintptr_t lo = a0 & ~(uintptr_t)15, hi = (a0 + 4 * (uintptr_t)b.nl + 15) & ~(uintptr_t)15;
+  b.off = (int)((a0 - lo) >> 2);
+  b.staged = true;
+  if (lane == 0) {
+    fence_proxy_async_smem();  // this warp's earlier reads of buf come first
+    mbar_arrive_expect_tx(bar, (uint32_t)(hi - lo));
+    bulk_copy_g2s(buf, reinterpret_cast<const void *>(lo), (uint32_t)(hi - lo), bar);
+  }
+  return b;
+}
+
+__device__ __forceinline__ uint32_t bt_count_staged(const BtEdge &b, const int32_t *buf, int lane) {
+  const int32_t *S = buf + b.off;
+  uint32_t c = 0;
+  int lo = 0;
+  for (int i = lane; i < b.nk; i += 32) {  // keys ascend, so each lane's lower bound only moves up
+    const int32_t key = __ldg(b.keys + i);
+    int hi = b.nl;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (S[mid] < key) lo = mid + 1; else hi = mid;
+    }
+    if (lo < b.nl && S[lo] == key) ++c;
+  }
+  return c;
+}
+
+__global__ void __launch_bounds__(CT_THREADS) bsearch_tma_kernel(DevDag g, const uint32_t *__restrict__ qtiles,
+                                                                const int64_t *__restrict__ qoff, int arm,
+                                                                unsigned *head, uint32_t *out,
+                                                                unsigned long long *total,
+                                                                unsigned long long *tile_cycles) {
+  __shared__ __align__(16) int32_t stage[BT_WARPS][2][BT_STAGE + 8];
+  __shared__ __align__(8) uint64_t bar[BT_WARPS][2];
+  __shared__ int64_t s_tile;
+  const int64_t qb = qoff[arm], qn = qoff[arm + 1] - qb;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) {
+    mbar_init(&bar[w][0], 1);
+    mbar_init(&bar[w][1], 1);
+    fence_mbar_init();
+  }
+  __syncwarp();
+  uint32_t parity[2] = {0u, 0u};  // parity of the next phase of each buffer's barrier
+  bool stage_ok = true;           // false after a wait gave up: this warp stops staging
+  bool pending[2] = {false, false};
+  unsigned long long acc = 0;
+  for (;;) {
+    const int64_t tile = next_tile(qtiles, qb, qn, head, &s_tile);
+    if (tile < 0) break;
+    const long long c0 = clock64();
+    const int64_t e0 = tile * TILE_EDGES, e1 = min(g.m, e0 + TILE_EDGES);
+    int cur = 0;
+    int64_t e = e0 + w;
+    BtEdge b = {};
+    if (e < e1) {
+      b = bt_issue(g, e, stage[w][cur], &bar[w][cur], stage_ok, lane);
+      pending[cur] = b.staged;
+    }
+    for (; e < e1; e += BT_WARPS) {
+      BtEdge nb = {};
+      const int64_t en = e + BT_WARPS;
+      if (en < e1) {  // the next edge's copy overlaps this edge's search
+        nb = bt_issue(g, en, stage[w][cur ^ 1], &bar[w][cur ^ 1], stage_ok, lane);
+        pending[cur ^ 1] = nb.staged;
+      }
+      uint32_t c = 0;
+      bool in_place = !b.staged;
+      if (b.staged) {
+        const bool ok = mbar_wait_bounded(&bar[w][cur], parity[cur], BT_WAIT_LIMIT);
+        if (__all_sync(TC_FULL_MASK, ok)) {
+          parity[cur] ^= 1u;
+          pending[cur] = false;
+        } else {  // give up staging; count in place
+          if (lane == 0 && g.flags) atomicOr(g.flags, (unsigned)VF_TIMEOUT);
+          stage_ok = false;
+          in_place = true;
+        }
+      }
+      if (!in_place) c = bt_count_staged(b, stage[w][cur], lane);
+      else if (b.nk > 0 && b.nl > 0) c = pivot_search_count(b.keys, b.nk, b.list, b.nl, lane);
+      c = warp_sum(c);
+      if (lane == 0) {
+        put_edge_count(g, out, e, c);
+        acc += c;
+      }
+      __syncwarp();  // every lane is done with this buffer before it takes a new copy
+      cur ^= 1;
+      b = nb;
+    }
+    if (tile_cycles) {
+      __syncthreads();
+      if (threadIdx.x == 0) atomicAdd(&tile_cycles[tile], (unsigned long long)(clock64() - c0));
+    }
+  }
+  // a copy left in flight by a wait that gave up lands before the block exits
+  for (int k = 0; k < 2; ++k)
+    if (pending[k]) (void)mbar_wait_bounded(&bar[w][k], parity[k], BT_WAIT_LIMIT);
+  flush_total(acc, total);
+}
+
 // ---- MERGE_G ---------------------------------------------------------------------
 
 template <int G>
@@ -1073,16 +1227,31 @@ __device__ __forceinline__ uint32_t attr_search_count(const int32_t *__restrict_
 
 constexpr int PL_THREADS = 128;
 constexpr int PL_WARPS = PL_THREADS / 32;
-constexpr int PL_WORDS = 2048;  // per warp: a 65536-id bitmap or a 2048-slot hash table
+#ifndef TC_PL_WORDS
+#define TC_PL_WORDS 2048
+#endif
+#ifndef TC_PL_MIN_BLOCKS
+#define TC_PL_MIN_BLOCKS 6
+#endif
+constexpr int PL_WORDS = TC_PL_WORDS;  // per warp: a 65536-id bitmap or a 2048-slot hash table
 constexpr int PL_UNROLL = 4;      // table build: list loads in flight per lane
-constexpr int PL_GUNROLL = 4;      // flattened probing: 16-byte loads in flight per lane
+#ifndef TC_PL_GUNROLL
+#define TC_PL_GUNROLL 4
+#endif
+constexpr int PL_GUNROLL = TC_PL_GUNROLL;  // flattened probing: 16-byte loads in flight per lane
 constexpr int PL_GROUP_THREADS = 256;
 // Dense edges: an edge u->v whose source is a hub and whose row suffix holds
 // more than PL_DENSE_NUM / PL_DENSE_DEN entries per 32-bit word of v's
 // bitmap table is counted by ANDing u's hub bit row with the table, 32
 // candidates per word, instead of probing the suffix entry by entry.
-constexpr int PL_DENSE_NUM = 1;
-constexpr int PL_DENSE_DEN = 1;
+#ifndef TC_PL_DENSE_NUM
+#define TC_PL_DENSE_NUM 1
+#endif
+#ifndef TC_PL_DENSE_DEN
+#define TC_PL_DENSE_DEN 1
+#endif
+constexpr int PL_DENSE_NUM = TC_PL_DENSE_NUM;
+constexpr int PL_DENSE_DEN = TC_PL_DENSE_DEN;
 // Dense edges join two of the top PL_DENSE_HUB ids; their bit rows take
 // PL_DENSE_HUB^2 / 8 bytes (512 MB).
 constexpr int64_t PL_DENSE_HUB = 65536;
@@ -1387,7 +1556,7 @@ __device__ __forceinline__ unsigned pull_next_chunk(unsigned *head, int64_t np, 
 // counts (g.vlabel set).  Separate instantiations, so the plain kernel
 // (MODE 0) keeps its registers.
 template <int MODE>
-__global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint2 *__restrict__ er,
+__global__ void __launch_bounds__(PL_THREADS, TC_PL_MIN_BLOCKS) pull_kernel(DevDag g, const uint2 *__restrict__ er,
                                                          const unsigned *__restrict__ npull,
                                                          unsigned *head, uint32_t *out, unsigned long long *total,
                                                          unsigned long long *tile_cycles, int item, int item_min) {
@@ -1431,13 +1600,19 @@ __global__ void __launch_bounds__(PL_THREADS) pull_kernel(DevDag g, const uint2 
       // down to a 128-id boundary counted from hub0 (a hub target's list lies
       // in (v, n), so the window still fits)
       PullDense pd{hub0, 0, 0, hub_e0};
-      const bool dense_run = MODE != 1 && g.hub_bits != nullptr && bitmap && nb > 0 && v >= hub0;
+      bool dense_run = MODE != 1 && g.hub_bits != nullptr && bitmap && nb > 0 && v >= hub0;
       if (dense_run) {
         const int32_t bmax = bmin + (int32_t)span - 1;
-        pd.woff4 = (bmin - hub0) >> 7;
-        bmin = hub0 + 128 * pd.woff4;
-        span = (uint32_t)(bmax - bmin) + 1u;
-        pd.tw4 = (int)((span + 127u) >> 7);
+        const int woff4 = (bmin - hub0) >> 7;
+        const uint32_t span2 = (uint32_t)(bmax - (hub0 + 128 * woff4)) + 1u;
+        if (span2 <= (uint32_t)PL_WORDS * 32u) {  // the aligned window still fits the table
+          pd.woff4 = woff4;
+          bmin = hub0 + 128 * woff4;
+          span = span2;
+          pd.tw4 = (int)((span + 127u) >> 7);
+        } else {
+          dense_run = false;
+        }
       }
       if (!bitmap && nb > PL_WORDS / 2) {  // wide window and long list: warp pivot search per edge
         long long tq = tr0;
@@ -1558,7 +1733,11 @@ typedef void (*ArmKernel)(DevDag, const uint32_t *, const int64_t *, int, unsign
 static ArmKernel arm_kernel(int arm) {
   switch (arm) {
     case TC_ARM_BSEARCH_4: return bsearch_kernel<4>;
+#if TC_BS32_PIVOT
     case TC_ARM_BSEARCH_32: return bsearch_kernel<32>;
+#else
+    case TC_ARM_BSEARCH_32: return bsearch_tma_kernel;
+#endif
     case TC_ARM_MERGE_8: return merge_kernel<8>;
     case TC_ARM_MERGE_32: return merge_kernel<32>;
     case TC_ARM_HASH: return hash_kernel;
@@ -1645,6 +1824,7 @@ tc_status count_carve(const tc_ctx *ctx, int64_t n, int64_t m, Bump &bump, Count
 // Pinned host scratch layout used by run_count / count_stats (64 words).
 constexpr int PIN_QOFF = 16;                           // TC_NUM_ARMS + 1 int64
 constexpr int PIN_BYTES = PIN_QOFF + TC_NUM_ARMS + 1;  // TC_NUM_ARMS uint64
+constexpr int PIN_PULL = PIN_BYTES + TC_NUM_ARMS;       // uint32: edges the PULL arm grouped
 static_assert(PIN_BYTES + TC_NUM_ARMS <= 64, "pinned scratch holds 64 words");
 static_assert(sizeof(((tc_ctx *)nullptr)->ev) / sizeof(cudaEvent_t) >= 10 + TC_NUM_ARMS, "one event per arm");
 
@@ -1695,7 +1875,7 @@ __global__ void hub_bits_kernel(DevDag g, int32_t hub0, int wpr4, const unsigned
   }
 }
 
-static tc_status run_pull(tc_ctx *ctx, const DevDag &g_in, CountBufs &cb, uint32_t *out, int64_t T) {
+static tc_status run_pull(tc_ctx *ctx, const DevDag &g_in, CountBufs &cb, uint32_t *out, int64_t T, bool timing) {
   PullKeys pk;
   const int64_t K = pull_key_count(g_in.n, T, &pk);
   unsigned *pos = cb.pull_pos;
@@ -1717,6 +1897,11 @@ static tc_status run_pull(tc_ctx *ctx, const DevDag &g_in, CountBufs &cb, uint32
   }
   // pos[K] (no edge has key K) still holds the number of grouped edges
   const int grid = ctx->num_sms * ctx->arm_blocks_per_sm[TC_ARM_PULL];
+  if (timing) {
+    TC_CHECK_CUDA(ctx, cudaMemcpyAsync(&ctx->h_pinned[PIN_PULL], pos + K, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                                       ctx->stream));
+    TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[10 + TC_NUM_ARMS], ctx->stream));
+  }
   if (g.top)
     pull_kernel<1><<<grid, PL_THREADS, 0, ctx->stream>>>(g, cb.pull_er, pos + K, ctx->d_heads + TC_ARM_PULL, out,
                                                         ctx->d_total, cb.tile_cycles, ctx->pull_item,
@@ -1730,10 +1915,16 @@ static tc_status run_pull(tc_ctx *ctx, const DevDag &g_in, CountBufs &cb, uint32
                                                     ctx->d_heads + TC_ARM_PULL, out, ctx->d_total, cb.tile_cycles, ctx->pull_item,
                                                         ctx->pull_item_min);
   TC_CHECK_LAUNCH(ctx);
+  if (timing) {
+    TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[11 + TC_NUM_ARMS], ctx->stream));
+    ctx->pull_timed = true;
+  }
   return TC_OK;
 }
 
-tc_status run_count(tc_ctx *ctx, const DevDag &g, const tc_opts &opts, CountBufs &cb, uint32_t *out, bool timing) {
+tc_status run_count(tc_ctx *ctx, const DevDag &g_in, const tc_opts &opts, CountBufs &cb, uint32_t *out, bool timing) {
+  DevDag g = g_in;
+  g.flags = ctx->d_flags;
   const int64_t T = (g.m + TILE_EDGES - 1) / TILE_EDGES;
   if (opts.selector == TC_SELECT_LEARNED && !ctx->mlp_loaded)
     return set_error(ctx, TC_ERR_INVALID_ARG, "learned selector requested but no MLP weights are loaded");
@@ -1772,7 +1963,7 @@ tc_status run_count(tc_ctx *ctx, const DevDag &g, const tc_opts &opts, CountBufs
   if (timing) TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[9], ctx->stream));
   for (int a = 0; a < TC_NUM_ARMS; ++a) {
     if (T > 0 && a == TC_ARM_PULL) {
-      TC_TRY(run_pull(ctx, g, cb, out, T));
+      TC_TRY(run_pull(ctx, g, cb, out, T, timing));
     } else if (T > 0) {
       const int grid = ctx->num_sms * ctx->arm_blocks_per_sm[a];
       arm_kernel(a)<<<grid, arm_threads(a), arm_smem(a), ctx->stream>>>(g, sv, cb.qoff, a, ctx->d_heads + a, out,
@@ -1933,6 +2124,11 @@ void count_stats(tc_ctx *ctx, tc_stats *st, bool timing) {
   }
   st->alg_bytes = tot;
   if (!timing) return;
+  if (ctx->pull_timed) {
+    st->ms_pull_kernel = ev_ms(ctx->ev[10 + TC_NUM_ARMS], ctx->ev[11 + TC_NUM_ARMS]);
+    st->pull_edges = (uint64_t)(uint32_t)(ctx->h_pinned[PIN_PULL] & 0xffffffffull);
+    ctx->pull_timed = false;
+  }
   st->ms_plan = ev_ms(ctx->ev[8], ctx->ev[9]);
   st->ms_count = ev_ms(ctx->ev[9], ctx->ev[10 + TC_NUM_ARMS - 1]);
   for (int a = 0; a < TC_NUM_ARMS; ++a) st->ms_arm[a] = ev_ms(ctx->ev[a == 0 ? 9 : 9 + a], ctx->ev[10 + a]);

@@ -32,8 +32,10 @@ struct tc_ctx {
   unsigned int *d_heads = nullptr;        // [64] work-queue heads
   unsigned long long *h_pinned = nullptr; // [64] pinned host scratch
   // events: [0..8) entry-point phases, [8] plan start, [9] count start,
-  // [10 + a] end of arm a's kernel
-  cudaEvent_t ev[10 + TC_NUM_ARMS] = {};
+  // [10 + a] end of arm a's kernel, [10 + TC_NUM_ARMS] and [11 + TC_NUM_ARMS]
+  // around the PULL arm's probing kernel (pull_kernel) alone
+  cudaEvent_t ev[12 + TC_NUM_ARMS] = {};
+  bool pull_timed = false;                // the pull_kernel events belong to this call
   // host input of tc_count: the column array is uploaded in pieces on a
   // second stream while the orientation starts (one event per piece)
   cudaStream_t copy_stream = nullptr;
@@ -54,6 +56,10 @@ struct tc_ctx {
   cudaGraphExec_t batch_exec = nullptr;
   int64_t batch_key[14] = {};
   int64_t batch_launches = 0;
+  // captured front half (group ids, validation, ranks, kept counts, scans)
+  cudaGraphExec_t batch_front_exec = nullptr;
+  int64_t batch_front_key[12] = {};
+  int64_t batch_front_launches = 0;
   char err[1024] = {0};
 };
 
@@ -109,6 +115,52 @@ struct Sizer {
 };
 
 // ---- device primitives ------------------------------------------------------
+
+// Bulk asynchronous copies (the TMA unit, non-tensor form) with mbarrier
+// completion.  A copy moves `bytes` (a multiple of 16) from a 16-byte
+// aligned global address to a 16-byte aligned shared address and completes
+// the mbarrier's transaction count; waits poll try_wait with a bound.
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+// Makes mbarrier initialisation visible to the async (bulk copy) proxy.
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+// Orders this thread's earlier generic shared-memory accesses before later
+// async-proxy accesses (a bulk copy overwriting a buffer that was read).
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+
+// True once the mbarrier phase of the given parity has completed.
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Polls at most `limit` times; false when the phase did not complete.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, uint32_t limit) {
+  for (uint32_t i = 0; i < limit; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
 
 __device__ __forceinline__ unsigned lanemask_lt() {
   unsigned m;

@@ -41,6 +41,7 @@ struct DevDag {
   const uint8_t *vlabel = nullptr;   // [n] labelled mode: vertex labels (relabelled ids; PULL arm only)
   int label = 0;                     // labelled mode: count common neighbours with this label
   int restrict_after = 0;
+  unsigned *flags = nullptr;         // VF_* error bits (ctx->d_flags): a bounded device wait that gave up
   // PULL dense edges: bit rows of the DAG rows of the top hub ids, one row of
   // hub_wpr4 16-byte words per hub (null: dense path off)
   const uint4 *hub_bits = nullptr;
@@ -150,6 +151,10 @@ void orient_carve(const tc_ctx *ctx, int64_t n, int64_t nnz, bool perm, bool dag
                   int pieces = 1);
 tc_status orient_front(tc_ctx *ctx, const DevCSR &d, const tc_opts &o, OrientBufs &ob, int64_t *m, float *ms_validate,
                        float *ms_a);
+// orient_front in two halves: the launches (graph-capturable: kernels, event
+// records and the queued copies of m and the flags) and the wait for them.
+tc_status orient_front_launch(tc_ctx *ctx, const DevCSR &d, const tc_opts &o, OrientBufs &ob);
+tc_status orient_front_finish(tc_ctx *ctx, int64_t *m, float *ms_validate, float *ms_a);
 float elapsed(cudaEvent_t a, cudaEvent_t b);
 const char *flag_text(unsigned f);
 tc_status init_arm_occupancy(tc_ctx *ctx);

@@ -105,6 +105,10 @@ typedef struct tc_stats {
    * edge itself); alg_bytes adds 8*(n+1) for the row pointers. */
   uint64_t alg_bytes_arm[TC_NUM_ARMS];
   uint64_t alg_bytes;
+  /* The PULL arm's probing kernel alone (its grouping and bit-row kernels
+   * excluded) and the number of edges it grouped (0 when no tile chose it). */
+  float ms_pull_kernel;
+  uint64_t pull_edges;
 } tc_stats;
 
 /* ---- context ---------------------------------------------------------- */
@@ -232,7 +236,9 @@ tc_status tc_l2_bandwidth(tc_ctx *ctx, int64_t bytes, int32_t passes, double *gb
  *   default stream).  The call is asynchronous: *total is valid once the
  *   stream has been synchronised.  Inputs are not validated on the device.
  * The first call on each device looks up the array's device address
- * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * (cudaGetSymbolAddress), and so does the first call after the device's
+ * context has been replaced (cudaDeviceReset); make such a call before any
+ * stream capture.
  * All calls share the one array and every call overwrites it: calls whose
  * work overlaps on the GPU (other streams or threads without ordering) race
  * and return wrong counts.  Errors are reported by tc_last_error(NULL). */
