@@ -316,15 +316,17 @@ def engine_arm(args, rank, world, local_rank, dist):
         if have_weights:
             eng.set_selector_weights(w)
 
-    # the project's autotuner picks the PULL work-chunk size for this graph
-    # (counts it with each candidate before the timed region)
+    # the project's autotuner picks the run-time tuning for this graph (PULL
+    # chunk and source-block sizes, dense ratio, orientation geometry) by
+    # counting it with each trial setting before the timed region
     tune = None
     if not args.no_autotune:
         t0 = time.time()
-        best_item, tune_ms = eng.autotune_pull(rowptr.data_ptr(), (colidx.data_ptr(), nnz),
-                                               candidates=(256, 512, 1024), reps=2, on_device_n=n)
-        tune = {"pull_chunk": best_item, "ms_per_candidate": {str(k): round(v, 3) for k, v in tune_ms.items()}}
-        log(f"[rank {rank}] autotune: PULL chunk {best_item} {tune['ms_per_candidate']} ({time.time() - t0:.1f}s)")
+        default = eng.get_tuning()
+        best_t, best_ms, trials = eng.autotune(rowptr.data_ptr(), (colidx.data_ptr(), nnz), reps=2, on_device_n=n)
+        tune = {"chosen": best_t, "default": default, "ms_chosen": round(best_ms, 3), "trials": trials,
+                "seconds": round(time.time() - t0, 1)}
+        log(f"[rank {rank}] autotune: {best_t} {best_ms:.3f} ms after {trials} trials ({time.time() - t0:.1f}s)")
 
     per_edge = torch.empty(m if args.per_edge else 1, dtype=torch.int32, device=dev)
 

@@ -555,6 +555,41 @@ class Engine:
                                            ms.ctypes.data_as(C.POINTER(C.c_float)), C.byref(best)))
         return int(best.value), {int(c): float(t) for c, t in zip(cands, ms)}
 
+    def get_tuning(self) -> dict:
+        """The engine's run-time tuning (tc_tuning) as a dict."""
+        t = _ffi.Tuning()
+        self._chk(self._L.tc_get_tuning(self._h, C.byref(t)))
+        return t.as_dict()
+
+    def set_tuning(self, **kw) -> None:
+        """Changes fields of the run-time tuning (tc_tuning); the rest keep their values."""
+        t = _ffi.Tuning(**self.get_tuning())
+        for k, v in kw.items():
+            if k not in dict(_ffi.Tuning._fields_):
+                raise ValueError(f"unknown tuning field {k}")
+            setattr(t, k, int(v))
+        self._chk(self._L.tc_set_tuning(self._h, C.byref(t)))
+
+    def autotune(self, rowptr, colidx, reps: int = 2, *, selector: str = "fixed", on_device_n: int = 0):
+        """Coordinate-descent autotuner over the PULL chunk size, source-block
+        size, dense ratio and orientation geometry (tc_autotune); keeps the
+        fastest setting in this engine.  Returns (tuning dict, ms, trials).
+        rowptr/colidx are host arrays, or device pointers when on_device_n
+        (the vertex count) is given, with colidx then paired as (ptr, nnz)."""
+        if on_device_n:
+            (rp_ptr, cl_ptr, nnz) = rowptr, colidx[0], colidx[1]
+            g = _ffi.Csr(int(on_device_n), int(nnz), int(rp_ptr), int(cl_ptr), 1)
+        else:
+            rowptr, colidx = _i64(rowptr), _i32(colidx)
+            g = _ffi.Csr(len(rowptr) - 1, len(colidx), _ptr(rowptr).value, _ptr(colidx).value, 0)
+        o = _opts(selector, None, True)
+        t = _ffi.Tuning()
+        ms = C.c_float(0)
+        trials = C.c_int32(0)
+        self._chk(self._L.tc_autotune(self._h, C.byref(g), C.byref(o), int(reps), C.byref(t), C.byref(ms),
+                                      C.byref(trials)))
+        return t.as_dict(), float(ms.value), int(trials.value)
+
     def l2_bandwidth(self, nbytes: int = 64 << 20, passes: int = 128) -> float:
         """L2 read ceiling in GB/s: one kernel streams an L2-resident buffer
         `passes` times with L1-bypassing 16-byte loads (tc_l2_bandwidth)."""

@@ -73,6 +73,14 @@ class Batch(C.Structure):
                 ("colidx", C.c_void_p), ("on_device", C.c_int32)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("pull_item", C.c_int32), ("pull_item_min", C.c_int32), ("pull_block_tiles", C.c_int32),
+                ("pull_dense_num", C.c_int32), ("pull_dense_den", C.c_int32), ("orient_blocks_per_sm", C.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
+
+
 class BatchSpec(C.Structure):
     _fields_ = [("num_graphs", C.c_int64), ("n_min", C.c_int64), ("n_max", C.c_int64), ("deg_min", C.c_double),
                 ("deg_max", C.c_double), ("a", C.c_double), ("b", C.c_double), ("c", C.c_double),
@@ -113,6 +121,9 @@ _SIGS = {
     "tc_set_pull_chunks": (C.c_int, [P, I32, I32]),
     "tc_get_pull_chunks": (C.c_int, [P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "tc_autotune_pull": (C.c_int, [P, C.POINTER(Csr), C.POINTER(Opts), P, I32, I32, PF, C.POINTER(C.c_int32)]),
+    "tc_get_tuning": (C.c_int, [P, C.POINTER(Tuning)]),
+    "tc_set_tuning": (C.c_int, [P, C.POINTER(Tuning)]),
+    "tc_autotune": (C.c_int, [P, C.POINTER(Csr), C.POINTER(Opts), I32, C.POINTER(Tuning), PF, C.POINTER(C.c_int32)]),
     "tc_count_dag_parts": (C.c_int, [P, C.POINTER(Csr), P, I32, I32, C.POINTER(Opts), PU64, P, C.POINTER(Stats)]),
     "tc_count_edges": (C.c_int, [P, I64, I64, P, P, I32, C.POINTER(Opts), PU64, C.POINTER(Stats)]),
     "tc_tile_profile": (C.c_int, [P, C.POINTER(Csr), P, P, I64, PI64]),

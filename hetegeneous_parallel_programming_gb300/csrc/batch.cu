@@ -129,7 +129,7 @@ tc_status tc_batch_count(tc_ctx *ctx, const tc_batch *b, const tc_opts *opts_in,
   // batch shape and buffers repeat; the host then reads m and the flags.
   const int64_t fkey[12] = {n, nnz, G, o.validate, (int64_t)(uintptr_t)ctx->arena, (int64_t)ctx->arena_cap,
                             (int64_t)(uintptr_t)d_col, (int64_t)(uintptr_t)d_row, (int64_t)(uintptr_t)d_off,
-                            (int64_t)b->on_device, 0, 0};
+                            (int64_t)b->on_device, ctx->orient_blocks_per_sm, 0};
   const bool fsame = ctx->batch_front_exec && memcmp(fkey, ctx->batch_front_key, sizeof(fkey)) == 0;
   if (!fsame) {
     if (ctx->batch_front_exec) {
@@ -171,8 +171,9 @@ tc_status tc_batch_count(tc_ctx *ctx, const tc_batch *b, const tc_opts *opts_in,
   // a CUDA graph when the batch shape and buffers repeat.
   const int64_t key[14] = {n, nnz, m, G, o.selector, o.force_arm, (int64_t)(uintptr_t)ctx->arena,
                            (int64_t)ctx->arena_cap, (int64_t)(uintptr_t)d_col, (int64_t)(uintptr_t)d_row,
-                           (int64_t)(uintptr_t)d_off, (int64_t)ctx->mlp_loaded, ctx->pull_item,
-                           ctx->pull_item_min};
+                           (int64_t)(uintptr_t)d_off, (int64_t)ctx->mlp_loaded,
+                           ((int64_t)ctx->pull_item << 32) | (uint32_t)ctx->pull_item_min,
+                           ((int64_t)ctx->pull_block_tiles << 32) | (ctx->pull_dense_num << 16) | ctx->pull_dense_den};
   const bool same = ctx->batch_exec && memcmp(key, ctx->batch_key, sizeof(key)) == 0;
   TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[4], ctx->stream));
   if (!same) {

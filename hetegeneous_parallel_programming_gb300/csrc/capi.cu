@@ -269,6 +269,106 @@ tc_status tc_autotune_pull(tc_ctx *ctx, const tc_csr *g, const tc_opts *opts, co
   return TC_OK;
 }
 
+tc_status tc_get_tuning(const tc_ctx *ctx, tc_tuning *out) {
+  if (!ctx || !out) return set_error(nullptr, TC_ERR_INVALID_ARG, "null ctx or tuning");
+  out->pull_item = ctx->pull_item;
+  out->pull_item_min = ctx->pull_item_min;
+  out->pull_block_tiles = ctx->pull_block_tiles;
+  out->pull_dense_num = ctx->pull_dense_num;
+  out->pull_dense_den = ctx->pull_dense_den;
+  out->orient_blocks_per_sm = ctx->orient_blocks_per_sm;
+  return TC_OK;
+}
+
+tc_status tc_set_tuning(tc_ctx *ctx, const tc_tuning *t) {
+  if (!ctx || !t) return set_error(ctx, TC_ERR_INVALID_ARG, "null ctx or tuning");
+  if (t->pull_item_min < 32 || t->pull_item < t->pull_item_min || t->pull_item > 65536)
+    return set_error(ctx, TC_ERR_INVALID_ARG, "PULL chunks need 32 <= item_min <= item <= 65536");
+  if (t->pull_block_tiles < 64 || t->pull_block_tiles > (1 << 20))
+    return set_error(ctx, TC_ERR_INVALID_ARG, "pull_block_tiles %d outside [64, 2^20]", (int)t->pull_block_tiles);
+  if (t->pull_dense_num < 1 || t->pull_dense_num > 64 || t->pull_dense_den < 1 || t->pull_dense_den > 64)
+    return set_error(ctx, TC_ERR_INVALID_ARG, "dense ratio terms outside [1, 64]");
+  if (t->orient_blocks_per_sm < 1 || t->orient_blocks_per_sm > 64)
+    return set_error(ctx, TC_ERR_INVALID_ARG, "orient_blocks_per_sm %d outside [1, 64]", (int)t->orient_blocks_per_sm);
+  ctx->pull_item = t->pull_item;
+  ctx->pull_item_min = t->pull_item_min;
+  ctx->pull_block_tiles = t->pull_block_tiles;
+  ctx->pull_dense_num = t->pull_dense_num;
+  ctx->pull_dense_den = t->pull_dense_den;
+  ctx->orient_blocks_per_sm = t->orient_blocks_per_sm;
+  return TC_OK;
+}
+
+tc_status tc_autotune(tc_ctx *ctx, const tc_csr *g, const tc_opts *opts, int32_t reps, tc_tuning *best,
+                      float *best_ms, int32_t *trials) {
+  if (!ctx || !g || reps < 1) return set_error(ctx, TC_ERR_INVALID_ARG, "need ctx, graph and reps >= 1");
+  tc_tuning old, cur;
+  TC_TRY(tc_get_tuning(ctx, &old));
+  cur = old;
+  uint64_t first_total = 0;
+  bool have_total = false;
+  int32_t ntrials = 0;
+  // time one setting: a warm-up call, then the best of `reps` calls
+  auto trial = [&](const tc_tuning &t, float *ms_out) -> tc_status {
+    TC_TRY(tc_set_tuning(ctx, &t));
+    float best_t = 0.f;
+    for (int32_t r = 0; r <= reps; ++r) {
+      uint64_t total = 0;
+      tc_stats st;
+      TC_TRY(tc_count(ctx, g, opts, &total, nullptr, 0, &st));
+      if (!have_total) {
+        first_total = total;
+        have_total = true;
+      }
+      if (total != first_total)
+        return set_error(ctx, TC_ERR_INVALID_GRAPH, "a tuning trial counted %llu triangles, the first %llu",
+                         (unsigned long long)total, (unsigned long long)first_total);
+      if (r > 0 && (best_t == 0.f || st.ms_total < best_t)) best_t = st.ms_total;
+    }
+    ++ntrials;
+    *ms_out = best_t;
+    return TC_OK;
+  };
+  float cur_ms = 0.f;
+  tc_status s = trial(cur, &cur_ms);
+  for (int dim = 0; s == TC_OK && dim < 4; ++dim) {
+    for (int c = 0; s == TC_OK && c < 3; ++c) {
+      tc_tuning t = cur;
+      if (dim == 0) {
+        static const int items[3] = {256, 512, 1024};
+        t.pull_item = items[c];
+        t.pull_item_min = std::max(32, items[c] / 4);
+      } else if (dim == 1) {
+        static const int tiles[3] = {1280, 2560, 5120};
+        t.pull_block_tiles = tiles[c];
+      } else if (dim == 2) {
+        static const int num[3] = {1, 1, 2}, den[3] = {2, 1, 1};
+        t.pull_dense_num = num[c];
+        t.pull_dense_den = den[c];
+      } else {
+        static const int bps[3] = {3, 6, 12};
+        t.orient_blocks_per_sm = bps[c];
+      }
+      if (memcmp(&t, &cur, sizeof(t)) == 0) continue;  // already timed
+      float ms = 0.f;
+      s = trial(t, &ms);
+      if (s == TC_OK && ms < cur_ms) {
+        cur = t;
+        cur_ms = ms;
+      }
+    }
+  }
+  if (s != TC_OK) {
+    (void)tc_set_tuning(ctx, &old);
+    return s;
+  }
+  TC_TRY(tc_set_tuning(ctx, &cur));
+  if (best) *best = cur;
+  if (best_ms) *best_ms = cur_ms;
+  if (trials) *trials = ntrials;
+  return TC_OK;
+}
+
 tc_status tc_l2_bandwidth(tc_ctx *ctx, int64_t bytes, int32_t passes, double *gbs) {
   if (!ctx || !gbs || bytes < 4096 || passes < 1)
     return set_error(ctx, TC_ERR_INVALID_ARG, "need ctx, gbs, bytes >= 4096 and passes >= 1");

@@ -1241,17 +1241,10 @@ constexpr int PL_UNROLL = 4;      // table build: list loads in flight per lane
 constexpr int PL_GUNROLL = TC_PL_GUNROLL;  // flattened probing: 16-byte loads in flight per lane
 constexpr int PL_GROUP_THREADS = 256;
 // Dense edges: an edge u->v whose source is a hub and whose row suffix holds
-// more than PL_DENSE_NUM / PL_DENSE_DEN entries per 32-bit word of v's
-// bitmap table is counted by ANDing u's hub bit row with the table, 32
-// candidates per word, instead of probing the suffix entry by entry.
-#ifndef TC_PL_DENSE_NUM
-#define TC_PL_DENSE_NUM 1
-#endif
-#ifndef TC_PL_DENSE_DEN
-#define TC_PL_DENSE_DEN 1
-#endif
-constexpr int PL_DENSE_NUM = TC_PL_DENSE_NUM;
-constexpr int PL_DENSE_DEN = TC_PL_DENSE_DEN;
+// more than dense_num / dense_den entries per 32-bit word of v's bitmap
+// table (ctx->pull_dense_num / pull_dense_den, 1/1 unless tuned) is counted
+// by ANDing u's hub bit row with the table, 32 candidates per word, instead
+// of probing the suffix entry by entry.
 // Dense edges join two of the top PL_DENSE_HUB ids; their bit rows take
 // PL_DENSE_HUB^2 / 8 bytes (512 MB).
 constexpr int64_t PL_DENSE_HUB = 65536;
@@ -1268,7 +1261,8 @@ constexpr int PL_DUNROLL = 2;  // dense edges: 16-byte word loads in flight per 
 // table) is grouped over all blocks at once, key B * PL_HUB + v, so its runs
 // are not split block by block.
 constexpr int64_t PL_HUB = (int64_t)PL_WORDS * 32;  // 65536
-constexpr int64_t PL_BLOCK_TILES = 2560;            // 10.5M edges, 42 MB of adjacency
+// tiles per source block: ctx->pull_block_tiles (default 2560 tiles = 10.5M
+// edges, 42 MB of adjacency; tc_tuning)
 constexpr int PL_MAX_BLOCKS = 64;
 
 
@@ -1363,6 +1357,7 @@ struct PullDense {
   int32_t hub0;
   int woff4, tw4;
   int64_t hub_e0;  // first edge of the hub rows (rowptr[hub0])
+  int dnum, dden;  // dense when suffix entries * dden > dnum * 32-bit words of the table
 };
 
 template <bool BITMAP, bool PER_EDGE, bool TOP, bool DENSE>
@@ -1401,7 +1396,7 @@ __device__ __forceinline__ void pull_run(const DevDag &g, const uint2 *__restric
     }
     bool dense = false;
     if (DENSE) {  // counted by the word loop below instead of probed; hub rows own edges [hub_e0, m)
-      dense = e >= pd.hub_e0 && (int64_t)na * PL_DENSE_DEN > (int64_t)PL_DENSE_NUM * 4 * pd.tw4;
+      dense = e >= pd.hub_e0 && (int64_t)na * pd.dden > (int64_t)pd.dnum * 4 * pd.tw4;
       if (dense) na = 0;
     }
     const uintptr_t A = reinterpret_cast<uintptr_t>(g.col + a0);
@@ -1559,7 +1554,8 @@ template <int MODE>
 __global__ void __launch_bounds__(PL_THREADS, TC_PL_MIN_BLOCKS) pull_kernel(DevDag g, const uint2 *__restrict__ er,
                                                          const unsigned *__restrict__ npull,
                                                          unsigned *head, uint32_t *out, unsigned long long *total,
-                                                         unsigned long long *tile_cycles, int item, int item_min) {
+                                                         unsigned long long *tile_cycles, int item, int item_min,
+                                                         int dense_num, int dense_den) {
   __shared__ __align__(16) uint32_t tab[PL_WARPS][PL_ROW];
   __shared__ PullBatch s_batch[PL_WARPS];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -1599,7 +1595,7 @@ __global__ void __launch_bounds__(PL_THREADS, TC_PL_MIN_BLOCKS) pull_kernel(DevD
       // dense edges need the table aligned with the hub bit rows: the base goes
       // down to a 128-id boundary counted from hub0 (a hub target's list lies
       // in (v, n), so the window still fits)
-      PullDense pd{hub0, 0, 0, hub_e0};
+      PullDense pd{hub0, 0, 0, hub_e0, dense_num, dense_den};
       bool dense_run = MODE != 1 && g.hub_bits != nullptr && bitmap && nb > 0 && v >= hub0;
       if (dense_run) {
         const int32_t bmax = bmin + (int32_t)span - 1;
@@ -1770,10 +1766,10 @@ tc_status init_arm_occupancy(tc_ctx *ctx) {
   return TC_OK;
 }
 
-static int64_t pull_key_count(int64_t n, int64_t T, PullKeys *pk);
+static int64_t pull_key_count(int64_t n, int64_t T, int block_tiles, PullKeys *pk);
 
 static size_t count_sort_scratch_bytes(const tc_ctx *ctx, int64_t n, int64_t T) {
-  return std::max(radix_sort_scratch_bytes(ctx, T > 0 ? T : 1), scan_scratch_bytes(ctx, pull_key_count(n, T, nullptr) + 1));
+  return std::max(radix_sort_scratch_bytes(ctx, T > 0 ? T : 1), scan_scratch_bytes(ctx, pull_key_count(n, T, ctx->pull_block_tiles, nullptr) + 1));
 }
 
 // Hub bit rows: one row per dense hub (the top min(n, PL_DENSE_HUB) ids), each
@@ -1795,7 +1791,7 @@ size_t count_scratch_bytes(const tc_ctx *ctx, int64_t n, int64_t m) {
   sz.take<unsigned long long>(T);
   sz.take<unsigned long long>(T);
   sz.take<unsigned long long>(TC_NUM_ARMS);
-  sz.take<uint32_t>(pull_key_count(n, T, nullptr) + 1);
+  sz.take<uint32_t>(pull_key_count(n, T, ctx->pull_block_tiles, nullptr) + 1);
   sz.take<uint2>(m);
   sz.take<uint4>(hub_bits_words4(n));
   return sz.used + count_sort_scratch_bytes(ctx, n, T) + 256;
@@ -1814,7 +1810,7 @@ tc_status count_carve(const tc_ctx *ctx, int64_t n, int64_t m, Bump &bump, Count
   cb.tile_cycles = want_cycles ? cyc : nullptr;
   cb.tile_bytes = bump.take<unsigned long long>(T);
   cb.arm_bytes = bump.take<unsigned long long>(TC_NUM_ARMS);
-  cb.pull_pos = bump.take<uint32_t>(pull_key_count(n, T, nullptr) + 1);
+  cb.pull_pos = bump.take<uint32_t>(pull_key_count(n, T, ctx->pull_block_tiles, nullptr) + 1);
   cb.pull_er = bump.take<uint2>(m);
   cb.hub_bits = bump.take<uint4>(hub_bits_words4(n));
   cb.sort_scratch = bump.take<char>((int64_t)count_sort_scratch_bytes(ctx, n, T));
@@ -1829,8 +1825,8 @@ static_assert(PIN_BYTES + TC_NUM_ARMS <= 64, "pinned scratch holds 64 words");
 static_assert(sizeof(((tc_ctx *)nullptr)->ev) / sizeof(cudaEvent_t) >= 10 + TC_NUM_ARMS, "one event per arm");
 
 // Number of keys of the PULL grouping of a graph with n vertices and T tiles.
-static int64_t pull_key_count(int64_t n, int64_t T, PullKeys *pk) {
-  const int64_t per_block = std::max<int64_t>(PL_BLOCK_TILES, (T + PL_MAX_BLOCKS - 1) / PL_MAX_BLOCKS);
+static int64_t pull_key_count(int64_t n, int64_t T, int block_tiles, PullKeys *pk) {
+  const int64_t per_block = std::max<int64_t>(block_tiles, (T + PL_MAX_BLOCKS - 1) / PL_MAX_BLOCKS);
   const int64_t blocks = std::max<int64_t>(1, (T + per_block - 1) / per_block);
   if (pk) {
     pk->hub_span = PL_HUB;
@@ -1877,7 +1873,7 @@ __global__ void hub_bits_kernel(DevDag g, int32_t hub0, int wpr4, const unsigned
 
 static tc_status run_pull(tc_ctx *ctx, const DevDag &g_in, CountBufs &cb, uint32_t *out, int64_t T, bool timing) {
   PullKeys pk;
-  const int64_t K = pull_key_count(g_in.n, T, &pk);
+  const int64_t K = pull_key_count(g_in.n, T, ctx->pull_block_tiles, &pk);
   unsigned *pos = cb.pull_pos;
   const int gblocks = (int)std::min<int64_t>(T, (int64_t)ctx->num_sms * 8);
   TC_TRY(exclusive_scan_u32(ctx, cb.pull_pos, cb.pull_pos, K + 1, cb.sort_scratch));
@@ -1905,15 +1901,15 @@ static tc_status run_pull(tc_ctx *ctx, const DevDag &g_in, CountBufs &cb, uint32
   if (g.top)
     pull_kernel<1><<<grid, PL_THREADS, 0, ctx->stream>>>(g, cb.pull_er, pos + K, ctx->d_heads + TC_ARM_PULL, out,
                                                         ctx->d_total, cb.tile_cycles, ctx->pull_item,
-                                                        ctx->pull_item_min);
+                                                        ctx->pull_item_min, ctx->pull_dense_num, ctx->pull_dense_den);
   else if (g.vlabel)
     pull_kernel<2><<<grid, PL_THREADS, 0, ctx->stream>>>(g, cb.pull_er, pos + K, ctx->d_heads + TC_ARM_PULL, out,
                                                         ctx->d_total, cb.tile_cycles, ctx->pull_item,
-                                                        ctx->pull_item_min);
+                                                        ctx->pull_item_min, ctx->pull_dense_num, ctx->pull_dense_den);
   else
     pull_kernel<0><<<grid, PL_THREADS, 0, ctx->stream>>>(g, cb.pull_er, pos + K,
                                                     ctx->d_heads + TC_ARM_PULL, out, ctx->d_total, cb.tile_cycles, ctx->pull_item,
-                                                        ctx->pull_item_min);
+                                                        ctx->pull_item_min, ctx->pull_dense_num, ctx->pull_dense_den);
   TC_CHECK_LAUNCH(ctx);
   if (timing) {
     TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[11 + TC_NUM_ARMS], ctx->stream));
@@ -1938,7 +1934,7 @@ tc_status run_count(tc_ctx *ctx, const DevDag &g_in, const tc_opts &opts, CountB
     const int plan_blocks = (int)((T + (PLAN_THREADS / 32) - 1) / (PLAN_THREADS / 32));
     const size_t plan_smem = opts.selector == TC_SELECT_LEARNED ? TC_MLP_PARAM_COUNT * sizeof(float) : 0;
     PullKeys pk;
-    const int64_t K = pull_key_count(g.n, T, &pk);
+    const int64_t K = pull_key_count(g.n, T, ctx->pull_block_tiles, &pk);
     TC_CHECK_CUDA(ctx, cudaMemsetAsync(cb.pull_pos, 0, sizeof(uint32_t) * (K + 1), ctx->stream));
     plan_kernel<<<plan_blocks, PLAN_THREADS, plan_smem, ctx->stream>>>(g, T, opts.selector, opts.force_arm,
                                                                        ctx->d_mlp, cb.features, cb.arm, cb.qkeys0,

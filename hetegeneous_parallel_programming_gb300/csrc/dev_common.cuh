@@ -51,6 +51,11 @@ struct tc_ctx {
   // smallest; tc_set_pull_chunks / tc_autotune_pull change them
   int pull_item = 512;
   int pull_item_min = 128;
+  // tc_tuning: PULL source-block size (tiles), dense-edge ratio, and the
+  // orientation passes' entry-chunk geometry (blocks per SM)
+  int pull_block_tiles = 2560;
+  int pull_dense_num = 1, pull_dense_den = 1;
+  int orient_blocks_per_sm = 6;
   // captured back half of the batched pipeline (batch.cu), keyed by shape,
   // options and the buffers it reads
   cudaGraphExec_t batch_exec = nullptr;

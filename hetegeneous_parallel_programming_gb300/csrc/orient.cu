@@ -16,7 +16,8 @@ constexpr int OR_PER = ENTRY_TILE / OR_THREADS;  // 8 entries per thread per til
 
 void orient_geometry(const tc_ctx *ctx, int64_t nnz, int pieces, int *G, int64_t *chunk) {
   int64_t tiles = (nnz + ENTRY_TILE - 1) / ENTRY_TILE;
-  int64_t g = (int64_t)ctx->num_sms * 6 * pieces;  // resident at once: 6 blocks of 256 per SM
+  // blocks of 256 per SM in the entry-chunk geometry (6 are resident at once)
+  int64_t g = (int64_t)ctx->num_sms * ctx->orient_blocks_per_sm * pieces;
   if (g > tiles) g = tiles;
   if (g < 1) g = 1;
   *chunk = ((tiles + g - 1) / g) * ENTRY_TILE;

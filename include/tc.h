@@ -205,6 +205,47 @@ tc_status tc_get_pull_chunks(const tc_ctx *ctx, int32_t *item, int32_t *item_min
 tc_status tc_autotune_pull(tc_ctx *ctx, const tc_csr *g, const tc_opts *opts, const int32_t *candidates,
                            int32_t ncand, int32_t reps, float *ms, int32_t *best);
 
+/* Run-time tuning of one ctx.  Results never depend on it; speed does, per
+ * graph.
+ *   pull_item, pull_item_min  PULL work chunks (tc_set_pull_chunks)
+ *   pull_block_tiles          4096-edge tiles per PULL source block: the hub
+ *                             targets' in-edges are grouped per block of rows
+ *                             so that the rows they probe stay in L2
+ *                             (default 2560 = 42 MB of adjacency)
+ *   pull_dense_num / _den     a hub-hub edge is counted by ANDing bit rows
+ *                             when its row suffix holds more than num/den
+ *                             entries per 32-bit word of the target's bitmap
+ *                             (default 1/1)
+ *   orient_blocks_per_sm      entry-chunk geometry of the orientation passes:
+ *                             chunks per SM of the kept-count and placement
+ *                             passes (default 6, the blocks resident per SM)
+ * This replaces the reference's fixed launch shape (multigpu.cu:203-206,
+ * grid from BLOCK_SIZE and the vertex count). */
+typedef struct tc_tuning {
+  int32_t pull_item, pull_item_min;
+  int32_t pull_block_tiles;
+  int32_t pull_dense_num, pull_dense_den;
+  int32_t orient_blocks_per_sm;
+} tc_tuning;
+
+tc_status tc_get_tuning(const tc_ctx *ctx, tc_tuning *out);
+/* Checks ranges: 32 <= item_min <= item <= 65536, 64 <= block_tiles <=
+ * 1<<20, 1 <= dense_num, dense_den <= 64, 1 <= orient_blocks_per_sm <= 64. */
+tc_status tc_set_tuning(tc_ctx *ctx, const tc_tuning *t);
+
+/* Autotuner for the ctx's tuning: coordinate descent over the PULL chunk
+ * size (256, 512, 1024), the source-block size (1280, 2560, 5120 tiles),
+ * the dense ratio (1/2, 1/1, 2/1) and the orientation geometry (3, 6, 12
+ * chunks per SM), one dimension at a time with the others at their best so
+ * far.  Every trial counts g (the tc_count contract) once to warm up and
+ * `reps` times, keeping the best device time (CUDA events on the ctx
+ * stream); every trial must count the same triangles, else
+ * TC_ERR_INVALID_GRAPH is returned and the ctx keeps its previous tuning.
+ * best (optional) receives the chosen tuning, *best_ms its time and
+ * *trials (optional) the number of settings timed. */
+tc_status tc_autotune(tc_ctx *ctx, const tc_csr *g, const tc_opts *opts, int32_t reps, tc_tuning *best,
+                      float *best_ms, int32_t *trials);
+
 /* ---- measurement ---------------------------------------------------------- */
 
 /* L2 read ceiling of the ctx's GPU: one kernel reads a device buffer of

@@ -187,6 +187,41 @@ def test_pull_chunk_sizes_and_autotune(engine):
         engine.set_pull_chunks(*old)
 
 
+def test_tuning_changes_speed_not_counts(engine):
+    """Every tc_tuning field (PULL chunks, source-block size, dense ratio,
+    orientation geometry) leaves totals and per-edge counts bit-exact, on a
+    graph whose PULL edges span several source blocks; the autotuner keeps a
+    valid setting; out-of-range settings are rejected."""
+    rowptr, colidx = gen_csr(tc.GenSpec("rmat", scale=19, edge_factor=16, seed=8))
+    ref, ref_pe, _, _ = oracle.triangles(rowptr, colidx, per_edge=True)
+    old = engine.get_tuning()
+    assert old == {"pull_item": 512, "pull_item_min": 128, "pull_block_tiles": 2560, "pull_dense_num": 1,
+                   "pull_dense_den": 1, "orient_blocks_per_sm": 6}
+    vtx_off = np.array([0, len(rowptr) - 1], np.int64)
+    try:
+        for kw in (dict(pull_block_tiles=64), dict(pull_block_tiles=300, pull_dense_num=1, pull_dense_den=8),
+                   dict(pull_dense_num=8, pull_dense_den=1, orient_blocks_per_sm=1),
+                   dict(orient_blocks_per_sm=64, pull_item=64, pull_item_min=32)):
+            engine.set_tuning(**old)
+            engine.set_tuning(**kw)
+            for sel, arm in (("fixed", None), ("force", tc.ARM_NAMES.index("pull"))):
+                total, pe, _ = engine.count(rowptr, colidx, selector=sel, force_arm=arm, edge_counts=True)
+                assert total == ref and np.array_equal(pe, ref_pe), (kw, sel)
+                assert engine.count(rowptr, colidx, selector=sel, force_arm=arm)[0] == ref, (kw, sel, "total")
+            assert engine.batch_count(vtx_off, rowptr, colidx)[0].tolist() == [ref], kw
+        engine.set_tuning(**old)
+        best, ms, trials = engine.autotune(rowptr, colidx, reps=1)
+        assert trials >= 5 and ms > 0 and engine.get_tuning() == best
+        assert engine.count(rowptr, colidx)[0] == ref
+        for bad in (dict(pull_block_tiles=10), dict(pull_dense_num=0), dict(orient_blocks_per_sm=100),
+                    dict(pull_item=16, pull_item_min=16)):
+            with pytest.raises(tc.TCError):
+                engine.set_tuning(**bad)
+        assert engine.get_tuning() == best  # a rejected setting changes nothing
+    finally:
+        engine.set_tuning(**old)
+
+
 def test_pull_dense_core(engine):
     """A 3000-vertex core with edge probability 1/2 inside a sparse 200 000-vertex
     graph: the core vertices are the top-ranked hubs and their row suffixes are
