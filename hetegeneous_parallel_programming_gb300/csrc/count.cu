@@ -62,7 +62,8 @@ __device__ __forceinline__ int fixed_select(const PlanStats &s) {
 // MLP cost model (16 -> 64 -> 64 -> arms, ReLU); weights staged in shared
 // memory rounded to bf16, fp32 accumulation.  Returns the arm with the lowest
 // predicted cost.
-__device__ int mlp_select(const float *__restrict__ w, const float *f, int lane) {
+// The arm of lowest predicted cost, `exclude` (an arm, or -1) left out.
+__device__ int mlp_select(const float *__restrict__ w, const float *f, int lane, int exclude) {
   const float *W1 = w, *b1 = W1 + TC_MLP_FEATURES * TC_MLP_HIDDEN;
   const float *W2 = b1 + TC_MLP_HIDDEN, *b2 = W2 + TC_MLP_HIDDEN * TC_MLP_HIDDEN;
   const float *W3 = b2 + TC_MLP_HIDDEN, *b3 = W3 + TC_MLP_HIDDEN * TC_NUM_ARMS;
@@ -85,13 +86,14 @@ __device__ int mlp_select(const float *__restrict__ w, const float *f, int lane)
     }
     h2[q] = fmaxf(a, 0.f);
   }
-  int best = 0;
+  int best = -1;
   float bestv = 0.f;
 #pragma unroll
   for (int k = 0; k < TC_NUM_ARMS; ++k) {
     float p = h2[0] * W3[lane * TC_NUM_ARMS + k] + h2[1] * W3[(lane + 32) * TC_NUM_ARMS + k];
     p = warp_sum(p) + b3[k];
-    if (k == 0 || p < bestv) { bestv = p; best = k; }
+    if (k == exclude) continue;
+    if (best < 0 || p < bestv) { bestv = p; best = k; }
   }
   return best;
 }
@@ -198,8 +200,17 @@ __global__ void __launch_bounds__(PLAN_THREADS) plan_kernel(DevDag g, int64_t T,
   f[15] = flog2p1((float)g.m) / 32.f;  // graph size: how much of it the L2 can hold
   int arm;
   if (selector == TC_SELECT_FORCE) arm = force_arm;
-  else if (selector == TC_SELECT_LEARNED) arm = mlp_select(s_w, f, lane);
-  else arm = fixed_select(st);
+  else if (selector == TC_SELECT_LEARNED) {
+    // The fixed rule keeps the PULL decision: a PULL tile's cost depends on
+    // how many of its targets' in-edges other PULL tiles share (the table
+    // build is spread over them), which per-tile costs profiled one arm at a
+    // time cannot show.  The cost model picks among the per-edge arms for
+    // every other tile.
+    const int fx = __shfl_sync(TC_FULL_MASK, fixed_select(st), 0);
+    arm = fx == TC_ARM_PULL ? TC_ARM_PULL : mlp_select(s_w, f, lane, TC_ARM_PULL);
+  } else {
+    arm = fixed_select(st);
+  }
   arm = __shfl_sync(TC_FULL_MASK, arm, 0);
   if (lane < TC_MLP_FEATURES) feats[t * TC_MLP_FEATURES + lane] = f[lane];
   if (arm == TC_ARM_PULL)
@@ -279,6 +290,36 @@ __device__ __forceinline__ int64_t next_tile(const uint32_t *__restrict__ qtiles
   const int64_t t = *s_tile;
   __syncthreads();
   return t;
+}
+
+// The group arms (BSEARCH_G, MERGE_G, GALLOP_G, MPATH_G) take their tiles in
+// GROUP_SUBS pieces (512 edges each), so an arm that gets a few heavy tiles
+// spreads them over several blocks instead of leaving one block to finish a
+// whole tile while the rest of the GPU waits.
+#ifndef TC_GROUP_SUBS
+#define TC_GROUP_SUBS 8
+#endif
+constexpr int GROUP_SUBS = TC_GROUP_SUBS;
+
+// Next piece of this arm's queue (block-uniform): its tile and edge range.
+__device__ __forceinline__ bool next_sub_tile(const uint32_t *__restrict__ qtiles, int64_t qb, int64_t qn,
+                                              unsigned *head, int64_t *s_item, int64_t m, int64_t *tile,
+                                              int64_t *e0, int64_t *e1) {
+  if (threadIdx.x == 0) {
+    const unsigned it = atomicAdd(head, 1u);
+    *s_item = (int64_t)it < qn * GROUP_SUBS
+                  ? (int64_t)qtiles[qb + it / GROUP_SUBS] * GROUP_SUBS + (int64_t)(it % GROUP_SUBS)
+                  : -1;
+  }
+  __syncthreads();
+  const int64_t item = *s_item;
+  __syncthreads();
+  if (item < 0) return false;
+  constexpr int64_t SUB = TILE_EDGES / GROUP_SUBS;
+  *tile = item / GROUP_SUBS;
+  *e0 = *tile * TILE_EDGES + (item % GROUP_SUBS) * SUB;
+  *e1 = min(m, *e0 + SUB);
+  return true;
 }
 
 __device__ __forceinline__ void flush_total(unsigned long long acc, unsigned long long *total) {
@@ -419,10 +460,9 @@ __global__ void __launch_bounds__(CT_THREADS) bsearch_kernel(DevDag g, const uin
   const unsigned gm = group_mask<G>(lane);
   unsigned long long acc = 0;
   for (;;) {
-    const int64_t tile = next_tile(qtiles, qb, qn, head, &s_tile);
-    if (tile < 0) break;
+    int64_t tile, e0, e1;
+    if (!next_sub_tile(qtiles, qb, qn, head, &s_tile, g.m, &tile, &e0, &e1)) break;
     const long long c0 = clock64();
-    const int64_t e0 = tile * TILE_EDGES, e1 = min(g.m, e0 + TILE_EDGES);
     for (int64_t e = e0 + gid; e < e1; e += NG) {
       int32_t s;
       const EdgeLists L = edge_lists(g, e, s);
@@ -556,10 +596,9 @@ __global__ void __launch_bounds__(CT_THREADS) bsearch_tma_kernel(DevDag g, const
   bool pending[2] = {false, false};
   unsigned long long acc = 0;
   for (;;) {
-    const int64_t tile = next_tile(qtiles, qb, qn, head, &s_tile);
-    if (tile < 0) break;
+    int64_t tile, e0, e1;
+    if (!next_sub_tile(qtiles, qb, qn, head, &s_tile, g.m, &tile, &e0, &e1)) break;
     const long long c0 = clock64();
-    const int64_t e0 = tile * TILE_EDGES, e1 = min(g.m, e0 + TILE_EDGES);
     int cur = 0;
     int64_t e = e0 + w;
     BtEdge b = {};
@@ -647,10 +686,9 @@ __global__ void __launch_bounds__(CT_THREADS) merge_kernel(DevDag g, const uint3
   const unsigned gm = group_mask<G>(lane);
   unsigned long long acc = 0;
   for (;;) {
-    const int64_t tile = next_tile(qtiles, qb, qn, head, &s_tile);
-    if (tile < 0) break;
+    int64_t tile, e0, e1;
+    if (!next_sub_tile(qtiles, qb, qn, head, &s_tile, g.m, &tile, &e0, &e1)) break;
     const long long c0 = clock64();
-    const int64_t e0 = tile * TILE_EDGES, e1 = min(g.m, e0 + TILE_EDGES);
     for (int64_t e = e0 + gid; e < e1; e += NG) {
       int32_t s;
       const EdgeLists L = edge_lists(g, e, s);
@@ -734,10 +772,9 @@ __global__ void __launch_bounds__(CT_THREADS) gallop_kernel(DevDag g, const uint
   const unsigned gm = group_mask<G>(lane);
   unsigned long long acc = 0;
   for (;;) {
-    const int64_t tile = next_tile(qtiles, qb, qn, head, &s_tile);
-    if (tile < 0) break;
+    int64_t tile, e0, e1;
+    if (!next_sub_tile(qtiles, qb, qn, head, &s_tile, g.m, &tile, &e0, &e1)) break;
     const long long c0 = clock64();
-    const int64_t e0 = tile * TILE_EDGES, e1 = min(g.m, e0 + TILE_EDGES);
     for (int64_t e = e0 + gid; e < e1; e += NG) {
       int32_t s;
       const EdgeLists L = edge_lists(g, e, s);
@@ -820,10 +857,9 @@ __global__ void __launch_bounds__(CT_THREADS) mpath_kernel(DevDag g, const uint3
   const unsigned gm = group_mask<G>(lane);
   unsigned long long acc = 0;
   for (;;) {
-    const int64_t tile = next_tile(qtiles, qb, qn, head, &s_tile);
-    if (tile < 0) break;
+    int64_t tile, e0, e1;
+    if (!next_sub_tile(qtiles, qb, qn, head, &s_tile, g.m, &tile, &e0, &e1)) break;
     const long long c0 = clock64();
-    const int64_t e0 = tile * TILE_EDGES, e1 = min(g.m, e0 + TILE_EDGES);
     for (int64_t e = e0 + gid; e < e1; e += NG) {
       int32_t s;
       const EdgeLists L = edge_lists(g, e, s);

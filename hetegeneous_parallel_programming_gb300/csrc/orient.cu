@@ -13,6 +13,18 @@ namespace tc {
 
 constexpr int OR_THREADS = 256;
 constexpr int OR_PER = ENTRY_TILE / OR_THREADS;  // 8 entries per thread per tile
+// 1: the placement writes every relabelled entry's row (nsrc) next to its
+// column; 0: a streaming pass derives the rows from the relabelled row
+// pointers afterwards (sequential writes instead of scattered ones)
+#ifndef TC_PLACE_SRC
+#define TC_PLACE_SRC 1
+#endif
+constexpr bool PLACE_SRC = TC_PLACE_SRC != 0;
+// 1: rows of <= 32 entries are sorted by a warp per 32 consecutive rows
+#ifndef TC_SEG_WARP_CHUNK
+#define TC_SEG_WARP_CHUNK 1
+#endif
+constexpr bool SEG_WARP_CHUNK = TC_SEG_WARP_CHUNK != 0;
 
 void orient_geometry(const tc_ctx *ctx, int64_t nnz, int pieces, int *G, int64_t *chunk) {
   int64_t tiles = (nnz + ENTRY_TILE - 1) / ENTRY_TILE;
@@ -380,7 +392,7 @@ __global__ void __launch_bounds__(OR_THREADS, 6) place_kernel(const int64_t *__r
           const int32_t ru = rank[u];
           const long long dst = nrowptr[ru] + (p - orowptr[u]);
           ncol[dst] = rv[k];
-          nsrc[dst] = ru;
+          if (PLACE_SRC) nsrc[dst] = ru;
           if (VALS) perm[dst] = (uint32_t)p;
         }
         if (DAGCOL) dag_col[p] = vv[k];
@@ -534,6 +546,72 @@ __global__ void seg_sort_warp_kernel(const int64_t *__restrict__ nrowptr, int64_
     if (lane < L) {
       ncol[b + lane] = key;
       if (VALS) perm[b + lane] = val;
+    }
+  }
+}
+
+// The same sort with a warp per 32 consecutive rows: the warp reads their 33
+// row pointers with one coalesced load, then sorts the rows one after
+// another, loading the next row while it sorts the current one, so a row
+// costs one memory round trip instead of the two dependent ones (its
+// pointers, then its entries) of a warp per row.
+template <bool VALS>
+__device__ __forceinline__ void warp_sort32(int32_t &key, uint32_t &val, int L, int lane) {
+  int P = 2;  // levels up to the row's padded length only (warp-uniform)
+  while (P < L) P <<= 1;
+#pragma unroll
+  for (int k = 2; k <= 32; k <<= 1) {
+    if (k > P) break;
+    {
+      const int partner = lane ^ (k - 1);
+      const int32_t ok = __shfl_sync(TC_FULL_MASK, key, partner);
+      const uint32_t ov = VALS ? __shfl_sync(TC_FULL_MASK, val, partner) : 0u;
+      const bool take = lane < partner ? ok < key : ok > key;
+      if (take) { key = ok; if (VALS) val = ov; }
+    }
+#pragma unroll
+    for (int j = k >> 2; j >= 1; j >>= 1) {
+      const int partner = lane ^ j;
+      const int32_t ok = __shfl_sync(TC_FULL_MASK, key, partner);
+      const uint32_t ov = VALS ? __shfl_sync(TC_FULL_MASK, val, partner) : 0u;
+      const bool take = lane < partner ? ok < key : ok > key;
+      if (take) { key = ok; if (VALS) val = ov; }
+    }
+  }
+}
+
+template <bool VALS>
+__global__ void seg_sort_warp_chunk_kernel(const int64_t *__restrict__ nrowptr, int64_t n,
+                                           int32_t *__restrict__ ncol, uint32_t *__restrict__ perm) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t r0 = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; r0 < n; r0 += warps * 32) {
+    const int64_t rl = min(r0 + lane, n);  // lane's row start (row n: the end)
+    const int64_t lo_l = nrowptr[rl];
+    const int64_t hi_l = nrowptr[min(rl + 1, n)];
+    const int rows = (int)min<int64_t>(32, n - r0);
+    // prefetch the first row
+    int64_t b = __shfl_sync(TC_FULL_MASK, lo_l, 0);
+    int L = (int)(__shfl_sync(TC_FULL_MASK, hi_l, 0) - b);
+    int32_t key = (L >= 2 && L <= 32 && lane < L) ? ncol[b + lane] : INT32_MAX;
+    uint32_t val = (VALS && L >= 2 && L <= 32 && lane < L) ? perm[b + lane] : 0u;
+    for (int j = 0; j < rows; ++j) {
+      const int64_t bj = b;
+      const int Lj = L;
+      int32_t kj = key;
+      uint32_t vj = val;
+      if (j + 1 < rows) {  // next row's entries in flight while this one sorts
+        b = __shfl_sync(TC_FULL_MASK, lo_l, j + 1);
+        L = (int)(__shfl_sync(TC_FULL_MASK, hi_l, j + 1) - b);
+        key = (L >= 2 && L <= 32 && lane < L) ? ncol[b + lane] : INT32_MAX;
+        val = (VALS && L >= 2 && L <= 32 && lane < L) ? perm[b + lane] : 0u;
+      }
+      if (Lj < 2 || Lj > 32) continue;  // warp-uniform
+      warp_sort32<VALS>(kj, vj, Lj, lane);
+      if (lane < Lj) {
+        ncol[bj + lane] = kj;
+        if (VALS) perm[bj + lane] = vj;
+      }
     }
   }
 }
@@ -705,7 +783,11 @@ __global__ void __launch_bounds__(1024) seg_sort_global_kernel(const int64_t *__
 template <bool VALS>
 static tc_status launch_row_sorts(tc_ctx *ctx, const DevCSR &g, OrientBufs &b) {
   uint32_t *pv = VALS ? b.perm : nullptr;
-  seg_sort_warp_kernel<VALS><<<grid_for(ctx, g.n * 32, 256, 8), 256, 0, ctx->stream>>>(b.nrowptr, g.n, b.ncol, pv);
+  if (SEG_WARP_CHUNK)
+    seg_sort_warp_chunk_kernel<VALS><<<grid_for(ctx, g.n, 256, 8), 256, 0, ctx->stream>>>(b.nrowptr, g.n, b.ncol,
+                                                                                          pv);
+  else
+    seg_sort_warp_kernel<VALS><<<grid_for(ctx, g.n * 32, 256, 8), 256, 0, ctx->stream>>>(b.nrowptr, g.n, b.ncol, pv);
   TC_CHECK_LAUNCH(ctx);
   seg_sort_warpsmem_kernel<VALS><<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(b.nrowptr, b.mid_list, b.seg_counts,
                                                                             b.ncol, pv);
@@ -736,9 +818,10 @@ tc_status orient_phase_b(tc_ctx *ctx, const DevCSR &g, OrientBufs &b, int64_t m,
     TC_CHECK_LAUNCH(ctx);
   }
   if (!relabel) return TC_OK;
-  // place_kernel wrote every entry's row into nsrc; the row sorts keep
-  // entries inside their rows
+  // the row sorts keep entries inside their rows, so every entry's row
+  // (nsrc) is the same before and after them
   if (m > 1) TC_TRY(want_perm ? launch_row_sorts<true>(ctx, g, b) : launch_row_sorts<false>(ctx, g, b));
+  if (!PLACE_SRC) TC_TRY(launch_expand_src(ctx, b.nrowptr, g.n, m, b.nsrc));
   out->n = g.n;
   out->m = m;
   out->rowptr = b.nrowptr;

@@ -13,7 +13,9 @@ the tiles do the same work in the two regimes and only their costs differ
 device forward/backward/AdamW kernels (tc_selector_train).  Held-out graphs
 (other seeds, the default (0.57, 0.19, 0.19)) measure regret: the summed
 cost of the chosen arm per tile over the summed cost of the per-tile best
-arm, for the fixed-threshold selector and for the MLP.  Several candidates
+arm, for the fixed-threshold selector and for the learned selection as the
+engine makes it (PULL where the fixed rule picks PULL, else the MLP's
+cheapest per-edge arm).  Several candidates
 (seed x weight decay x epochs) are trained and the one with the lowest mean
 regret on the scale-21 and scale-22 held-out graphs and a held-out batch is
 kept; the scale-20 and scale-24 graphs (the latter is the benchmark graph)
@@ -58,6 +60,17 @@ def batch_union(num_graphs: int, seed: int):
     gid = np.repeat(np.arange(len(vtx_off) - 1), np.diff(vtx_off))
     shift = vtx_off[:-1][np.repeat(gid, np.diff(rowptr))]
     return rowptr.astype(np.int64), (colidx.astype(np.int64) + shift).astype(np.int32)
+
+
+PULL = tc.ARM_NAMES.index("pull")
+
+
+def hybrid_choice(pred: np.ndarray, fixed: np.ndarray) -> np.ndarray:
+    """The engine's learned selection: PULL where the fixed rule picks PULL,
+    else the per-edge arm of lowest predicted cost."""
+    masked = pred.copy()
+    masked[:, PULL] = np.inf
+    return np.where(fixed == PULL, PULL, masked.argmin(1))
 
 
 def regret(costs: np.ndarray, chosen: np.ndarray) -> float:
@@ -127,14 +140,14 @@ def main():
     for scale, seed in [(20, 5), (21, 6), (22, 7), (24, 0)]:
         r, cidx = rmat_graph(eng, scale, 0.57, 0.19, 0.19, seed=seed)
         f, k = eng.tile_profile(r, cidx)
-        held_graphs.append((scale, seed, r, cidx, f, k))
+        held_graphs.append((scale, seed, r, cidx, f, k, eng.plan_arms(r, cidx, selector="fixed")))
     # mixed small-graph batches of 4096 graphs: seed 3 validates, seed 1 (the
     # benchmark's batch) only reports; "scale" 0 marks a batch
     if args.batches:
         for seed in (3, 1):
             r, cidx = batch_union(4096, seed)
             f, k = eng.tile_profile(r, cidx)
-            held_graphs.append((0, seed, r, cidx, f, k))
+            held_graphs.append((0, seed, r, cidx, f, k, eng.plan_arms(r, cidx, selector="fixed")))
     t_prof = time.time() - t0
     t0 = time.time()
     validation = [g for g in held_graphs if g[0] in (21, 22) or (g[0] == 0 and g[1] == 3)]
@@ -144,7 +157,8 @@ def main():
         for wd in [float(x) for x in args.weight_decay.split(",")]:
             for sd in [int(x) for x in args.train_seeds.split(",")]:
                 loss = eng.train_selector(X, Y, epochs=ep, lr=args.lr, weight_decay=wd, seed=sd)
-                val = float(np.mean([regret(k, eng.selector_predict(f).argmin(1)) for _, _, _, _, f, k in validation]))
+                val = float(np.mean([regret(k, hybrid_choice(eng.selector_predict(f), fx))
+                                     for _, _, _, _, f, k, fx in validation]))
                 candidates.append({"epochs": ep, "weight_decay": wd, "seed": sd, "loss": loss, "val_regret": val})
                 if best is None or val < best[0]:
                     best = (val, eng.get_selector_weights(), candidates[-1])
@@ -153,10 +167,11 @@ def main():
     eng.set_selector_weights(w)
     loss = best[2]["loss"]
     pred = eng.selector_predict(X)
-    train_regret = {"learned": regret(Y, pred.argmin(1)), "fixed": regret(Y, np.concatenate(fixed))}
+    fixed_all = np.concatenate(fixed)
+    train_regret = {"learned": regret(Y, hybrid_choice(pred, fixed_all)), "fixed": regret(Y, fixed_all)}
     held = []
     held_sets = {}
-    for scale, seed, r, cidx, f, k in held_graphs:
+    for scale, seed, r, cidx, f, k, _ in held_graphs:
         learned = eng.plan_arms(r, cidx, selector="learned")
         fx = eng.plan_arms(r, cidx, selector="fixed")
         name = f"s{scale}" if scale else f"batch{seed}"
