@@ -603,16 +603,22 @@ class Engine:
 
     def load_shipped_selector(self) -> bool:
         """Loads the shipped MLP cost-model weights (data/selector_mlp.npz)
-        for selector="learned"; False when the file is absent or holds
-        weights for another arm set."""
+        and their switching margin for selector="learned"; False when the
+        file is absent or holds weights for another arm set."""
         path = Path(__file__).resolve().parent / "data" / "selector_mlp.npz"
         if not path.exists():
             return False
-        w = np.load(path)["params"].astype(np.float32)
+        z = np.load(path)
+        w = z["params"].astype(np.float32)
         if w.size != TC_MLP_PARAM_COUNT:
             return False
         self.set_selector_weights(w)
+        self.set_selector_margin(float(z["margin"]) if "margin" in z.files else 0.0)
         return True
+
+    def set_selector_margin(self, margin: float) -> None:
+        """log2-cost gain the learned selector needs to leave the fixed rule's arm."""
+        self._chk(self._L.tc_selector_set_margin(self._h, float(margin)))
 
     def get_selector_weights(self) -> np.ndarray:
         out = np.zeros(TC_MLP_PARAM_COUNT, np.float32)

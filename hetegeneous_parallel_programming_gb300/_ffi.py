@@ -129,6 +129,7 @@ _SIGS = {
     "tc_tile_profile": (C.c_int, [P, C.POINTER(Csr), P, P, I64, PI64]),
     "tc_plan_arms": (C.c_int, [P, C.POINTER(Csr), C.POINTER(Opts), P, I64, PI64]),
     "tc_selector_train": (C.c_int, [P, P, P, I64, I32, C.c_float, C.c_float, U64, PF]),
+    "tc_selector_set_margin": (C.c_int, [P, C.c_float]),
     "tc_selector_set_weights": (C.c_int, [P, P, I64]),
     "tc_selector_get_weights": (C.c_int, [P, P, I64]),
     "tc_selector_predict": (C.c_int, [P, P, I64, P]),

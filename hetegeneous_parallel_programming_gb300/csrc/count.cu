@@ -62,8 +62,10 @@ __device__ __forceinline__ int fixed_select(const PlanStats &s) {
 // MLP cost model (16 -> 64 -> 64 -> arms, ReLU); weights staged in shared
 // memory rounded to bf16, fp32 accumulation.  Returns the arm with the lowest
 // predicted cost.
-// The arm of lowest predicted cost, `exclude` (an arm, or -1) left out.
-__device__ int mlp_select(const float *__restrict__ w, const float *f, int lane, int exclude) {
+// The arm of lowest predicted cost, `exclude` (an arm, or -1) left out; it
+// replaces `keep` only when predicted at least `margin` (log2 cost) cheaper.
+__device__ int mlp_select(const float *__restrict__ w, const float *f, int lane, int exclude, int keep,
+                          float margin) {
   const float *W1 = w, *b1 = W1 + TC_MLP_FEATURES * TC_MLP_HIDDEN;
   const float *W2 = b1 + TC_MLP_HIDDEN, *b2 = W2 + TC_MLP_HIDDEN * TC_MLP_HIDDEN;
   const float *W3 = b2 + TC_MLP_HIDDEN, *b3 = W3 + TC_MLP_HIDDEN * TC_NUM_ARMS;
@@ -87,15 +89,16 @@ __device__ int mlp_select(const float *__restrict__ w, const float *f, int lane,
     h2[q] = fmaxf(a, 0.f);
   }
   int best = -1;
-  float bestv = 0.f;
+  float bestv = 0.f, keepv = 0.f;
 #pragma unroll
   for (int k = 0; k < TC_NUM_ARMS; ++k) {
     float p = h2[0] * W3[lane * TC_NUM_ARMS + k] + h2[1] * W3[(lane + 32) * TC_NUM_ARMS + k];
     p = warp_sum(p) + b3[k];
+    if (k == keep) keepv = p;
     if (k == exclude) continue;
     if (best < 0 || p < bestv) { bestv = p; best = k; }
   }
-  return best;
+  return (keep >= 0 && keep != exclude && keepv - bestv < margin) ? keep : best;
 }
 
 // Grouping key of the PULL arm's counting sort (see the PULL section).
@@ -118,7 +121,8 @@ __global__ void __launch_bounds__(PLAN_THREADS) plan_kernel(DevDag g, int64_t T,
                                                            uint64_t *__restrict__ qkeys,
                                                            uint32_t *__restrict__ qvals,
                                                            unsigned long long *__restrict__ tile_bytes,
-                                                           PullKeys pk, unsigned *__restrict__ pull_cnt) {
+                                                           PullKeys pk, unsigned *__restrict__ pull_cnt,
+                                                           float margin) {
   extern __shared__ float s_w[];
   const int lane = threadIdx.x & 31;
   if (selector == TC_SELECT_LEARNED) {
@@ -207,7 +211,7 @@ __global__ void __launch_bounds__(PLAN_THREADS) plan_kernel(DevDag g, int64_t T,
     // time cannot show.  The cost model picks among the per-edge arms for
     // every other tile.
     const int fx = __shfl_sync(TC_FULL_MASK, fixed_select(st), 0);
-    arm = fx == TC_ARM_PULL ? TC_ARM_PULL : mlp_select(s_w, f, lane, TC_ARM_PULL);
+    arm = fx == TC_ARM_PULL ? TC_ARM_PULL : mlp_select(s_w, f, lane, TC_ARM_PULL, fx, margin);
   } else {
     arm = fixed_select(st);
   }
@@ -1974,7 +1978,7 @@ tc_status run_count(tc_ctx *ctx, const DevDag &g_in, const tc_opts &opts, CountB
     TC_CHECK_CUDA(ctx, cudaMemsetAsync(cb.pull_pos, 0, sizeof(uint32_t) * (K + 1), ctx->stream));
     plan_kernel<<<plan_blocks, PLAN_THREADS, plan_smem, ctx->stream>>>(g, T, opts.selector, opts.force_arm,
                                                                        ctx->d_mlp, cb.features, cb.arm, cb.qkeys0,
-                                                                       cb.qvals0, cb.tile_bytes, pk, cb.pull_pos);
+                                                                       cb.qvals0, cb.tile_bytes, pk, cb.pull_pos, ctx->mlp_margin);
     TC_CHECK_LAUNCH(ctx);
   }
   uint64_t *sk = cb.qkeys0;

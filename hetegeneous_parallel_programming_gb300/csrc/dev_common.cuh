@@ -42,6 +42,7 @@ struct tc_ctx {
   cudaEvent_t piece_ev[TC_MAX_PIECES] = {};
   // learned selector
   float *d_mlp = nullptr;                 // TC_MLP_PARAM_COUNT floats
+  float mlp_margin = 0.f;                 // log2-cost gain a learned switch away from the fixed arm needs
   bool mlp_loaded = false;
   // per-arm kernel occupancy (blocks per SM), filled at create
   int arm_blocks_per_sm[TC_NUM_ARMS] = {};

@@ -215,6 +215,13 @@ static void init_weights(uint64_t seed, std::vector<float> &w) {
 
 extern "C" {
 
+tc_status tc_selector_set_margin(tc_ctx *ctx, float margin) {
+  if (!ctx || !(margin >= 0.f) || margin > 64.f)
+    return set_error(ctx, TC_ERR_INVALID_ARG, "margin must lie in [0, 64]");
+  ctx->mlp_margin = margin;
+  return TC_OK;
+}
+
 tc_status tc_selector_set_weights(tc_ctx *ctx, const float *params, int64_t count) {
   if (!ctx || !params || count != P) return set_error(ctx, TC_ERR_INVALID_ARG, "expected %d parameters", P);
   TC_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));

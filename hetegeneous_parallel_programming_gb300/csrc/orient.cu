@@ -589,7 +589,7 @@ __global__ void seg_sort_warp_chunk_kernel(const int64_t *__restrict__ nrowptr, 
     const int64_t rl = min(r0 + lane, n);  // lane's row start (row n: the end)
     const int64_t lo_l = nrowptr[rl];
     const int64_t hi_l = nrowptr[min(rl + 1, n)];
-    const int rows = (int)min<int64_t>(32, n - r0);
+    const int rows = (int)min((int64_t)32, n - r0);
     // prefetch the first row
     int64_t b = __shfl_sync(TC_FULL_MASK, lo_l, 0);
     int L = (int)(__shfl_sync(TC_FULL_MASK, hi_l, 0) - b);

@@ -335,6 +335,12 @@ tc_status tc_selector_train(tc_ctx *ctx, const float *features, const float *cos
                             TC_MLP_HIDDEN * TC_MLP_HIDDEN + TC_MLP_HIDDEN +   \
                             TC_MLP_HIDDEN * TC_NUM_ARMS + TC_NUM_ARMS)
 tc_status tc_selector_set_weights(tc_ctx *ctx, const float *params, int64_t count);
+/* The learned selector keeps the fixed rule's arm for a tile unless the cost
+ * model predicts another arm at least `margin` cheaper in log2 cost (0: any
+ * predicted gain switches; default 0).  The PULL decision always stays with
+ * the fixed rule: a PULL tile's cost depends on how many of its targets'
+ * in-edges other PULL tiles share, which per-tile profiles cannot show. */
+tc_status tc_selector_set_margin(tc_ctx *ctx, float margin);
 tc_status tc_selector_get_weights(tc_ctx *ctx, float *params, int64_t count);
 /* Predicted per-arm costs for host feature rows (inference kernel). */
 tc_status tc_selector_predict(tc_ctx *ctx, const float *features, int64_t rows, float *pred);
