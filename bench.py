@@ -41,7 +41,6 @@ WORKLOADS = {
     "er16k": dict(kind="er", n=16384, avg_degree=16, seed=0),
     "chunglu26": dict(kind="chung_lu", n=1 << 26, avg_degree=32, gamma=2.1, seed=0),
 }
-WEIGHTS = ROOT / "hetegeneous_parallel_programming_gb300" / "data" / "selector_mlp.npz"
 TRAFFIC = ROOT / "profiles" / "pull_kernel_traffic.json"
 
 
@@ -309,12 +308,9 @@ def engine_arm(args, rank, world, local_rank, dist):
     n, nnz, rowptr, colidx = make_graph(eng, wl, torch, dev)
     m = nnz // 2
     log(f"[rank {rank}] graph {args.workload}: n={n} nnz={nnz} m={m} ({time.time() - t0:.1f}s)")
-    have_weights = WEIGHTS.exists()
-    if have_weights:
-        w = np.load(WEIGHTS)["params"].astype(np.float32)
-        have_weights = w.size == tc.TC_MLP_PARAM_COUNT  # weights of another arm set are not used
-        if have_weights:
-            eng.set_selector_weights(w)
+    # the shipped cost model and its switching margin (weights of another arm
+    # set are not used)
+    have_weights = eng.load_shipped_selector()
 
     # the project's autotuner picks the run-time tuning for this graph (PULL
     # chunk and source-block sizes, dense ratio, orientation geometry) by

@@ -18,7 +18,9 @@ engine makes it (PULL where the fixed rule picks PULL, else the MLP's
 cheapest per-edge arm).  Several candidates
 (seed x weight decay x epochs) are trained and the one with the lowest mean
 regret on the scale-21 and scale-22 held-out graphs and a held-out batch is
-kept; the scale-20 and scale-24 graphs (the latter is the benchmark graph)
+kept; its switching margin (the predicted log2-cost gain needed to leave the
+fixed rule's arm) is then chosen by measured plan + count time on the same
+validation graphs; the scale-20 and scale-24 graphs (the latter is the benchmark graph)
 and the benchmark's batch only report.  Mixed small-graph batches (ER /
 R-MAT / RGG, as the batched path counts them) can join the training set as
 disjoint unions (--batches, 2048 graphs each).
@@ -73,6 +75,12 @@ def hybrid_choice(pred: np.ndarray, fixed: np.ndarray) -> np.ndarray:
     return np.where(fixed == PULL, PULL, masked.argmin(1))
 
 
+def timed_phases(eng: tc.Engine, rowptr, colidx, selector: str) -> float:
+    """Device time of the plan and count phases of one count (ms)."""
+    _, _, st = eng.count(rowptr, colidx, selector=selector)
+    return st["ms_plan"] + st["ms_count"]
+
+
 def regret(costs: np.ndarray, chosen: np.ndarray) -> float:
     """Summed cost of the chosen arms over the summed per-tile best cost."""
     best = costs.min(axis=1).sum()
@@ -87,6 +95,9 @@ def main():
     ap.add_argument("--weight-decay", default="0,0.01", help="candidate decoupled weight decays")
     ap.add_argument("--train-seeds", default="7,11,13,17", help="candidate initialisation seeds")
     ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--margins", default="0,0.1,0.25,0.5,1,2",
+                    help="candidate switching margins (log2 cost), chosen by measured time")
+    ap.add_argument("--time-reps", type=int, default=5, help="timed counts per graph and selector (best kept)")
     ap.add_argument("--no-union", action="store_true", help="profile each graph alone only")
     ap.add_argument("--save-heldout", action="store_true", help="also write the held-out graphs' tile profiles")
     ap.add_argument("--batches", type=int, default=0,
@@ -166,6 +177,23 @@ def main():
     w = best[1]
     eng.set_selector_weights(w)
     loss = best[2]["loss"]
+    # the switching margin: chosen by measured time, not by the cost model.
+    # On the validation graphs the plan + count phases (the only ones the
+    # selector changes) are timed with the fixed rule and with the learned
+    # selection at each candidate margin; the margin with the best mean
+    # fixed/learned ratio is kept.
+    margin_trials = []
+    for mg in [float(x) for x in args.margins.split(",")]:
+        eng.set_selector_margin(mg)
+        ratios = []
+        for _, _, r, cidx, _, _, _ in validation:
+            fx = min(timed_phases(eng, r, cidx, "fixed") for _ in range(args.time_reps))
+            ln = min(timed_phases(eng, r, cidx, "learned") for _ in range(args.time_reps))
+            ratios.append(fx / ln)
+        margin_trials.append({"margin": mg, "fixed_over_learned": float(np.mean(ratios)),
+                              "per_graph": [float(x) for x in ratios]})
+    best_margin = max(margin_trials, key=lambda t: t["fixed_over_learned"])
+    eng.set_selector_margin(best_margin["margin"])
     pred = eng.selector_predict(X)
     fixed_all = np.concatenate(fixed)
     train_regret = {"learned": regret(Y, hybrid_choice(pred, fixed_all)), "fixed": regret(Y, fixed_all)}
@@ -188,9 +216,10 @@ def main():
                      "learned_arm_share": np.bincount(learned, minlength=tc.TC_NUM_ARMS).tolist(),
                      "fixed_arm_share": np.bincount(fx, minlength=tc.TC_NUM_ARMS).tolist(),
                      "per_arm_total": k.sum(0).tolist()})
-    np.savez(out / "selector_mlp.npz", params=w.astype(np.float32))
+    np.savez(out / "selector_mlp.npz", params=w.astype(np.float32), margin=np.float32(best_margin["margin"]))
     info = {"architecture": f"16 -> 64 -> 64 -> {tc.TC_NUM_ARMS}, ReLU; bf16 weights at inference, fp32 accumulate",
             "loss": loss, "chosen": best[2], "candidates": candidates, "lr": args.lr, "rows": int(len(X)),
+            "margin": best_margin, "margin_trials": margin_trials,
             "profile_seconds": round(t_prof, 1), "train_seconds": round(t_train, 2),
             "train_regret": train_regret, "held_out": held, "graphs": meta, "union": union, "batches": batches,
             "arms": tc.ARM_NAMES}
@@ -198,7 +227,7 @@ def main():
     np.savez_compressed(out / "selector_training_set.npz", features=X, costs=Y)
     if held_sets:
         np.savez_compressed(out / "selector_heldout_set.npz", **held_sets)
-    print(json.dumps({k: info[k] for k in ("loss", "rows", "train_regret", "held_out")}, indent=1))
+    print(json.dumps({k: info[k] for k in ("loss", "rows", "train_regret", "held_out", "margin_trials")}, indent=1))
     eng.close()
 
 

@@ -90,6 +90,7 @@ def test_shipped_selector_gains_over_fixed_rule(engine):
     except tc.TCError:  # nothing loaded yet
         old = None
     engine.set_selector_weights(w)
+    engine.set_selector_margin(0.0)  # the network's own picks, before the switching margin
     try:
         n, s, d = tc.gen_edges_host(tc.GenSpec("rmat", scale=18, edge_factor=16, seed=99))
         rowptr, colidx = oracle.csr_from_edges(n, s, d)
@@ -105,3 +106,24 @@ def test_shipped_selector_gains_over_fixed_rule(engine):
     finally:
         if old is not None:
             engine.set_selector_weights(old)
+
+
+def test_learned_selection_falls_back_to_the_fixed_rule(engine):
+    """The learned selection keeps the fixed rule's PULL decision on every
+    tile, and with a margin no predicted gain reaches it picks the fixed
+    rule's arm everywhere (the fixed rule is the fallback)."""
+    assert engine.load_shipped_selector()
+    n, s, d = tc.gen_edges_host(tc.GenSpec("rmat", scale=18, edge_factor=16, seed=98))
+    rowptr, colidx = oracle.csr_from_edges(n, s, d)
+    pull = tc.ARM_NAMES.index("pull")
+    fixed = engine.plan_arms(rowptr, colidx, selector="fixed")
+    try:
+        engine.set_selector_margin(0.0)
+        learned = engine.plan_arms(rowptr, colidx, selector="learned")
+        assert np.array_equal(learned == pull, fixed == pull)
+        engine.set_selector_margin(64.0)
+        assert np.array_equal(engine.plan_arms(rowptr, colidx, selector="learned"), fixed)
+        with pytest.raises(tc.TCError):
+            engine.set_selector_margin(-1.0)
+    finally:
+        engine.load_shipped_selector()
