@@ -136,9 +136,31 @@ def make_graph(eng, wl, torch, dev):
     return n, nnz, rowptr, colidx
 
 
+class NoGC:
+    """Python's cyclic garbage collector off for a timed region, so that a
+    collection pass in this harness process is not timed as engine work."""
+
+    def __enter__(self):
+        import gc
+        self.was = gc.isenabled()
+        gc.collect()
+        gc.disable()
+        return self
+
+    def __exit__(self, *exc):
+        import gc
+        if self.was:
+            gc.enable()
+
+
 def timed(fn, steps, warmup, eng, torch, dist):
     """W untimed calls, then K calls bracketed by barrier + sync and CUDA
     events on the engine's stream; returns max-over-ranks ms per step."""
+    with NoGC():
+        return _timed(fn, steps, warmup, eng, torch, dist)
+
+
+def _timed(fn, steps, warmup, eng, torch, dist):
     for _ in range(warmup):
         fn()
     s = torch.cuda.ExternalStream(eng.stream)
@@ -164,6 +186,11 @@ def timed(fn, steps, warmup, eng, torch, dist):
 def timed_steps(fn, steps, warmup, eng, torch, dist):
     """As timed(), plus every step's own device time (a pair of CUDA events
     around each call) for the median and spread."""
+    with NoGC():
+        return _timed_steps(fn, steps, warmup, eng, torch, dist)
+
+
+def _timed_steps(fn, steps, warmup, eng, torch, dist):
     for _ in range(warmup):
         fn()
     s = torch.cuda.ExternalStream(eng.stream)
@@ -435,6 +462,7 @@ def engine_arm(args, rank, world, local_rank, dist):
                     "ms_per_step": round(ms_e2e, 3), "steps": len(e2e_steps),
                     "ms_median": round(statistics.median(e2e_steps), 3),
                     "ms_min": round(min(e2e_steps), 3), "ms_max": round(max(e2e_steps), 3),
+                    "ms_steps": [round(x, 2) for x in e2e_steps],
                     "ms_h2d_in_call": round(st_e2e["ms_h2d"], 3),
                     # e2e against its model: the device-resident step plus the
                     # upload at this box's pinned copy rate (the upload is
