@@ -279,9 +279,14 @@ def pull_roofline(args, st, calls, n, m, hbm, kind, l2_gbs):
         out["dram"] = {"bytes": int(rec["dram_bytes"]), "achieved": round(rec["dram_bytes"] / t_s / 1e9, 1),
                        "frac": round(rec["dram_bytes"] / t_s / 1e9 / hbm, 4),
                        "bytes_over_alg": round(rec["dram_bytes"] / alg, 2)}
-        out["issue_active_pct"] = rec.get("issue_active_pct")
-        out["warps_active_pct"] = rec.get("warps_active_pct")
-        out["shared_bank_conflict_pct"] = rec.get("shared_bank_conflict_pct")
+        # issue and stall counters need a full capture, taken on the smaller
+        # R-MAT scale-22 case only; other workloads carry those, labelled
+        cnt = rec if rec.get("issue_active_pct") is not None else None
+        if cnt is None:
+            cnt, _ = profile_of("rmat22")
+            out["counters_from"] = "rmat22 (full ncu capture of the smaller case)" if cnt else None
+        for k in ("issue_active_pct", "warps_active_pct", "shared_bank_conflict_pct"):
+            out[k] = cnt.get(k) if cnt else None
     l2b = rec.get("l2_bytes") if rec else None
     out["l2"] = {"peak": round(l2_gbs, 1), "unit": "GB/s",
                  "peak_kind": "measured here: tc_l2_bandwidth, 64 MB read 128 times with L1-bypassing loads",
