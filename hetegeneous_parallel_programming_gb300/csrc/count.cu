@@ -1573,6 +1573,218 @@ __device__ __forceinline__ void pull_run(const DevDag &g, const uint2 *__restric
   }
 }
 
+// Packed hash runs.  Most targets whose list needs the hash table have few
+// in-edges (at R-MAT scale 22 half of them have at most 3), and each run pays
+// a chain of dependent loads (record, target, row pointers, list ends, list)
+// before its one or two probe passes.  When a run of a hash target ends
+// inside the first 32 records, the following complete runs of hash targets
+// in those 32 records (lists of at most PK_NB entries) are counted with it:
+// each gets its own hash table, carved from the warp's words (at most
+// PK_TSEL words in all), the lists are inserted as one flattened sequence,
+// and the <= 32 edges are probed as one batch, each edge testing its own
+// run's table.  The words [PK_TSEL, PL_WORDS) hold each edge's table
+// (word offset | bits << 16) during the batch.
+#ifndef TC_PL_PACK
+#define TC_PL_PACK 1
+#endif
+constexpr int PK_NB = 256;
+constexpr int PK_TSEL = PL_WORDS - 32;
+
+// Lane j stands for record k + j; `v` is record k's target and `vw` the
+// target of record k + 1 + lane (-1 past p1).  Returns the end of the packed
+// records, or k when fewer than two runs qualify (nothing was done).
+template <bool PER_EDGE>
+__device__ __forceinline__ int64_t pull_pack(const DevDag &g, const uint2 *__restrict__ er, int64_t k, int64_t p1,
+                                             int32_t v, int32_t vw, uint32_t *tb, int lane, PullBatch &sb,
+                                             uint32_t *out, unsigned long long &acc,
+                                             unsigned long long *tile_cycles) {
+  const long long t0 = clock64();
+  const bool valid = k + lane < p1;
+  int32_t tgt = __shfl_up_sync(TC_FULL_MASK, vw, 1);
+  if (lane == 0) tgt = v;
+  const int32_t prev = __shfl_up_sync(TC_FULL_MASK, tgt, 1);
+  const bool start = valid && (lane == 0 || tgt != prev);
+  const unsigned E = __ballot_sync(TC_FULL_MASK, valid && vw != tgt);  // last record of its run
+  int nb = 0, words = 0, bits = 3;
+  int64_t bb = 0;
+  bool ok = false;
+  if (start && (E >> lane) != 0u) {  // the run ends inside the window
+    bb = g.rowptr[tgt];
+    nb = (int)(g.rowptr[tgt + 1] - bb);
+    if (nb > 0 && nb <= PK_NB) {
+      const uint32_t span = (uint32_t)(__ldg(g.col + bb + nb - 1) - __ldg(g.col + bb)) + 1u;
+      if (span > (uint32_t)PL_WORDS * 32u) {  // a hash target, as in the single-run rule
+        while ((1 << bits) < nb) ++bits;
+        words = 4 << bits;
+        ok = true;
+      }
+    }
+  }
+  const unsigned bad = __ballot_sync(TC_FULL_MASK, start && !ok);
+  const unsigned below = bad ? (1u << (__ffs(bad) - 1)) - 1u : 0xffffffffu;  // lanes before the first misfit
+  int wi = ok ? words : 0, ni = ok ? nb : 0;  // inclusive sums over the runs
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int a = __shfl_up_sync(TC_FULL_MASK, wi, o), b = __shfl_up_sync(TC_FULL_MASK, ni, o);
+    if (lane >= o) {
+      wi += a;
+      ni += b;
+    }
+  }
+  const unsigned inc = __ballot_sync(TC_FULL_MASK, start) & below & __ballot_sync(TC_FULL_MASK, wi <= PK_TSEL);
+  if (__popc(inc) < 2) return k;
+  const int L = 31 - __clz(inc);                       // start of the last packed run
+  const int ne = __ffs(E & ~((1u << L) - 1u));         // records in the pack: through that run's end
+  const int tot_words = __shfl_sync(TC_FULL_MASK, wi, L), tot_nb = __shfl_sync(TC_FULL_MASK, ni, L);
+  // per run: (inclusive entry sum, table word offset | bits << 16, list base
+  // such that pack entry i is col[base + i])
+  if ((inc >> lane) & 1u) {
+    const int64_t base = bb - (int64_t)(ni - nb);
+    sb.ed[__popc(inc & lanemask_lt())] =
+        make_int4(ni, (wi - words) | (bits << 16), (int)(uint32_t)(uint64_t)base, (int)((uint64_t)base >> 32));
+  }
+  __syncwarp();
+  {  // build: the runs' lists as one flattened sequence, PL_UNROLL loads in flight per lane
+    int c = 0;
+    int4 cur = sb.ed[0];
+    for (int q0 = 0; q0 < tot_nb; q0 += 32 * PL_UNROLL) {
+      int32_t x[PL_UNROLL];
+      uint32_t ts[PL_UNROLL];
+#pragma unroll
+      for (int u = 0; u < PL_UNROLL; ++u) {
+        const int i = q0 + 32 * u + lane;
+        x[u] = 0;
+        ts[u] = 0u;
+        if (i < tot_nb) {
+          while (i >= cur.x) cur = sb.ed[++c];  // ends: the last run's sum is tot_nb > i
+          const int64_t base = (int64_t)(((uint64_t)(uint32_t)cur.w << 32) | (uint64_t)(uint32_t)cur.z);
+          x[u] = __ldg(g.col + base + i);
+          ts[u] = (uint32_t)cur.y;
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < PL_UNROLL; ++u) {
+        if (q0 + 32 * u + lane >= tot_nb) continue;
+        uint32_t *T = tb + (ts[u] & 0xffffu);
+        const int tbits = (int)(ts[u] >> 16);
+        const uint32_t mask = (1u << tbits) - 1u, val = (uint32_t)x[u] + 1u;
+        uint32_t b = hslot(x[u], tbits);
+        for (;;) {  // ends: every table is at most a quarter full
+          uint32_t *bk = T + 4 * b;
+          if (atomicCAS(bk, 0u, val) == 0u || atomicCAS(bk + 1, 0u, val) == 0u || atomicCAS(bk + 2, 0u, val) == 0u ||
+              atomicCAS(bk + 3, 0u, val) == 0u)
+            break;
+          b = (b + 1) & mask;
+        }
+      }
+    }
+  }
+  __syncwarp();
+  const bool mine = lane < ne;
+  const uint32_t tsel = mine ? (uint32_t)sb.ed[__popc(inc & (lanemask_lt() | (1u << lane))) - 1].y : 0u;
+  int64_t e = -1;
+  uint32_t y = 0;
+  if (mine) {
+    const uint2 p = er[k + lane];
+    e = p.x;
+    y = p.y;
+  }
+  int64_t a0 = 0;
+  int na = 0;
+  if (mine) {
+    if (g.restrict_after) {
+      a0 = e + 1;
+      na = (int)((int64_t)y - a0);
+    } else {
+      a0 = g.rowptr[y];
+      na = (int)(g.rowptr[y + 1] - a0);
+    }
+  }
+  // the batch's records, as in pull_run
+  const uintptr_t A = reinterpret_cast<uintptr_t>(g.col + a0);
+  const int off = na > 0 ? (int)((A >> 2) & 3u) : 0;
+  const int ng = na > 0 ? (off + na + 3) >> 2 : 0;
+  int gincl = ng;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(TC_FULL_MASK, gincl, o);
+    if (lane >= o) gincl += t;
+  }
+  const int G = __shfl_sync(TC_FULL_MASK, gincl, 31);
+  const int gexcl = gincl - ng;
+  const uintptr_t col_blk = reinterpret_cast<uintptr_t>(g.col) >> 4;
+  __syncwarp();  // every lane has read its run's table from sb.ed
+  sb.ed[lane] = make_int4(gincl, 4 * gexcl + off, 4 * gexcl + off + na, (int)((A >> 4) - col_blk) - gexcl);
+  tb[PK_TSEL + lane] = tsel;
+  if (PER_EDGE) sb.hits[lane] = 0u;
+  __syncwarp();
+  int c = 0;
+  int4 cur = sb.ed[0];
+  uint32_t cts = tb[PK_TSEL];
+  uint32_t h = 0;
+  int hc = 0;
+  for (int gb = 0; gb < G; gb += 32 * PL_GUNROLL) {
+    int4 q[PL_GUNROLL];
+    int lo[PL_GUNROLL], hi[PL_GUNROLL], ce[PL_GUNROLL];
+    uint32_t ts[PL_GUNROLL];
+#pragma unroll
+    for (int j = 0; j < PL_GUNROLL; ++j) {
+      const int gi = gb + 32 * j + lane;
+      q[j] = make_int4(0, 0, 0, 0);
+      lo[j] = 0;
+      hi[j] = 0;
+      if (gi < G) {
+        while (gi >= cur.x) {  // ends: ed[31].x == G > gi
+          cur = sb.ed[++c];
+          cts = tb[PK_TSEL + c];
+        }
+        q[j] = __ldg(reinterpret_cast<const int4 *>((col_blk + (uintptr_t)(cur.w + gi)) << 4));
+        lo[j] = cur.y - 4 * gi;
+        hi[j] = cur.z - 4 * gi;
+      }
+      ce[j] = c;
+      ts[j] = cts;
+    }
+#pragma unroll
+    for (int j = 0; j < PL_GUNROLL; ++j) {
+      if (PER_EDGE && ce[j] != hc) {
+        if (h) atomicAdd(&sb.hits[hc], h);
+        hc = ce[j];
+        h = 0;
+      }
+      const int32_t xs[4] = {q[j].x, q[j].y, q[j].z, q[j].w};
+#pragma unroll
+      for (int t = 0; t < 4; ++t)
+        if (t >= lo[j] && t < hi[j]) h += pull_test<false>(tb + (ts[j] & 0xffffu), 0, (int)(ts[j] >> 16), xs[t]);
+    }
+  }
+  if (PER_EDGE) {
+    if (h) atomicAdd(&sb.hits[hc], h);
+    __syncwarp();
+    if (mine) {
+      const uint32_t cnt = sb.hits[lane];
+      put_edge_count(g, out, e, cnt);
+      acc += cnt;
+    }
+  } else {
+    acc += h;
+  }
+  if (tile_cycles) {  // the pack's time, shared by the edges' probe counts
+    const unsigned tot = __reduce_add_sync(TC_FULL_MASK, (unsigned)(mine ? na + 1 : 0));
+    if (mine) {
+      const unsigned long long dt = (unsigned long long)(clock64() - t0);
+      atomicAdd(&tile_cycles[e / TILE_EDGES], dt * (unsigned long long)(na + 1) / tot);
+    }
+  }
+  __syncwarp();
+  // back to all zero: the tables and the per-edge table words
+  uint4 *t4 = reinterpret_cast<uint4 *>(tb);
+  for (int q2 = lane; q2 < (tot_words >> 2); q2 += 32) t4[q2] = make_uint4(0u, 0u, 0u, 0u);
+  if (lane < 8) t4[(PK_TSEL >> 2) + lane] = make_uint4(0u, 0u, 0u, 0u);
+  __syncwarp();
+  return k + ne;
+}
+
 // Work is taken in chunks of grouped entries that shrink from `item` to
 // `item_min` as the remaining work falls, so the last chunks end together
 // (the ctx's pull_item / pull_item_min; 512 and 128 unless tuned).
@@ -1618,12 +1830,15 @@ __global__ void __launch_bounds__(PL_THREADS, TC_PL_MIN_BLOCKS) pull_kernel(DevD
     for (int64_t k = p0; k < p1;) {
       const long long tr0 = clock64();  // profiling: the run's search and table build are its edges' cost too
       const int32_t v = __ldg(g.col + er[k].x);
-      // end of the run of target v inside this chunk
+      // end of the run of target v inside this chunk; vw keeps the targets of
+      // records k + 1 .. k + 32 for packing short hash runs
       int64_t k2 = k + 1;
-      for (;;) {
+      int32_t vw = -1;
+      for (bool first = true;; first = false) {
         const int64_t j = k2 + lane;
-        const bool diff = j >= p1 || __ldg(g.col + er[j].x) != v;
-        const unsigned bal = __ballot_sync(TC_FULL_MASK, diff);
+        const int32_t vj = j < p1 ? __ldg(g.col + er[j].x) : -1;
+        if (first) vw = vj;
+        const unsigned bal = __ballot_sync(TC_FULL_MASK, vj != v);
         if (bal) { k2 += __ffs(bal) - 1; break; }
         k2 += 32;
       }
@@ -1632,6 +1847,18 @@ __global__ void __launch_bounds__(PL_THREADS, TC_PL_MIN_BLOCKS) pull_kernel(DevD
       int32_t bmin = nb > 0 ? __ldg(g.col + bb) : 0;
       uint32_t span = nb > 0 ? (uint32_t)(__ldg(g.col + bb + nb - 1) - bmin) + 1u : 0u;
       const bool bitmap = span <= (uint32_t)PL_WORDS * 32u;
+#if TC_PL_PACK
+      if (MODE == 0 && !bitmap && nb <= PK_NB && k2 <= k + 32 && k2 < p1) {  // a short hash run: pack it
+        const int64_t kp = out == nullptr ? pull_pack<false>(g, er, k, p1, v, vw, tb, lane, s_batch[w], out, acc,
+                                                             tile_cycles)
+                                          : pull_pack<true>(g, er, k, p1, v, vw, tb, lane, s_batch[w], out, acc,
+                                                            tile_cycles);
+        if (kp > k) {
+          k = kp;
+          continue;
+        }
+      }
+#endif
       // dense edges need the table aligned with the hub bit rows: the base goes
       // down to a 128-id boundary counted from hub0 (a hub target's list lies
       // in (v, n), so the window still fits)
