@@ -107,8 +107,13 @@ struct PullKeys {
   int64_t hub_span;     // hub ids, one key per (source block, hub)
   int64_t block_edges;  // edges per source block
   int64_t global0;      // first key of the non-hub part: blocks * hub_span
-  __device__ __forceinline__ int64_t key(int64_t e, int32_t v) const {
-    return v >= hub0 ? (e / block_edges) * hub_span + (v - hub0) : global0 + v;
+  // key of an edge u->v of tile t (a tile lies in one source block):
+  // key_in(block_base(t), v) = v >= hub0 ? block(t) * hub_span + (v - hub0) : global0 + v
+  __device__ __forceinline__ int64_t block_base(int64_t t) const {
+    return (t * TILE_EDGES / block_edges) * hub_span - hub0;
+  }
+  __device__ __forceinline__ int64_t key_in(int64_t base, int32_t v) const {
+    return v >= hub0 ? base + v : global0 + v;
   }
 };
 
@@ -217,8 +222,10 @@ __global__ void __launch_bounds__(PLAN_THREADS) plan_kernel(DevDag g, int64_t T,
   }
   arm = __shfl_sync(TC_FULL_MASK, arm, 0);
   if (lane < TC_MLP_FEATURES) feats[t * TC_MLP_FEATURES + lane] = f[lane];
-  if (arm == TC_ARM_PULL)
-    for (int64_t e = e0 + lane; e < e1; e += 32) atomicAdd(pull_cnt + pk.key(e, g.col[e]), 1u);
+  if (arm == TC_ARM_PULL) {
+    const int64_t kb = pk.block_base(t);
+    for (int64_t e = e0 + lane; e < e1; e += 32) atomicAdd(pull_cnt + pk.key_in(kb, g.col[e]), 1u);
+  }
   if (lane == 0) {
     arm_out[t] = arm;
     const unsigned long long W40 = (1ULL << 40) - 1;
@@ -1280,6 +1287,12 @@ constexpr int PL_UNROLL = 4;      // table build: list loads in flight per lane
 #endif
 constexpr int PL_GUNROLL = TC_PL_GUNROLL;  // flattened probing: 16-byte loads in flight per lane
 constexpr int PL_GROUP_THREADS = 256;
+// edges per thread whose atomics are issued together in the scatter (1: at
+// R-MAT scale 24, 2 and 4 were 0.3 ms slower; at scale 22 4 was 0.05 ms faster)
+#ifndef TC_PL_SCATTER_UNROLL
+#define TC_PL_SCATTER_UNROLL 1
+#endif
+constexpr int PL_SCATTER_UNROLL = TC_PL_SCATTER_UNROLL;
 // Dense edges: an edge u->v whose source is a hub and whose row suffix holds
 // more than dense_num / dense_den entries per 32-bit word of v's bitmap
 // table (ctx->pull_dense_num / pull_dense_den, 1/1 unless tuned) is counted
@@ -1321,14 +1334,32 @@ __global__ void __launch_bounds__(PL_GROUP_THREADS) pull_scatter_kernel(const in
                                                                        unsigned *__restrict__ pos,
                                                                        uint2 *__restrict__ er) {
   const int64_t T = (m + TILE_EDGES - 1) / TILE_EDGES;
+  constexpr int U = PL_SCATTER_UNROLL;  // edges per thread in flight: their atomics overlap
   for (int64_t t = blockIdx.x; t < T; t += gridDim.x) {
     if (arm[t] != TC_ARM_PULL) continue;
-    const int64_t e1 = min(m, (t + 1) * TILE_EDGES);
-    for (int64_t e = t * TILE_EDGES + threadIdx.x; e < e1; e += PL_GROUP_THREADS) {
-      const unsigned slot = atomicAdd(pos + pk.key(e, __ldg(col + e)), 1u);
-      const int32_t r = __ldg(src + e);
-      const uint32_t y = row_end ? (uint32_t)__ldg(rowptr + r + 1) : (uint32_t)r;
-      er[slot] = make_uint2((uint32_t)e, y);  // one 8-byte store
+    const int64_t e1 = min(m, (t + 1) * TILE_EDGES), kb = pk.block_base(t);
+    for (int64_t eb = t * TILE_EDGES + threadIdx.x; eb < e1; eb += U * PL_GROUP_THREADS) {
+      int64_t key[U];
+      int32_t r[U];
+      unsigned slot[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int64_t e = eb + u * PL_GROUP_THREADS;
+        key[u] = -1;
+        r[u] = 0;
+        if (e < e1) {
+          key[u] = pk.key_in(kb, __ldg(col + e));
+          r[u] = __ldg(src + e);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) slot[u] = key[u] >= 0 ? atomicAdd(pos + key[u], 1u) : 0u;
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if (key[u] < 0) continue;
+        const uint32_t y = row_end ? (uint32_t)__ldg(rowptr + r[u] + 1) : (uint32_t)r[u];
+        er[slot[u]] = make_uint2((uint32_t)(eb + u * PL_GROUP_THREADS), y);  // one 8-byte store
+      }
     }
   }
 }

@@ -224,8 +224,17 @@ __device__ __forceinline__ int64_t row_of_entry(const int64_t *__restrict__ rowp
   return lo;
 }
 
-// Row of every entry of the tile [t0, t_end) of a CSR, into rows[0..t_end-t0)
-// (shared, TILE slots).  All threads of the block call it with the same
+// Shared row array of an entry tile: entry i sits in slot i + i / 32 (one
+// pad word per 32 entries), so the max-scan below, where thread t walks
+// entries [8t, 8t + 8), hits 32 distinct banks at every step (without the
+// pad it is 8-way conflicted), while 32 consecutive entries read by a warp
+// stay in 32 consecutive slots.
+template <int TILE>
+constexpr int row_slots() { return TILE + TILE / 32; }
+__device__ __forceinline__ int rslot(int i) { return i + (i >> 5); }
+
+// Row of every entry of the tile [t0, t_end) of a CSR, into rows[rslot(0 ..
+// t_end-t0-1)] (shared, row_slots<TILE>() slots).  All threads of the block call it with the same
 // `hint`: -1, or the row of entry t0 - 1 (the previous tile's last entry),
 // which it updates to the row of entry t_end - 1.  With a hint one warp finds
 // the tile's first row among the next 32 rows instead of a binary search over
@@ -234,7 +243,7 @@ template <int TILE>
 __device__ void expand_rows(const int64_t *__restrict__ rowptr, int64_t n, int64_t t0, int64_t t_end,
                             int *rows, int *scan_tmp, int64_t &hint) {
   __shared__ int64_t s_first;
-  for (int i = threadIdx.x; i < TILE; i += blockDim.x) rows[i] = -1;
+  for (int i = threadIdx.x; i < TILE; i += blockDim.x) rows[rslot(i)] = -1;
   if (threadIdx.x < 32) {
     int64_t r = -1;
     if (hint >= 0) {  // first r >= hint with rowptr[r + 1] > t0
@@ -247,11 +256,11 @@ __device__ void expand_rows(const int64_t *__restrict__ rowptr, int64_t n, int64
   }
   __syncthreads();
   const int64_t r0 = s_first;
-  if (threadIdx.x == 0) rows[0] = (int)r0;
+  if (threadIdx.x == 0) rows[rslot(0)] = (int)r0;
   for (int64_t r = r0 + 1 + threadIdx.x; r < n; r += blockDim.x) {
     const int64_t s = rowptr[r];
     if (s >= t_end) break;
-    if (s > t0) atomicMax(&rows[s - t0], (int)r);
+    if (s > t0) atomicMax(&rows[rslot((int)(s - t0))], (int)r);
   }
   __syncthreads();
   // inclusive max-scan (row ids only grow): per-thread segment, then block.
@@ -259,7 +268,7 @@ __device__ void expand_rows(const int64_t *__restrict__ rowptr, int64_t n, int64
   int base = threadIdx.x * PER;
   int m = -1;
 #pragma unroll
-  for (int k = 0; k < PER; ++k) m = max(m, rows[base + k]);
+  for (int k = 0; k < PER; ++k) m = max(m, rows[rslot(base + k)]);
   // exclusive max-scan of m across the block
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int x = m;
@@ -285,11 +294,11 @@ __device__ void expand_rows(const int64_t *__restrict__ rowptr, int64_t n, int64
   if (lane > 0) carry = max(carry, xin);
 #pragma unroll
   for (int k = 0; k < PER; ++k) {
-    carry = max(carry, rows[base + k]);
-    rows[base + k] = carry;
+    carry = max(carry, rows[rslot(base + k)]);
+    rows[rslot(base + k)] = carry;
   }
   __syncthreads();
-  hint = rows[t_end - t0 - 1];
+  hint = rows[rslot((int)(t_end - t0 - 1))];
 }
 
 // ---- host-side launch helpers shared by the .cu files --------------------------

@@ -59,7 +59,7 @@ __global__ void validate_rowptr_kernel(const int64_t *__restrict__ rowptr, int64
 __global__ void __launch_bounds__(OR_THREADS) validate_col_kernel(const int64_t *__restrict__ rowptr,
                                                                  const int32_t *__restrict__ col, int64_t n,
                                                                  int64_t nnz, int simple, unsigned *flags) {
-  __shared__ int rows[ENTRY_TILE];
+  __shared__ int rows[row_slots<ENTRY_TILE>()];
   __shared__ int scan_tmp[32];
   unsigned f = 0;
   const int64_t tiles = (nnz + ENTRY_TILE - 1) / ENTRY_TILE;
@@ -74,7 +74,7 @@ __global__ void __launch_bounds__(OR_THREADS) validate_col_kernel(const int64_t 
       const int32_t v = col[e];
       if (v < 0 || (int64_t)v >= n) { f |= VF_ID_RANGE; continue; }
       if (simple) {
-        const int u = rows[e - t0];
+        const int u = rows[rslot((int)(e - t0))];
         if (u == v) f |= VF_SELF_LOOP;
         if (u >= 0 && u < n && e > 0 && e > rowptr[u] && col[e - 1] >= v) f |= VF_UNSORTED;
       }
@@ -135,7 +135,7 @@ __global__ void __launch_bounds__(OR_THREADS, 6) kept_count_kernel(const int64_t
                                                                int b_off, int32_t *__restrict__ rv_out,
                                                                const int32_t *__restrict__ vgroup,
                                                                const int64_t *__restrict__ vtx_off) {
-  __shared__ int rows[ENTRY_TILE];
+  __shared__ int rows[row_slots<ENTRY_TILE>()];
   __shared__ int scan_tmp[32];
   __shared__ unsigned long long bsum;
   if (threadIdx.x == 0) bsum = 0;
@@ -160,7 +160,7 @@ __global__ void __launch_bounds__(OR_THREADS, 6) kept_count_kernel(const int64_t
       for (int k = 0; k < OR_PER; ++k) {
         const int64_t e = t0 + k * OR_THREADS + threadIdx.x;
         if (e >= t1) continue;
-        const int u = rows[e - t0];
+        const int u = rows[rslot((int)(e - t0))];
         int64_t base = 0, size = 0;
         if (u >= 0 && u < n) {
           const int32_t gi = vgroup[u];
@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(OR_THREADS, 6) kept_count_kernel(const int64_t
       bool keep = false;
       int u = -1;
       if (e < t1) {
-        u = rows[e - t0];
+        u = rows[rslot((int)(e - t0))];
         const int32_t v = vv[k];
         keep = u >= 0 && rv[k] >= 0 && rv[k] > rank[u];
         if (VALIDATE) {
@@ -200,10 +200,17 @@ __global__ void __launch_bounds__(OR_THREADS, 6) kept_count_kernel(const int64_t
           if (u >= 0 && u < n && e > 0 && e > rowptr[u] && col[e - 1] >= col[e]) f |= VF_UNSORTED;
         }
       }
+      // the warp's 32 entries are consecutive, so each row is a run of
+      // lanes: the run's first lane adds the run's kept entries
       const unsigned km = __ballot_sync(TC_FULL_MASK, keep);
-      if (keep) {
-        const unsigned peers = __match_any_sync(km, u);
-        if (lane == __ffs(peers) - 1) atomicAdd(&kept[u], (unsigned long long)__popc(peers));
+      const int u_prev = __shfl_up_sync(TC_FULL_MASK, u, 1);
+      const bool head = e < t1 && (lane == 0 || u != u_prev);
+      const unsigned hm = __ballot_sync(TC_FULL_MASK, head);
+      if (head && km) {
+        const unsigned later = hm & ~(lanemask_lt() | (1u << lane));  // first lanes of the following runs
+        const unsigned run = (later ? (later & (0u - later)) - 1u : 0xffffffffu) & ~lanemask_lt();
+        const unsigned c = __popc(km & run);
+        if (c) atomicAdd(&kept[u], (unsigned long long)c);
       }
       mine += keep ? 1 : 0;
     }
@@ -334,7 +341,7 @@ __global__ void __launch_bounds__(OR_THREADS, 6) place_kernel(const int64_t *__r
                                                           uint32_t *__restrict__ perm,
                                                           int32_t *__restrict__ dag_col,
                                                           const int32_t *__restrict__ rv_in) {
-  __shared__ int rows[ENTRY_TILE];
+  __shared__ int rows[row_slots<ENTRY_TILE>()];
   __shared__ int scan_tmp[32];
   __shared__ long long s_wbase[OR_THREADS / 32 + 1];
   constexpr int NW = OR_THREADS / 32;
@@ -355,7 +362,7 @@ __global__ void __launch_bounds__(OR_THREADS, 6) place_kernel(const int64_t *__r
       const int i = wbase + k * 32 + lane;
       const bool in = t0 + i < t1;
       vv[k] = in && (DAGCOL || !rv_in) ? col[t0 + i] : -1;
-      uu[k] = in ? rows[i] : -1;
+      uu[k] = in ? rows[rslot(i)] : -1;
       if (rv_in) rv[k] = in ? rv_in[t0 + i] : -1;  // ranks of the targets, from the kept-count pass
     }
     if (!rv_in) {
@@ -838,14 +845,14 @@ tc_status orient_phase_b(tc_ctx *ctx, const DevCSR &g, OrientBufs &b, int64_t m,
 
 __global__ void __launch_bounds__(OR_THREADS) expand_src_kernel(const int64_t *__restrict__ rowptr, int64_t n,
                                                                int64_t m, int32_t *__restrict__ src) {
-  __shared__ int rows[ENTRY_TILE];
+  __shared__ int rows[row_slots<ENTRY_TILE>()];
   __shared__ int scan_tmp[32];
   const int64_t tiles = (m + ENTRY_TILE - 1) / ENTRY_TILE;
   for (int64_t t = blockIdx.x; t < tiles; t += gridDim.x) {
     const int64_t t0 = t * ENTRY_TILE, t1 = min(m, t0 + ENTRY_TILE);
     int64_t hint = -1;  // tiles of one block are not contiguous here
     expand_rows<ENTRY_TILE>(rowptr, n, t0, t1, rows, scan_tmp, hint);
-    for (int k = threadIdx.x; k < t1 - t0; k += OR_THREADS) src[t0 + k] = rows[k];
+    for (int k = threadIdx.x; k < t1 - t0; k += OR_THREADS) src[t0 + k] = rows[rslot((int)k)];
     __syncthreads();
   }
 }
