@@ -25,6 +25,12 @@ constexpr bool PLACE_SRC = TC_PLACE_SRC != 0;
 #define TC_SEG_WARP_CHUNK 1
 #endif
 constexpr bool SEG_WARP_CHUNK = TC_SEG_WARP_CHUNK != 0;
+// 1: rows of 33..256 entries are sorted with their keys in registers
+// (seg_sort_warpreg_kernel); 0: in a warp's shared-memory slice
+#ifndef TC_SEG_WARP_REG
+#define TC_SEG_WARP_REG 1
+#endif
+constexpr bool SEG_WARP_REG = TC_SEG_WARP_REG != 0;
 
 void orient_geometry(const tc_ctx *ctx, int64_t nnz, int pieces, int *G, int64_t *chunk) {
   int64_t tiles = (nnz + ENTRY_TILE - 1) / ENTRY_TILE;
@@ -623,6 +629,128 @@ __global__ void seg_sort_warp_chunk_kernel(const int64_t *__restrict__ nrowptr, 
   }
 }
 
+// The flip network over 32 * E keys held E per lane in registers, lane l
+// holding entries [l*E, l*E + E): comparators between entries of one lane
+// are register compare-exchanges; between lanes, each lane trades one key
+// per entry with one shuffle and keeps the smaller (lower entry) or larger.
+// Entry i's flip partner at level lv is i ^ (lv - 1), i.e. lane l ^ (lv/E -
+// 1), slot E - 1 - x; its half-cleaner partner at distance j is i ^ j.
+template <bool VALS>
+__device__ __forceinline__ void reg_keep(int32_t &k, uint32_t &v, int32_t ok, uint32_t ov, bool lower) {
+  if (lower ? ok < k : ok > k) {
+    k = ok;
+    if (VALS) v = ov;
+  }
+}
+
+template <int E, bool VALS>
+__device__ __forceinline__ void warp_sort_blocked(int32_t (&k)[E], uint32_t (&v)[E], int lane) {
+  constexpr int P = 32 * E;
+#pragma unroll
+  for (int lv = 2; lv <= P; lv <<= 1) {
+    if (lv <= E) {
+#pragma unroll
+      for (int x = 0; x < E; ++x) {
+        const int y = x ^ (lv - 1);
+        if (y > x && k[y] < k[x]) {
+          const int32_t t = k[x];
+          k[x] = k[y];
+          k[y] = t;
+          if (VALS) {
+            const uint32_t s = v[x];
+            v[x] = v[y];
+            v[y] = s;
+          }
+        }
+      }
+    } else {
+      const int pl = lane ^ (lv / E - 1);
+      const bool lower = ((lane * E) & (lv >> 1)) == 0;
+      int32_t ok[E];
+      uint32_t ov[E];
+#pragma unroll
+      for (int x = 0; x < E; ++x) {
+        ok[x] = __shfl_sync(TC_FULL_MASK, k[E - 1 - x], pl);
+        if (VALS) ov[x] = __shfl_sync(TC_FULL_MASK, v[E - 1 - x], pl);
+      }
+#pragma unroll
+      for (int x = 0; x < E; ++x) reg_keep<VALS>(k[x], v[x], ok[x], VALS ? ov[x] : 0u, lower);
+    }
+#pragma unroll
+    for (int j = lv >> 2; j >= 1; j >>= 1) {
+      if (j < E) {
+#pragma unroll
+        for (int x = 0; x < E; ++x) {
+          if (x & j) continue;
+          const int y = x | j;
+          if (k[y] < k[x]) {
+            const int32_t t = k[x];
+            k[x] = k[y];
+            k[y] = t;
+            if (VALS) {
+              const uint32_t s = v[x];
+              v[x] = v[y];
+              v[y] = s;
+            }
+          }
+        }
+      } else {
+        const int pl = lane ^ (j / E);
+        const bool lower = ((lane * E) & j) == 0;
+#pragma unroll
+        for (int x = 0; x < E; ++x) {
+          const int32_t o = __shfl_sync(TC_FULL_MASK, k[x], pl);
+          const uint32_t w = VALS ? __shfl_sync(TC_FULL_MASK, v[x], pl) : 0u;
+          reg_keep<VALS>(k[x], v[x], o, w, lower);
+        }
+      }
+    }
+  }
+}
+
+template <int E, bool VALS>
+__device__ __forceinline__ void warp_sort_row_blocked(int32_t *__restrict__ ncol, uint32_t *__restrict__ perm,
+                                                      int64_t b, int L, int lane) {
+  int32_t k[E];
+  uint32_t v[E];
+#pragma unroll
+  for (int x = 0; x < E; ++x) {
+    const int i = lane * E + x;
+    k[x] = i < L ? ncol[b + i] : INT32_MAX;
+    v[x] = (VALS && i < L) ? perm[b + i] : 0u;
+  }
+  warp_sort_blocked<E, VALS>(k, v, lane);
+#pragma unroll
+  for (int x = 0; x < E; ++x) {
+    const int i = lane * E + x;
+    if (i < L) {
+      ncol[b + i] = k[x];
+      if (VALS) perm[b + i] = v[x];
+    }
+  }
+}
+
+// Rows of 33..SEG_WARP_MAX entries: one warp per row, 2, 4 or 8 keys per
+// lane in registers (warp_sort_blocked).
+template <bool VALS>
+__global__ void __launch_bounds__(256) seg_sort_warpreg_kernel(const int64_t *__restrict__ nrowptr,
+                                                              const int32_t *__restrict__ list,
+                                                              const unsigned *count, int32_t *__restrict__ ncol,
+                                                              uint32_t *__restrict__ perm) {
+  static_assert(SEG_WARP_MAX == 256, "rows of up to 8 keys per lane");
+  const int lane = threadIdx.x & 31;
+  const unsigned cnt = *count;
+  const unsigned warps = gridDim.x * (blockDim.x >> 5);
+  for (unsigned i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < cnt; i += warps) {
+    const int32_t r = list[i];
+    const int64_t b = nrowptr[r];
+    const int L = (int)(nrowptr[r + 1] - b);
+    if (L <= 64) warp_sort_row_blocked<2, VALS>(ncol, perm, b, L, lane);
+    else if (L <= 128) warp_sort_row_blocked<4, VALS>(ncol, perm, b, L, lane);
+    else warp_sort_row_blocked<8, VALS>(ncol, perm, b, L, lane);
+  }
+}
+
 // Rows of 33..SEG_WARP_MAX entries: one warp per row sorts in its own slice
 // of shared memory with the same flip network (register stages for
 // distances below 32), synchronising with __syncwarp.
@@ -796,7 +924,11 @@ static tc_status launch_row_sorts(tc_ctx *ctx, const DevCSR &g, OrientBufs &b) {
   else
     seg_sort_warp_kernel<VALS><<<grid_for(ctx, g.n * 32, 256, 8), 256, 0, ctx->stream>>>(b.nrowptr, g.n, b.ncol, pv);
   TC_CHECK_LAUNCH(ctx);
-  seg_sort_warpsmem_kernel<VALS><<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(b.nrowptr, b.mid_list, b.seg_counts,
+  if (SEG_WARP_REG)
+    seg_sort_warpreg_kernel<VALS><<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(b.nrowptr, b.mid_list, b.seg_counts,
+                                                                            b.ncol, pv);
+  else
+    seg_sort_warpsmem_kernel<VALS><<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(b.nrowptr, b.mid_list, b.seg_counts,
                                                                             b.ncol, pv);
   TC_CHECK_LAUNCH(ctx);
   seg_sort_smem_kernel<VALS><<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(b.nrowptr, b.big_list, b.seg_counts + 1,
