@@ -88,7 +88,7 @@ void orient_sizes(const tc_ctx *ctx, int64_t n, int64_t nnz, bool perm, bool dag
   sz.take<char>((int64_t)scr);
   sz.take<int64_t>(n + 1); sz.take<int64_t>(n + 1); sz.take<int64_t>(n + 1);
   sz.take<int2>(n);
-  sz.take<int32_t>(n); sz.take<int32_t>(n); sz.take<int32_t>(n); sz.take<unsigned>(3);
+  sz.take<int32_t>(n); sz.take<int32_t>(n); sz.take<int32_t>(n); sz.take<unsigned>(4);
   sz.take<int32_t>(nnz);
   sz.take<int32_t>(mmax); sz.take<int32_t>(mmax);
   if (perm) sz.take<uint32_t>(mmax);
@@ -116,7 +116,7 @@ void orient_carve(const tc_ctx *ctx, int64_t n, int64_t nnz, bool perm, bool dag
   b.mid_list = bump.take<int32_t>(n);
   b.big_list = bump.take<int32_t>(n);
   b.huge_list = bump.take<int32_t>(n);
-  b.seg_counts = bump.take<unsigned>(3);
+  b.seg_counts = bump.take<unsigned>(4);
   b.rv = bump.take<int32_t>(nnz);
   b.ncol = bump.take<int32_t>(mmax);
   b.nsrc = bump.take<int32_t>(mmax);

@@ -27,6 +27,10 @@ constexpr int BM_THREADS = 512;
 constexpr int BM_SMEM_BYTES = 100 * 1024;
 constexpr int64_t BM_BITS = (int64_t)BM_SMEM_BYTES * 8;
 constexpr int PLAN_THREADS = 256;
+#ifndef TC_PLAN_UNROLL
+#define TC_PLAN_UNROLL 2
+#endif
+constexpr int PLAN_UNROLL = TC_PLAN_UNROLL;  // plan_kernel: edges per lane with their gathers in flight
 
 // ---- plan: features + selection ------------------------------------------------
 
@@ -143,38 +147,65 @@ __global__ void __launch_bounds__(PLAN_THREADS) plan_kernel(DevDag g, int64_t T,
   unsigned long long work = 0, alg = 0;
   int nrows = 0;
   long long maxdr = 0, maxwin = 0;
-  for (int64_t e = e0 + lane; e < e1; e += 32) {
-    const int32_t r = g.src[e], s = g.col[e];
-    const int64_t rb = g.rowptr[r], re = g.rowptr[r + 1];
-    const int64_t a0 = g.restrict_after ? e + 1 : rb;
-    const float da = (float)(re - a0);
-    float db, ins;  // target's out-degree and DAG in-degree: one 8-byte gather on a relabelled DAG
-    if (g.dv) {
-      const int2 q = __ldg(g.dv + s);
-      db = (float)q.x;
-      ins = (float)q.y;
-    } else {
-      db = (float)(g.rowptr[s + 1] - g.rowptr[s]);
-      ins = g.indeg ? (float)g.indeg[s] : 0.f;
-    }
-    sda += da;
-    sdb += db;
-    const float mn = fminf(da, db), mx = fmaxf(da, db);
-    smin += mn;
-    smax += mx;
-    const float lr = flog2p1(da) - flog2p1(db);
-    salr += fabsf(lr);
-    sin += ins;  // how many edges share this target's list
-    const int bin = mn < 2.f ? 0 : mn < 8.f ? 1 : mn < 32.f ? 2 : mn < 128.f ? 3 : mn < 512.f ? 4 : 5;
+  // PLAN_UNROLL edges per lane at a time, their loads in three rounds, each
+  // round's loads all in flight: (row, target, previous edge's row); (row
+  // pointers, target degrees); for an edge that starts its row in the tile,
+  // the two ends of its row window
+  for (int64_t eb = e0 + lane; eb < e1; eb += 32 * PLAN_UNROLL) {
+    int32_t rr[PLAN_UNROLL], ss[PLAN_UNROLL], pr[PLAN_UNROLL];
 #pragma unroll
-    for (int k = 0; k < 6; ++k) bins[k] += (bin == k) ? 1.f : 0.f;
-    work += (unsigned long long)(da + db);
-    alg += 4ULL * (unsigned long long)((re - rb) + (int64_t)db) + 4ULL;
-    if (e == e0 || g.src[e - 1] != r) {
-      ++nrows;
-      maxdr = max(maxdr, (long long)(re - rb));
-      const int64_t s0 = g.restrict_after ? e + 1 : rb;
-      if (s0 < re) maxwin = max(maxwin, (long long)g.col[re - 1] - (long long)g.col[s0] + 1);
+    for (int u = 0; u < PLAN_UNROLL; ++u) {
+      const int64_t e = eb + 32 * u;
+      rr[u] = e < e1 ? g.src[e] : 0;
+      ss[u] = e < e1 ? g.col[e] : 0;
+      pr[u] = e < e1 && e > e0 ? g.src[e - 1] : -1;
+    }
+    int64_t rbs[PLAN_UNROLL], res[PLAN_UNROLL];
+    int2 dq[PLAN_UNROLL];
+#pragma unroll
+    for (int u = 0; u < PLAN_UNROLL; ++u) {
+      const bool in = eb + 32 * u < e1;
+      rbs[u] = in ? g.rowptr[rr[u]] : 0;
+      res[u] = in ? g.rowptr[rr[u] + 1] : 0;
+      if (!in) dq[u] = make_int2(0, 0);
+      else if (g.dv) dq[u] = __ldg(g.dv + ss[u]);  // (out-degree, DAG in-degree): one 8-byte gather
+      else dq[u] = make_int2((int)(g.rowptr[ss[u] + 1] - g.rowptr[ss[u]]), g.indeg ? g.indeg[ss[u]] : 0);
+    }
+    int32_t wlo[PLAN_UNROLL], whi[PLAN_UNROLL];
+#pragma unroll
+    for (int u = 0; u < PLAN_UNROLL; ++u) {
+      const int64_t e = eb + 32 * u;
+      const int64_t s0 = g.restrict_after ? e + 1 : rbs[u];
+      const bool wide = e < e1 && pr[u] != rr[u] && s0 < res[u];  // a row start with a window
+      wlo[u] = wide ? g.col[s0] : 0;
+      whi[u] = wide ? g.col[res[u] - 1] : -1;
+    }
+#pragma unroll
+    for (int u = 0; u < PLAN_UNROLL; ++u) {
+      const int64_t e = eb + 32 * u;
+      if (e >= e1) break;
+      const int64_t rb = rbs[u], re = res[u];
+      const int64_t a0 = g.restrict_after ? e + 1 : rb;
+      const float da = (float)(re - a0);
+      const float db = (float)dq[u].x, ins = (float)dq[u].y;  // target's out-degree and DAG in-degree
+      sda += da;
+      sdb += db;
+      const float mn = fminf(da, db), mx = fmaxf(da, db);
+      smin += mn;
+      smax += mx;
+      const float lr = flog2p1(da) - flog2p1(db);
+      salr += fabsf(lr);
+      sin += ins;  // how many edges share this target's list
+      const int bin = mn < 2.f ? 0 : mn < 8.f ? 1 : mn < 32.f ? 2 : mn < 128.f ? 3 : mn < 512.f ? 4 : 5;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) bins[k] += (bin == k) ? 1.f : 0.f;
+      work += (unsigned long long)(da + db);
+      alg += 4ULL * (unsigned long long)((re - rb) + (int64_t)db) + 4ULL;
+      if (pr[u] != rr[u]) {  // the edge starts its row in the tile (pr = -1 for the tile's first edge)
+        ++nrows;
+        maxdr = max(maxdr, (long long)(re - rb));
+        maxwin = max(maxwin, (long long)whi[u] - (long long)wlo[u] + 1);
+      }
     }
   }
   sda = warp_sum(sda); sdb = warp_sum(sdb); smin = warp_sum(smin); smax = warp_sum(smax);
@@ -1293,6 +1324,12 @@ constexpr int PL_GROUP_THREADS = 256;
 #define TC_PL_SCATTER_UNROLL 1
 #endif
 constexpr int PL_SCATTER_UNROLL = TC_PL_SCATTER_UNROLL;
+// 1: the scatter streams its column and row reads and its record stores with
+// evict-first hints, so the grouping counters (K * 4 bytes) stay in L2
+#ifndef TC_PL_SCATTER_STREAM
+#define TC_PL_SCATTER_STREAM 1
+#endif
+constexpr bool PL_SCATTER_STREAM = TC_PL_SCATTER_STREAM != 0;
 // Dense edges: an edge u->v whose source is a hub and whose row suffix holds
 // more than dense_num / dense_den entries per 32-bit word of v's bitmap
 // table (ctx->pull_dense_num / pull_dense_den, 1/1 unless tuned) is counted
@@ -1347,9 +1384,9 @@ __global__ void __launch_bounds__(PL_GROUP_THREADS) pull_scatter_kernel(const in
         const int64_t e = eb + u * PL_GROUP_THREADS;
         key[u] = -1;
         r[u] = 0;
-        if (e < e1) {
-          key[u] = pk.key_in(kb, __ldg(col + e));
-          r[u] = __ldg(src + e);
+        if (e < e1) {  // read once: streamed past L2, which keeps the counters
+          key[u] = pk.key_in(kb, PL_SCATTER_STREAM ? __ldcs(col + e) : __ldg(col + e));
+          r[u] = PL_SCATTER_STREAM ? __ldcs(src + e) : __ldg(src + e);
         }
       }
 #pragma unroll
@@ -1358,7 +1395,9 @@ __global__ void __launch_bounds__(PL_GROUP_THREADS) pull_scatter_kernel(const in
       for (int u = 0; u < U; ++u) {
         if (key[u] < 0) continue;
         const uint32_t y = row_end ? (uint32_t)__ldg(rowptr + r[u] + 1) : (uint32_t)r[u];
-        er[slot[u]] = make_uint2((uint32_t)(eb + u * PL_GROUP_THREADS), y);  // one 8-byte store
+        const uint2 rec = make_uint2((uint32_t)(eb + u * PL_GROUP_THREADS), y);  // one 8-byte store
+        if (PL_SCATTER_STREAM) __stcs(er + slot[u], rec);  // evict-first: the counters stay in L2
+        else er[slot[u]] = rec;
       }
     }
   }
@@ -1421,6 +1460,16 @@ struct PullBatch {
   uint32_t hits[32];  // PER_EDGE: triangles of each edge of the batch
 };
 
+// A grouped record.  TC_PULL_ER_STREAM 1 loads records with evict-first
+// hints (they are read in order, about once), leaving L2 to the row
+// suffixes and hub bit rows.
+#ifndef TC_PULL_ER_STREAM
+#define TC_PULL_ER_STREAM 0
+#endif
+__device__ __forceinline__ uint2 pull_rec(const uint2 *__restrict__ er, int64_t i) {
+  return TC_PULL_ER_STREAM ? __ldcs(er + i) : er[i];
+}
+
 // Dense edges (DENSE, bitmap tables of hub targets only): the table's base is
 // hub0 + 128 * woff4, so its 16-byte word j lines up with word woff4 + j of
 // every hub bit row; tw4 16-byte words cover it.
@@ -1440,7 +1489,7 @@ __device__ __forceinline__ void pull_run(const DevDag &g, const uint2 *__restric
   int64_t e_n = -1;
   uint32_t y_n = 0;
   if (k + lane < k2) {
-    const uint2 p = er[k + lane];
+    const uint2 p = pull_rec(er, k + lane);
     e_n = p.x;
     y_n = p.y;
   }
@@ -1450,7 +1499,7 @@ __device__ __forceinline__ void pull_run(const DevDag &g, const uint2 *__restric
     const uint32_t y = y_n;  // relabelled DAG: end of the edge's row; else its row
     e_n = -1;
     if (qb + 32 + lane < k2) {  // prefetch for the next batch
-      const uint2 p = er[qb + 32 + lane];
+      const uint2 p = pull_rec(er, qb + 32 + lane);
       e_n = p.x;
       y_n = p.y;
     }
@@ -1716,7 +1765,7 @@ __device__ __forceinline__ int64_t pull_pack(const DevDag &g, const uint2 *__res
   int64_t e = -1;
   uint32_t y = 0;
   if (mine) {
-    const uint2 p = er[k + lane];
+    const uint2 p = pull_rec(er, k + lane);
     e = p.x;
     y = p.y;
   }
@@ -1860,14 +1909,14 @@ __global__ void __launch_bounds__(PL_THREADS, TC_PL_MIN_BLOCKS) pull_kernel(DevD
     const int64_t p0 = (int64_t)it;
     for (int64_t k = p0; k < p1;) {
       const long long tr0 = clock64();  // profiling: the run's search and table build are its edges' cost too
-      const int32_t v = __ldg(g.col + er[k].x);
+      const int32_t v = __ldg(g.col + pull_rec(er, k).x);
       // end of the run of target v inside this chunk; vw keeps the targets of
       // records k + 1 .. k + 32 for packing short hash runs
       int64_t k2 = k + 1;
       int32_t vw = -1;
       for (bool first = true;; first = false) {
         const int64_t j = k2 + lane;
-        const int32_t vj = j < p1 ? __ldg(g.col + er[j].x) : -1;
+        const int32_t vj = j < p1 ? __ldg(g.col + pull_rec(er, j).x) : -1;
         if (first) vw = vj;
         const unsigned bal = __ballot_sync(TC_FULL_MASK, vj != v);
         if (bal) { k2 += __ffs(bal) - 1; break; }
@@ -1911,7 +1960,7 @@ __global__ void __launch_bounds__(PL_THREADS, TC_PL_MIN_BLOCKS) pull_kernel(DevD
       if (!bitmap && nb > PL_WORDS / 2) {  // wide window and long list: warp pivot search per edge
         long long tq = tr0;
         for (int64_t q = k; q < k2; ++q) {
-          const int64_t e = er[q].x;
+          const int64_t e = pull_rec(er, q).x;
           int32_t s;
           const EdgeLists L = edge_lists(g, e, s);
           uint32_t c = 0;
@@ -2139,6 +2188,9 @@ static int64_t pull_key_count(int64_t n, int64_t T, int block_tiles, PullKeys *p
 // counted the keys), then count.  The scatter kernel runs over every tile
 // (each block skips tiles of other arms) since the number of PULL tiles is
 // known only on the device.
+#ifndef TC_HUB_BITS_SCAN
+#define TC_HUB_BITS_SCAN 1
+#endif
 // Bit rows of the hubs' out-lists, one warp per hub row: the warp clears the
 // row, then ORs in its entries, one OR per distinct word (lanes matched by
 // word).  Every entry of a hub row is a hub (it ranks above its row).  Nothing
@@ -2158,12 +2210,28 @@ __global__ void hub_bits_kernel(DevDag g, int32_t hub0, int wpr4, const unsigned
       const bool in = e < e1;
       const int32_t w = in ? g.col[e] - hub0 : -1;
       const bool ok = in && w >= 0;  // false only outside a relabelled DAG
+#if TC_HUB_BITS_SCAN
+      // the row is sorted, so lanes sharing a word are a run: a segmented OR
+      // scan leaves the run's bits in its last lane, which stores them
+      // (for any order every bit still reaches the last lane of its run)
+      const int wid = ok ? (w >> 5) : -1;
+      unsigned x = ok ? 1u << (w & 31) : 0u;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(TC_FULL_MASK, x, o);
+        const int wy = __shfl_up_sync(TC_FULL_MASK, wid, o);
+        if (lane >= o && wy == wid) x |= y;
+      }
+      const int wn = __shfl_down_sync(TC_FULL_MASK, wid, 1);
+      if (ok && (lane == 31 || wn != wid)) atomicOr(b + wid, x);
+#else
       const unsigned act = __ballot_sync(TC_FULL_MASK, ok);
       if (ok) {
         const unsigned peers = __match_any_sync(act, w >> 5);
         const unsigned word = __reduce_or_sync(peers, 1u << (w & 31));
         if (lane == __ffs(peers) - 1) atomicOr(b + (w >> 5), word);
       }
+#endif
     }
     __syncwarp();
   }

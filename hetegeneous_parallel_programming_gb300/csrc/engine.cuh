@@ -69,7 +69,7 @@ struct OrientBufs {
   int64_t *dnew;               // [n+1] relabelled row lengths
   int2 *dv;                    // [n] (out-degree, in-degree) per relabelled vertex
   int32_t *mid_list, *big_list, *huge_list;  // [n] rows for the warp / block / global sorts
-  unsigned *seg_counts;        // [3]
+  unsigned *seg_counts;        // [4]: mid, big, huge rows; big rows left to the block sort
   int32_t *rv = nullptr;       // [nnz] rank of every entry's target, written by the kept-count pass
   // phase B
   int32_t *ncol, *nsrc;        // [m]

@@ -31,6 +31,12 @@ constexpr bool SEG_WARP_CHUNK = TC_SEG_WARP_CHUNK != 0;
 #define TC_SEG_WARP_REG 1
 #endif
 constexpr bool SEG_WARP_REG = TC_SEG_WARP_REG != 0;
+// 1: rows of 257..4096 entries whose ids span <= 32768 values are sorted
+// through a warp's bitmap (seg_sort_warpbits_kernel) before the block sort
+#ifndef TC_SEG_WARP_BITS
+#define TC_SEG_WARP_BITS 1
+#endif
+constexpr bool SEG_WARP_BITS = TC_SEG_WARP_BITS != 0;
 
 void orient_geometry(const tc_ctx *ctx, int64_t nnz, int pieces, int *G, int64_t *chunk) {
   int64_t tiles = (nnz + ENTRY_TILE - 1) / ENTRY_TILE;
@@ -324,7 +330,7 @@ tc_status orient_phase_a(tc_ctx *ctx, const DevCSR &g, OrientBufs &b) {
                                                                     b.dv);
   TC_CHECK_LAUNCH(ctx);
   TC_TRY(exclusive_scan_i64(ctx, b.dnew, b.nrowptr, g.n + 1, b.sort_scratch, nullptr));
-  TC_CHECK_CUDA(ctx, cudaMemsetAsync(b.seg_counts, 0, sizeof(unsigned) * 3, ctx->stream));
+  TC_CHECK_CUDA(ctx, cudaMemsetAsync(b.seg_counts, 0, sizeof(unsigned) * 4, ctx->stream));
   classify_rows_kernel<<<grid_for(ctx, g.n, 256, 8), 256, 0, ctx->stream>>>(b.dnew, g.n, b.mid_list, b.big_list,
                                                                             b.huge_list, b.seg_counts);
   TC_CHECK_LAUNCH(ctx);
@@ -751,6 +757,90 @@ __global__ void __launch_bounds__(256) seg_sort_warpreg_kernel(const int64_t *__
   }
 }
 
+// Rows of SEG_WARP_MAX+1..SEG_SMEM_MAX entries without payload whose ids
+// span at most WB_WORDS * 32 values: one warp per row sorts through a
+// bitmap in its own 4 KB of shared memory, with no block barrier (most such
+// rows have a few hundred entries, too few to keep a block busy between its
+// barriers).  Bits are set with atomicOr; a total popcount different from
+// the row's length means duplicate ids (unvalidated input only).  Then the
+// words are read back 32 at a time, one per lane, and a warp prefix sum of
+// their popcounts gives each lane where its word's ids go, in order; each
+// word is zeroed as it is read.  Rows that do not fit (wider windows,
+// duplicates) are appended to `defer` for seg_sort_smem_kernel.
+constexpr int WB_WORDS = 1024;
+constexpr int WB_WARPS = 8;
+
+__global__ void __launch_bounds__(WB_WARPS * 32) seg_sort_warpbits_kernel(const int64_t *__restrict__ nrowptr,
+                                                                         const int32_t *__restrict__ list,
+                                                                         const unsigned *count,
+                                                                         int32_t *__restrict__ ncol,
+                                                                         int32_t *__restrict__ defer,
+                                                                         unsigned *defer_count) {
+  __shared__ uint32_t bits_all[WB_WARPS][WB_WORDS];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint32_t *bm = bits_all[w];
+  for (int q = lane; q < WB_WORDS; q += 32) bm[q] = 0u;
+  __syncwarp();
+  const unsigned cnt = *count;
+  const unsigned warps = gridDim.x * WB_WARPS;
+  for (unsigned i = blockIdx.x * WB_WARPS + w; i < cnt; i += warps) {
+    const int32_t r = list[i];
+    const int64_t b = nrowptr[r];
+    const int L = (int)(nrowptr[r + 1] - b);
+    int32_t lo = INT32_MAX, hi = INT32_MIN;
+    for (int k = lane; k < L; k += 32) {
+      const int32_t x = ncol[b + k];
+      lo = min(lo, x);
+      hi = max(hi, x);
+    }
+    lo = __reduce_min_sync(TC_FULL_MASK, lo);
+    hi = __reduce_max_sync(TC_FULL_MASK, hi);
+    const int64_t span = (int64_t)hi - lo + 1;
+    bool fits = L > 0 && span <= (int64_t)WB_WORDS * 32;
+    const int W = fits ? (int)((span + 31) >> 5) : 0;
+    if (fits) {
+      for (int k = lane; k < L; k += 32) {
+        const uint32_t d = (uint32_t)(ncol[b + k] - lo);
+        atomicOr(&bm[d >> 5], 1u << (d & 31));
+      }
+      __syncwarp();
+      int c = 0;
+      for (int q = lane; q < W; q += 32) c += __popc(bm[q]);
+      fits = __reduce_add_sync(TC_FULL_MASK, (unsigned)c) == (unsigned)L;
+      if (!fits) {  // duplicate ids: clear, then leave the row to the block sort
+        __syncwarp();
+        for (int q = lane; q < W; q += 32) bm[q] = 0u;
+      }
+    }
+    if (!fits) {
+      if (lane == 0) defer[atomicAdd(defer_count, 1u)] = r;
+      __syncwarp();
+      continue;
+    }
+    int base = 0;
+    for (int q0 = 0; q0 < W; q0 += 32) {
+      const int q = q0 + lane;
+      uint32_t word = q < W ? bm[q] : 0u;
+      if (q < W) bm[q] = 0u;
+      const int pc = __popc(word);
+      int incl = pc;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(TC_FULL_MASK, incl, o);
+        if (lane >= o) incl += t;
+      }
+      int at = base + incl - pc;
+      while (word) {
+        const int bit = __ffs(word) - 1;
+        word &= word - 1u;
+        ncol[b + at++] = lo + 32 * q + bit;
+      }
+      base += __shfl_sync(TC_FULL_MASK, incl, 31);
+    }
+    __syncwarp();
+  }
+}
+
 // Rows of 33..SEG_WARP_MAX entries: one warp per row sorts in its own slice
 // of shared memory with the same flip network (register stages for
 // distances below 32), synchronising with __syncwarp.
@@ -931,8 +1021,18 @@ static tc_status launch_row_sorts(tc_ctx *ctx, const DevCSR &g, OrientBufs &b) {
     seg_sort_warpsmem_kernel<VALS><<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(b.nrowptr, b.mid_list, b.seg_counts,
                                                                             b.ncol, pv);
   TC_CHECK_LAUNCH(ctx);
-  seg_sort_smem_kernel<VALS><<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(b.nrowptr, b.big_list, b.seg_counts + 1,
-                                                                        b.ncol, pv);
+  if (!VALS && SEG_WARP_BITS) {
+    // narrow rows through warp bitmaps; the rest (deferred into mid_list,
+    // which the warp sort above has finished with) through the block sort
+    seg_sort_warpbits_kernel<<<ctx->num_sms * 4, WB_WARPS * 32, 0, ctx->stream>>>(
+        b.nrowptr, b.big_list, b.seg_counts + 1, b.ncol, b.mid_list, b.seg_counts + 3);
+    TC_CHECK_LAUNCH(ctx);
+    seg_sort_smem_kernel<VALS><<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(b.nrowptr, b.mid_list, b.seg_counts + 3,
+                                                                          b.ncol, pv);
+  } else {
+    seg_sort_smem_kernel<VALS><<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(b.nrowptr, b.big_list, b.seg_counts + 1,
+                                                                          b.ncol, pv);
+  }
   TC_CHECK_LAUNCH(ctx);
   seg_sort_global_kernel<VALS><<<ctx->num_sms, 1024, 0, ctx->stream>>>(b.nrowptr, b.huge_list, b.seg_counts + 2,
                                                                        b.ncol, pv);

@@ -360,6 +360,32 @@ def test_long_rows_every_sort_class(engine):
     assert int(np.diff(drow).max()) > 4096
 
 
+def test_wide_rows_of_257_to_4096_entries(engine):
+    """Rows of 257..4096 relabelled entries whose ids span more than the
+    32768 of a warp bitmap: a circulant graph on G = 36120 vertices (each
+    joined to the 130 ids on either side) plus 140 hubs, hub j joined to the
+    G vertices j, j + 140, j + 280, ...  Every G vertex then has degree 261,
+    so their ranks follow their ids, and each hub (degree 258, ranked below
+    them) has a DAG row of 258 entries spanning about 36000 ranks: these
+    rows go past the warp bitmap sort to the block sort.  Totals and
+    per-edge counts against the oracle."""
+    G, half, hubs = 36120, 130, 140
+    i = np.repeat(np.arange(G), half)
+    j = (i + np.tile(np.arange(1, half + 1), G)) % G
+    h = np.repeat(np.arange(hubs), G // hubs)
+    t = h + hubs * np.tile(np.arange(G // hubs), hubs)
+    src = np.concatenate([i, G + h]).astype(np.int32)
+    dst = np.concatenate([j, t]).astype(np.int32)
+    rowptr, colidx = engine.csr_from_edges(G + hubs, src, dst)
+    ref_total, ref_pe, _, _ = oracle.triangles(rowptr, colidx, per_edge=True)
+    deg = np.diff(rowptr)
+    assert set(deg[:G]) == {2 * half + 1} and set(deg[G:]) == {G // hubs}
+    total, per_edge, _ = engine.count(rowptr, colidx, edge_counts=True)
+    assert total == ref_total
+    assert np.array_equal(per_edge, ref_pe)
+    assert engine.count(rowptr, colidx)[0] == ref_total  # total only: rows without payload
+
+
 def test_edge_list_entry_path(engine, golden):
     for case in golden:
         e = np.array(case["edges"], np.int64).reshape(-1, 2)
