@@ -106,18 +106,26 @@ __device__ int mlp_select(const float *__restrict__ w, const float *f, int lane,
 }
 
 // Grouping key of the PULL arm's counting sort (see the PULL section).
+// Hub targets (the top hub_span ids) are grouped per source block of
+// block_edges edges, key block * hub_span + (v - hub0); every other target
+// per source block of low_block_edges edges, key global0 + block * hub0 + v
+// (one such block when TC_PL_WIDE_BLOCKS is 0).
 struct PullKeys {
-  int64_t hub0;         // first hub id: n - min(n, hub_span)
-  int64_t hub_span;     // hub ids, one key per (source block, hub)
-  int64_t block_edges;  // edges per source block
-  int64_t global0;      // first key of the non-hub part: blocks * hub_span
-  // key of an edge u->v of tile t (a tile lies in one source block):
-  // key_in(block_base(t), v) = v >= hub0 ? block(t) * hub_span + (v - hub0) : global0 + v
+  int64_t hub0;             // first hub id: n - min(n, hub_span)
+  int64_t hub_span;         // hub ids, one key per (source block, hub)
+  int64_t block_edges;      // edges per source block of the hub part
+  int64_t global0;          // first key of the non-hub part: blocks * hub_span
+  int64_t low_block_edges;  // edges per source block of the non-hub part
+  // key of an edge u->v of tile t (a tile lies in one block of each part):
+  // key_in(block_base(t), low_base(t), v)
   __device__ __forceinline__ int64_t block_base(int64_t t) const {
     return (t * TILE_EDGES / block_edges) * hub_span - hub0;
   }
-  __device__ __forceinline__ int64_t key_in(int64_t base, int32_t v) const {
-    return v >= hub0 ? base + v : global0 + v;
+  __device__ __forceinline__ int64_t low_base(int64_t t) const {
+    return global0 + (t * TILE_EDGES / low_block_edges) * hub0;
+  }
+  __device__ __forceinline__ int64_t key_in(int64_t base, int64_t lbase, int32_t v) const {
+    return v >= hub0 ? base + v : lbase + v;
   }
 };
 
@@ -254,8 +262,8 @@ __global__ void __launch_bounds__(PLAN_THREADS) plan_kernel(DevDag g, int64_t T,
   arm = __shfl_sync(TC_FULL_MASK, arm, 0);
   if (lane < TC_MLP_FEATURES) feats[t * TC_MLP_FEATURES + lane] = f[lane];
   if (arm == TC_ARM_PULL) {
-    const int64_t kb = pk.block_base(t);
-    for (int64_t e = e0 + lane; e < e1; e += 32) atomicAdd(pull_cnt + pk.key_in(kb, g.col[e]), 1u);
+    const int64_t kb = pk.block_base(t), lb = pk.low_base(t);
+    for (int64_t e = e0 + lane; e < e1; e += 32) atomicAdd(pull_cnt + pk.key_in(kb, lb, g.col[e]), 1u);
   }
   if (lane == 0) {
     arm_out[t] = arm;
@@ -1348,12 +1356,21 @@ constexpr int PL_DUNROLL = 2;  // dense edges: 16-byte word loads in flight per 
 // order, and the PULL kernel's warps, which take work in order, then probe
 // the rows of about one block at a time, a slice of the DAG small enough to
 // stay in L2.  Every other target (few in-edges; its list may need the hash
-// table) is grouped over all blocks at once, key B * PL_HUB + v, so its runs
-// are not split block by block.
+// table) is grouped over all blocks at once, after all hub groups (see
+// PullKeys), so its runs are not split block by block.
 constexpr int64_t PL_HUB = (int64_t)PL_WORDS * 32;  // 65536
 // tiles per source block: ctx->pull_block_tiles (default 2560 tiles = 10.5M
 // edges, 42 MB of adjacency; tc_tuning)
 constexpr int PL_MAX_BLOCKS = 64;
+// 1: targets outside the hubs are grouped per source block too, so the row
+// suffixes their runs probe are a block's rows; 0 (default): over all blocks
+// at once, longer runs.  R-MAT scale 24 with 1: 62.96 ms per step against
+// 56.22 (pull_kernel 35.2 against 30.4 ms): the extra runs and table builds
+// cost more than the L2-resident suffixes save.
+#ifndef TC_PL_WIDE_BLOCKS
+#define TC_PL_WIDE_BLOCKS 0
+#endif
+constexpr int64_t PL_LOW_KEY_BUDGET = (int64_t)1 << 28;  // keys of the non-hub part (1 GB of counters)
 
 
 // pos[key] starts at the exclusive scan of the histogram; each edge takes the
@@ -1374,7 +1391,7 @@ __global__ void __launch_bounds__(PL_GROUP_THREADS) pull_scatter_kernel(const in
   constexpr int U = PL_SCATTER_UNROLL;  // edges per thread in flight: their atomics overlap
   for (int64_t t = blockIdx.x; t < T; t += gridDim.x) {
     if (arm[t] != TC_ARM_PULL) continue;
-    const int64_t e1 = min(m, (t + 1) * TILE_EDGES), kb = pk.block_base(t);
+    const int64_t e1 = min(m, (t + 1) * TILE_EDGES), kb = pk.block_base(t), lb = pk.low_base(t);
     for (int64_t eb = t * TILE_EDGES + threadIdx.x; eb < e1; eb += U * PL_GROUP_THREADS) {
       int64_t key[U];
       int32_t r[U];
@@ -1385,7 +1402,7 @@ __global__ void __launch_bounds__(PL_GROUP_THREADS) pull_scatter_kernel(const in
         key[u] = -1;
         r[u] = 0;
         if (e < e1) {  // read once: streamed past L2, which keeps the counters
-          key[u] = pk.key_in(kb, PL_SCATTER_STREAM ? __ldcs(col + e) : __ldg(col + e));
+          key[u] = pk.key_in(kb, lb, PL_SCATTER_STREAM ? __ldcs(col + e) : __ldg(col + e));
           r[u] = PL_SCATTER_STREAM ? __ldcs(src + e) : __ldg(src + e);
         }
       }
@@ -1470,6 +1487,24 @@ __device__ __forceinline__ uint2 pull_rec(const uint2 *__restrict__ er, int64_t 
   return TC_PULL_ER_STREAM ? __ldcs(er + i) : er[i];
 }
 
+// Hash runs (targets whose list spans more than the bitmap window) probe
+// row suffixes of sources anywhere in the DAG, mostly DRAM misses: with
+// TC_PL_HASH_PREFETCH 1 the next batch's suffixes (relabelled DAG: entries
+// e + 1 .. row end) are prefetched into L2 while this batch is probed, and
+// a pack's before its tables are built, as the 16-byte blocks that hold
+// them (the blocks lie in the column array).  Off: at R-MAT scale 24
+// pull_kernel took 31.11 ms with it against 30.73 without.
+#ifndef TC_PL_HASH_PREFETCH
+#define TC_PL_HASH_PREFETCH 0
+#endif
+__device__ __forceinline__ void prefetch_suffix(const DevDag &g, int64_t e, uint32_t row_end) {
+  const int64_t a0 = e + 1;
+  if ((int64_t)row_end <= a0) return;
+  const uintptr_t lo = reinterpret_cast<uintptr_t>(g.col + a0) & ~(uintptr_t)15;
+  const uintptr_t hi = (reinterpret_cast<uintptr_t>(g.col + row_end) + 15) & ~(uintptr_t)15;
+  bulk_prefetch_l2(reinterpret_cast<const void *>(lo), (uint32_t)min((uintptr_t)65536, hi - lo));
+}
+
 // Dense edges (DENSE, bitmap tables of hub targets only): the table's base is
 // hub0 + 128 * woff4, so its 16-byte word j lines up with word woff4 + j of
 // every hub bit row; tw4 16-byte words cover it.
@@ -1502,6 +1537,7 @@ __device__ __forceinline__ void pull_run(const DevDag &g, const uint2 *__restric
       const uint2 p = pull_rec(er, qb + 32 + lane);
       e_n = p.x;
       y_n = p.y;
+      if (!BITMAP && TC_PL_HASH_PREFETCH && g.restrict_after && have_b) prefetch_suffix(g, e_n, y_n);
     }
     int64_t a0 = 0;
     int na = 0;
@@ -1668,6 +1704,11 @@ __device__ __forceinline__ void pull_run(const DevDag &g, const uint2 *__restric
 #define TC_PL_PACK 1
 #endif
 constexpr int PK_NB = 256;
+#ifndef TC_PK_LOAD
+#define TC_PK_LOAD 1  // 1 or 2: a table then is at most a quarter or half full
+#endif
+constexpr int PK_LOAD = TC_PK_LOAD;  // packed tables: entries per bucket on average (1 or 2)
+static_assert(PK_LOAD == 1 || PK_LOAD == 2, "a packed table must keep a free slot");
 constexpr int PK_TSEL = PL_WORDS - 32;
 
 // Lane j stands for record k + j; `v` is record k's target and `vw` the
@@ -1694,7 +1735,7 @@ __device__ __forceinline__ int64_t pull_pack(const DevDag &g, const uint2 *__res
     if (nb > 0 && nb <= PK_NB) {
       const uint32_t span = (uint32_t)(__ldg(g.col + bb + nb - 1) - __ldg(g.col + bb)) + 1u;
       if (span > (uint32_t)PL_WORDS * 32u) {  // a hash target, as in the single-run rule
-        while ((1 << bits) < nb) ++bits;
+        while ((1 << bits) < (nb + PK_LOAD - 1) / PK_LOAD) ++bits;  // at most PK_LOAD entries per 4-slot bucket on average
         words = 4 << bits;
         ok = true;
       }
@@ -1723,6 +1764,17 @@ __device__ __forceinline__ int64_t pull_pack(const DevDag &g, const uint2 *__res
     sb.ed[__popc(inc & lanemask_lt())] =
         make_int4(ni, (wi - words) | (bits << 16), (int)(uint32_t)(uint64_t)base, (int)((uint64_t)base >> 32));
   }
+  // the pack's records first, so that (hash-run prefetch) their row
+  // suffixes are on the way to L2 while the tables are built
+  const bool mine = lane < ne;
+  int64_t e = -1;
+  uint32_t y = 0;
+  if (mine) {
+    const uint2 p = pull_rec(er, k + lane);
+    e = p.x;
+    y = p.y;
+    if (TC_PL_HASH_PREFETCH && g.restrict_after) prefetch_suffix(g, e, y);
+  }
   __syncwarp();
   {  // build: the runs' lists as one flattened sequence, PL_UNROLL loads in flight per lane
     int c = 0;
@@ -1749,7 +1801,7 @@ __device__ __forceinline__ int64_t pull_pack(const DevDag &g, const uint2 *__res
         const int tbits = (int)(ts[u] >> 16);
         const uint32_t mask = (1u << tbits) - 1u, val = (uint32_t)x[u] + 1u;
         uint32_t b = hslot(x[u], tbits);
-        for (;;) {  // ends: every table is at most a quarter full
+        for (;;) {  // ends: every table is at most half full (PK_LOAD <= 2)
           uint32_t *bk = T + 4 * b;
           if (atomicCAS(bk, 0u, val) == 0u || atomicCAS(bk + 1, 0u, val) == 0u || atomicCAS(bk + 2, 0u, val) == 0u ||
               atomicCAS(bk + 3, 0u, val) == 0u)
@@ -1760,15 +1812,7 @@ __device__ __forceinline__ int64_t pull_pack(const DevDag &g, const uint2 *__res
     }
   }
   __syncwarp();
-  const bool mine = lane < ne;
   const uint32_t tsel = mine ? (uint32_t)sb.ed[__popc(inc & (lanemask_lt() | (1u << lane))) - 1].y : 0u;
-  int64_t e = -1;
-  uint32_t y = 0;
-  if (mine) {
-    const uint2 p = pull_rec(er, k + lane);
-    e = p.x;
-    y = p.y;
-  }
   int64_t a0 = 0;
   int na = 0;
   if (mine) {
@@ -2172,16 +2216,25 @@ static_assert(PIN_BYTES + TC_NUM_ARMS <= 64, "pinned scratch holds 64 words");
 static_assert(sizeof(((tc_ctx *)nullptr)->ev) / sizeof(cudaEvent_t) >= 10 + TC_NUM_ARMS, "one event per arm");
 
 // Number of keys of the PULL grouping of a graph with n vertices and T tiles.
+// The non-hub part takes hub0 keys per block; its blocks are the hub part's
+// (TC_PL_WIDE_BLOCKS 1) as far as PL_LOW_KEY_BUDGET keys allow, else coarser.
 static int64_t pull_key_count(int64_t n, int64_t T, int block_tiles, PullKeys *pk) {
   const int64_t per_block = std::max<int64_t>(block_tiles, (T + PL_MAX_BLOCKS - 1) / PL_MAX_BLOCKS);
   const int64_t blocks = std::max<int64_t>(1, (T + per_block - 1) / per_block);
+  const int64_t hub0 = n - std::min<int64_t>(n, PL_HUB);
+  int64_t low_blocks = 1;
+  if (TC_PL_WIDE_BLOCKS && hub0 > 0)
+    low_blocks = std::max<int64_t>(1, std::min<int64_t>(blocks, PL_LOW_KEY_BUDGET / hub0));
+  const int64_t low_per_block = std::max<int64_t>(1, (T + low_blocks - 1) / low_blocks);
+  low_blocks = std::max<int64_t>(1, (T + low_per_block - 1) / low_per_block);
   if (pk) {
     pk->hub_span = PL_HUB;
-    pk->hub0 = n - std::min<int64_t>(n, PL_HUB);
+    pk->hub0 = hub0;
     pk->block_edges = per_block * TILE_EDGES;
     pk->global0 = blocks * PL_HUB;
+    pk->low_block_edges = low_per_block * TILE_EDGES;
   }
-  return blocks * PL_HUB + n;
+  return blocks * PL_HUB + low_blocks * hub0;
 }
 
 // PULL arm: group the PULL tiles' edges (one counting sort: plan_kernel

@@ -150,6 +150,12 @@ __device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32
                : "memory");
 }
 
+// Bulk prefetch of [src, src + bytes) into L2 (no registers held, no
+// completion to wait for): src 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_prefetch_l2(const void *src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
+
 // True once the mbarrier phase of the given parity has completed.
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   uint32_t ok;
