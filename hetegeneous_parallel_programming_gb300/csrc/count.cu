@@ -27,6 +27,19 @@ constexpr int BM_THREADS = 512;
 constexpr int BM_SMEM_BYTES = 100 * 1024;
 constexpr int64_t BM_BITS = (int64_t)BM_SMEM_BYTES * 8;
 constexpr int PLAN_THREADS = 256;
+// 1: the planner visits tiles interleaved over the PULL source blocks, so
+// the SMs' histogram atomics at any moment go to different blocks' hub keys
+// instead of all to the hot hubs of one block (R-MAT scale 24: plan 3.88 ->
+// 2.80 ms).  The scatter keeps tile order (PL_SCATTER_INTERLEAVE 0): spread
+// over the blocks, its record stores lose locality (PULL arm +1.3 ms).
+#ifndef TC_PL_INTERLEAVE
+#define TC_PL_INTERLEAVE 1
+#endif
+constexpr bool PL_INTERLEAVE = TC_PL_INTERLEAVE != 0;
+#ifndef TC_PL_SCATTER_INTERLEAVE
+#define TC_PL_SCATTER_INTERLEAVE 0
+#endif
+constexpr bool PL_SCATTER_INTERLEAVE = TC_PL_SCATTER_INTERLEAVE != 0;
 #ifndef TC_PLAN_UNROLL
 #define TC_PLAN_UNROLL 2
 #endif
@@ -147,8 +160,13 @@ __global__ void __launch_bounds__(PLAN_THREADS) plan_kernel(DevDag g, int64_t T,
       s_w[i] = __bfloat162float(__float2bfloat16(mlp[i]));
     __syncthreads();
   }
-  const int64_t t = (int64_t)blockIdx.x * (PLAN_THREADS / 32) + (threadIdx.x >> 5);
-  if (t >= T) return;
+  // tiles interleaved over the PULL source blocks (see PL_INTERLEAVE): the
+  // grid covers S * per slots, some past the last tile
+  const int64_t per = pk.block_edges / TILE_EDGES, S = (T + per - 1) / per;
+  const int64_t i = (int64_t)blockIdx.x * (PLAN_THREADS / 32) + (threadIdx.x >> 5);
+  const bool lv = PL_INTERLEAVE && S > 1;
+  const int64_t t = lv ? (i % S) * per + i / S : i;
+  if (i >= (lv ? S * per : T) || t >= T) return;
   const int64_t e0 = t * TILE_EDGES, e1 = min(g.m, e0 + TILE_EDGES);
   float sda = 0, sdb = 0, smin = 0, smax = 0, salr = 0, sin = 0;
   float bins[6] = {0, 0, 0, 0, 0, 0};
@@ -1389,8 +1407,11 @@ __global__ void __launch_bounds__(PL_GROUP_THREADS) pull_scatter_kernel(const in
                                                                        uint2 *__restrict__ er) {
   const int64_t T = (m + TILE_EDGES - 1) / TILE_EDGES;
   constexpr int U = PL_SCATTER_UNROLL;  // edges per thread in flight: their atomics overlap
-  for (int64_t t = blockIdx.x; t < T; t += gridDim.x) {
-    if (arm[t] != TC_ARM_PULL) continue;
+  // tiles in order, or interleaved over the source blocks (see PL_INTERLEAVE)
+  const int64_t per = pk.block_edges / TILE_EDGES, S = (T + per - 1) / per;
+  for (int64_t i = blockIdx.x; i < (PL_SCATTER_INTERLEAVE ? S * per : T); i += gridDim.x) {
+    const int64_t t = PL_SCATTER_INTERLEAVE ? (i % S) * per + i / S : i;
+    if (t >= T || arm[t] != TC_ARM_PULL) continue;
     const int64_t e1 = min(m, (t + 1) * TILE_EDGES), kb = pk.block_base(t), lb = pk.low_base(t);
     for (int64_t eb = t * TILE_EDGES + threadIdx.x; eb < e1; eb += U * PL_GROUP_THREADS) {
       int64_t key[U];
@@ -2350,10 +2371,12 @@ tc_status run_count(tc_ctx *ctx, const DevDag &g_in, const tc_opts &opts, CountB
     TC_CHECK_CUDA(ctx, cudaMemsetAsync(cb.qoff, 0, sizeof(int64_t) * (TC_NUM_ARMS + 1), ctx->stream));
     TC_CHECK_CUDA(ctx, cudaMemsetAsync(cb.arm_bytes, 0, sizeof(unsigned long long) * TC_NUM_ARMS, ctx->stream));
   } else {
-    const int plan_blocks = (int)((T + (PLAN_THREADS / 32) - 1) / (PLAN_THREADS / 32));
     const size_t plan_smem = opts.selector == TC_SELECT_LEARNED ? TC_MLP_PARAM_COUNT * sizeof(float) : 0;
     PullKeys pk;
     const int64_t K = pull_key_count(g.n, T, ctx->pull_block_tiles, &pk);
+    const int64_t per = pk.block_edges / TILE_EDGES, S = (T + per - 1) / per;
+    const int64_t slots = PL_INTERLEAVE && S > 1 ? S * per : T;
+    const int plan_blocks = (int)((slots + (PLAN_THREADS / 32) - 1) / (PLAN_THREADS / 32));
     TC_CHECK_CUDA(ctx, cudaMemsetAsync(cb.pull_pos, 0, sizeof(uint32_t) * (K + 1), ctx->stream));
     plan_kernel<<<plan_blocks, PLAN_THREADS, plan_smem, ctx->stream>>>(g, T, opts.selector, opts.force_arm,
                                                                        ctx->d_mlp, cb.features, cb.arm, cb.qkeys0,
