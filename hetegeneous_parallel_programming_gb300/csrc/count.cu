@@ -30,8 +30,10 @@ constexpr int PLAN_THREADS = 256;
 // 1: the planner visits tiles interleaved over the PULL source blocks, so
 // the SMs' histogram atomics at any moment go to different blocks' hub keys
 // instead of all to the hot hubs of one block (R-MAT scale 24: plan 3.88 ->
-// 2.80 ms).  The scatter keeps tile order (PL_SCATTER_INTERLEAVE 0): spread
-// over the blocks, its record stores lose locality (PULL arm +1.3 ms).
+// 2.80 ms).  The scatter keeps tile order (PL_SCATTER_INTERLEAVE 0): the
+// records of a target group then follow the rows' order, which the probing
+// kernel's suffix loads profit from; interleaved tile by tile, or in chunks
+// of 64 or 256 tiles, the PULL arm took 1.3, 1.4 and 1.7 ms longer.
 #ifndef TC_PL_INTERLEAVE
 #define TC_PL_INTERLEAVE 1
 #endif
@@ -40,6 +42,10 @@ constexpr bool PL_INTERLEAVE = TC_PL_INTERLEAVE != 0;
 #define TC_PL_SCATTER_INTERLEAVE 0
 #endif
 constexpr bool PL_SCATTER_INTERLEAVE = TC_PL_SCATTER_INTERLEAVE != 0;
+#ifndef TC_PL_SCATTER_GRAIN
+#define TC_PL_SCATTER_GRAIN 1
+#endif
+constexpr int64_t PL_SCATTER_GRAIN = TC_PL_SCATTER_GRAIN;  // tiles per interleaved chunk of the scatter
 #ifndef TC_PLAN_UNROLL
 #define TC_PLAN_UNROLL 2
 #endif
@@ -1407,10 +1413,14 @@ __global__ void __launch_bounds__(PL_GROUP_THREADS) pull_scatter_kernel(const in
                                                                        uint2 *__restrict__ er) {
   const int64_t T = (m + TILE_EDGES - 1) / TILE_EDGES;
   constexpr int U = PL_SCATTER_UNROLL;  // edges per thread in flight: their atomics overlap
-  // tiles in order, or interleaved over the source blocks (see PL_INTERLEAVE)
+  // tiles in order, or chunks of PL_SCATTER_GRAIN tiles interleaved over the
+  // source blocks (see PL_INTERLEAVE)
   const int64_t per = pk.block_edges / TILE_EDGES, S = (T + per - 1) / per;
-  for (int64_t i = blockIdx.x; i < (PL_SCATTER_INTERLEAVE ? S * per : T); i += gridDim.x) {
-    const int64_t t = PL_SCATTER_INTERLEAVE ? (i % S) * per + i / S : i;
+  const bool il = PL_SCATTER_INTERLEAVE && S > 1 && per % PL_SCATTER_GRAIN == 0;
+  const int64_t cpb = per / PL_SCATTER_GRAIN;  // chunks per source block
+  for (int64_t i = blockIdx.x; i < (il ? S * per : T); i += gridDim.x) {
+    const int64_t c = i / PL_SCATTER_GRAIN;
+    const int64_t t = il ? ((c % S) * cpb + c / S) * PL_SCATTER_GRAIN + i % PL_SCATTER_GRAIN : i;
     if (t >= T || arm[t] != TC_ARM_PULL) continue;
     const int64_t e1 = min(m, (t + 1) * TILE_EDGES), kb = pk.block_base(t), lb = pk.low_base(t);
     for (int64_t eb = t * TILE_EDGES + threadIdx.x; eb < e1; eb += U * PL_GROUP_THREADS) {
