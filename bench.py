@@ -422,8 +422,13 @@ def engine_arm(args, rank, world, local_rank, dist):
                                   "label_classes": 4, "sum_over_classes_equals_T": True}
         del lab
     # e2e through the public API with pinned host buffers (H2D + D2H inside)
-    rowptr_h = rowptr.cpu().pin_memory()
-    colidx_h = colidx.cpu().pin_memory()
+    # pinned host buffers allocated as such and filled from the device (no
+    # pageable intermediate of several GB freed just before the timed region)
+    rowptr_h = torch.empty(rowptr.shape, dtype=rowptr.dtype, pin_memory=True)
+    colidx_h = torch.empty(colidx.shape, dtype=colidx.dtype, pin_memory=True)
+    rowptr_h.copy_(rowptr)
+    colidx_h.copy_(colidx)
+    torch.cuda.synchronize()
     ms_e2e, (tot_e2e, st_e2e), e2e_steps = timed_steps(
         lambda: eng.count_host_ptr(n, nnz, rowptr_h.data_ptr(), colidx_h.data_ptr(), selector=best),
         args.steps, args.warmup, eng, torch, dist)
