@@ -13,13 +13,21 @@ namespace tc {
 
 constexpr int OR_THREADS = 256;
 constexpr int OR_PER = ENTRY_TILE / OR_THREADS;  // 8 entries per thread per tile
-// 1: the placement writes every relabelled entry's row (nsrc) next to its
-// column; 0: a streaming pass derives the rows from the relabelled row
-// pointers afterwards (sequential writes instead of scattered ones)
+// Every relabelled entry's row (nsrc): 1: the placement writes it next to
+// its column (a second scattered store per entry); 2: the row sorts write it,
+// coalesced, for the rows they visit (rows of one entry included); 0: a
+// streaming pass derives it from the relabelled row pointers afterwards
 #ifndef TC_PLACE_SRC
-#define TC_PLACE_SRC 1
+#define TC_PLACE_SRC 2
 #endif
-constexpr bool PLACE_SRC = TC_PLACE_SRC != 0;
+constexpr bool PLACE_SRC = TC_PLACE_SRC == 1;
+constexpr bool SORT_SRC = TC_PLACE_SRC == 2;
+
+// src[b .. b + L) = r by threads tid, tid + nt, ... (the row sorts' nsrc writes)
+__device__ __forceinline__ void put_row_src(int32_t *__restrict__ src, int64_t b, int L, int32_t r, int tid, int nt) {
+  if (src)
+    for (int k = tid; k < L; k += nt) src[b + k] = r;
+}
 // 1: rows of <= 32 entries are sorted by a warp per 32 consecutive rows
 #ifndef TC_SEG_WARP_CHUNK
 #define TC_SEG_WARP_CHUNK 1
@@ -532,12 +540,13 @@ __device__ void hybrid_flip_bitonic(int32_t *key, uint32_t *val, int L, int warp
 
 template <bool VALS>
 __global__ void seg_sort_warp_kernel(const int64_t *__restrict__ nrowptr, int64_t n, int32_t *__restrict__ ncol,
-                                     uint32_t *__restrict__ perm) {
+                                     uint32_t *__restrict__ perm, int32_t *__restrict__ src) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += warps) {
     const int64_t b = nrowptr[r];
     const int L = (int)(nrowptr[r + 1] - b);
+    if (L <= 32) put_row_src(src, b, L, (int32_t)r, lane, 32);
     if (L < 2 || L > 32) continue;
     int32_t key = lane < L ? ncol[b + lane] : INT32_MAX;
     uint32_t val = (VALS && lane < L) ? perm[b + lane] : 0u;
@@ -601,7 +610,8 @@ __device__ __forceinline__ void warp_sort32(int32_t &key, uint32_t &val, int L, 
 
 template <bool VALS>
 __global__ void seg_sort_warp_chunk_kernel(const int64_t *__restrict__ nrowptr, int64_t n,
-                                           int32_t *__restrict__ ncol, uint32_t *__restrict__ perm) {
+                                           int32_t *__restrict__ ncol, uint32_t *__restrict__ perm,
+                                           int32_t *__restrict__ src) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   for (int64_t r0 = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; r0 < n; r0 += warps * 32) {
@@ -625,6 +635,7 @@ __global__ void seg_sort_warp_chunk_kernel(const int64_t *__restrict__ nrowptr, 
         key = (L >= 2 && L <= 32 && lane < L) ? ncol[b + lane] : INT32_MAX;
         val = (VALS && L >= 2 && L <= 32 && lane < L) ? perm[b + lane] : 0u;
       }
+      if (Lj <= 32) put_row_src(src, bj, Lj, (int32_t)(r0 + j), lane, 32);
       if (Lj < 2 || Lj > 32) continue;  // warp-uniform
       warp_sort32<VALS>(kj, vj, Lj, lane);
       if (lane < Lj) {
@@ -742,7 +753,7 @@ template <bool VALS>
 __global__ void __launch_bounds__(256) seg_sort_warpreg_kernel(const int64_t *__restrict__ nrowptr,
                                                               const int32_t *__restrict__ list,
                                                               const unsigned *count, int32_t *__restrict__ ncol,
-                                                              uint32_t *__restrict__ perm) {
+                                                              uint32_t *__restrict__ perm, int32_t *__restrict__ src) {
   static_assert(SEG_WARP_MAX == 256, "rows of up to 8 keys per lane");
   const int lane = threadIdx.x & 31;
   const unsigned cnt = *count;
@@ -754,6 +765,7 @@ __global__ void __launch_bounds__(256) seg_sort_warpreg_kernel(const int64_t *__
     if (L <= 64) warp_sort_row_blocked<2, VALS>(ncol, perm, b, L, lane);
     else if (L <= 128) warp_sort_row_blocked<4, VALS>(ncol, perm, b, L, lane);
     else warp_sort_row_blocked<8, VALS>(ncol, perm, b, L, lane);
+    put_row_src(src, b, L, r, lane, 32);
   }
 }
 
@@ -775,7 +787,8 @@ __global__ void __launch_bounds__(WB_WARPS * 32) seg_sort_warpbits_kernel(const 
                                                                          const unsigned *count,
                                                                          int32_t *__restrict__ ncol,
                                                                          int32_t *__restrict__ defer,
-                                                                         unsigned *defer_count) {
+                                                                         unsigned *defer_count,
+                                                                         int32_t *__restrict__ src) {
   __shared__ uint32_t bits_all[WB_WARPS][WB_WORDS];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   uint32_t *bm = bits_all[w];
@@ -837,6 +850,7 @@ __global__ void __launch_bounds__(WB_WARPS * 32) seg_sort_warpbits_kernel(const 
       }
       base += __shfl_sync(TC_FULL_MASK, incl, 31);
     }
+    put_row_src(src, b, L, r, lane, 32);
     __syncwarp();
   }
 }
@@ -848,7 +862,7 @@ template <bool VALS>
 __global__ void __launch_bounds__(256) seg_sort_warpsmem_kernel(const int64_t *__restrict__ nrowptr,
                                                                const int32_t *__restrict__ list,
                                                                const unsigned *count, int32_t *__restrict__ ncol,
-                                                               uint32_t *__restrict__ perm) {
+                                                               uint32_t *__restrict__ perm, int32_t *__restrict__ src) {
   __shared__ int32_t skey_all[8][SEG_WARP_MAX];
   __shared__ uint32_t sval_all[VALS ? 8 : 1][VALS ? SEG_WARP_MAX : 1];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -870,6 +884,7 @@ __global__ void __launch_bounds__(256) seg_sort_warpsmem_kernel(const int64_t *_
       ncol[b + k] = key[k];
       if (VALS) perm[b + k] = val[k];
     }
+    put_row_src(src, b, L, r, lane, 32);
     __syncwarp();
   }
 }
@@ -883,7 +898,8 @@ constexpr int SEG_BITMAP_KEYS = SEG_SMEM_MAX / 256;  // keys per thread (256 thr
 template <bool VALS>
 __global__ void __launch_bounds__(256) seg_sort_smem_kernel(const int64_t *__restrict__ nrowptr,
                                                            const int32_t *__restrict__ list, const unsigned *count,
-                                                           int32_t *__restrict__ ncol, uint32_t *__restrict__ perm) {
+                                                           int32_t *__restrict__ ncol, uint32_t *__restrict__ perm,
+                                                           int32_t *__restrict__ src) {
   __shared__ int32_t skey[SEG_SMEM_MAX];
   __shared__ uint32_t sval[VALS ? SEG_SMEM_MAX : 1];
   __shared__ int32_t s_red[2][8];
@@ -894,6 +910,7 @@ __global__ void __launch_bounds__(256) seg_sort_smem_kernel(const int64_t *__res
     const int32_t r = list[i];
     const int64_t b = nrowptr[r];
     const int L = (int)(nrowptr[r + 1] - b);
+    put_row_src(src, b, L, r, threadIdx.x, blockDim.x);  // the row's entries stay in it
     if (!VALS) {
       int32_t x[SEG_BITMAP_KEYS];
       int32_t lo = 0x7fffffff, hi = -1;
@@ -992,12 +1009,13 @@ __global__ void __launch_bounds__(256) seg_sort_smem_kernel(const int64_t *__res
 template <bool VALS>
 __global__ void __launch_bounds__(1024) seg_sort_global_kernel(const int64_t *__restrict__ nrowptr,
                                                               const int32_t *__restrict__ list, const unsigned *count,
-                                                              int32_t *ncol, uint32_t *perm) {
+                                                              int32_t *ncol, uint32_t *perm, int32_t *src) {
   const unsigned cnt = *count;
   for (unsigned i = blockIdx.x; i < cnt; i += gridDim.x) {
     const int32_t r = list[i];
     const int64_t b = nrowptr[r];
     const int L = (int)(nrowptr[r + 1] - b);
+    put_row_src(src, b, L, r, threadIdx.x, blockDim.x);
     block_flip_bitonic<VALS>(ncol + b, VALS ? perm + b : nullptr, L);
     __syncthreads();
   }
@@ -1008,34 +1026,36 @@ __global__ void __launch_bounds__(1024) seg_sort_global_kernel(const int64_t *__
 template <bool VALS>
 static tc_status launch_row_sorts(tc_ctx *ctx, const DevCSR &g, OrientBufs &b) {
   uint32_t *pv = VALS ? b.perm : nullptr;
+  int32_t *sv = SORT_SRC ? b.nsrc : nullptr;  // rows written by the sorts (every row visits one)
   if (SEG_WARP_CHUNK)
     seg_sort_warp_chunk_kernel<VALS><<<grid_for(ctx, g.n, 256, 8), 256, 0, ctx->stream>>>(b.nrowptr, g.n, b.ncol,
-                                                                                          pv);
+                                                                                          pv, sv);
   else
-    seg_sort_warp_kernel<VALS><<<grid_for(ctx, g.n * 32, 256, 8), 256, 0, ctx->stream>>>(b.nrowptr, g.n, b.ncol, pv);
+    seg_sort_warp_kernel<VALS><<<grid_for(ctx, g.n * 32, 256, 8), 256, 0, ctx->stream>>>(b.nrowptr, g.n, b.ncol, pv,
+                                                                                         sv);
   TC_CHECK_LAUNCH(ctx);
   if (SEG_WARP_REG)
     seg_sort_warpreg_kernel<VALS><<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(b.nrowptr, b.mid_list, b.seg_counts,
-                                                                            b.ncol, pv);
+                                                                            b.ncol, pv, sv);
   else
     seg_sort_warpsmem_kernel<VALS><<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(b.nrowptr, b.mid_list, b.seg_counts,
-                                                                            b.ncol, pv);
+                                                                            b.ncol, pv, sv);
   TC_CHECK_LAUNCH(ctx);
   if (!VALS && SEG_WARP_BITS) {
     // narrow rows through warp bitmaps; the rest (deferred into mid_list,
     // which the warp sort above has finished with) through the block sort
     seg_sort_warpbits_kernel<<<ctx->num_sms * 4, WB_WARPS * 32, 0, ctx->stream>>>(
-        b.nrowptr, b.big_list, b.seg_counts + 1, b.ncol, b.mid_list, b.seg_counts + 3);
+        b.nrowptr, b.big_list, b.seg_counts + 1, b.ncol, b.mid_list, b.seg_counts + 3, sv);
     TC_CHECK_LAUNCH(ctx);
     seg_sort_smem_kernel<VALS><<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(b.nrowptr, b.mid_list, b.seg_counts + 3,
-                                                                          b.ncol, pv);
+                                                                          b.ncol, pv, sv);
   } else {
     seg_sort_smem_kernel<VALS><<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(b.nrowptr, b.big_list, b.seg_counts + 1,
-                                                                          b.ncol, pv);
+                                                                          b.ncol, pv, sv);
   }
   TC_CHECK_LAUNCH(ctx);
   seg_sort_global_kernel<VALS><<<ctx->num_sms, 1024, 0, ctx->stream>>>(b.nrowptr, b.huge_list, b.seg_counts + 2,
-                                                                       b.ncol, pv);
+                                                                       b.ncol, pv, sv);
   TC_CHECK_LAUNCH(ctx);
   return TC_OK;
 }
@@ -1060,7 +1080,7 @@ tc_status orient_phase_b(tc_ctx *ctx, const DevCSR &g, OrientBufs &b, int64_t m,
   // the row sorts keep entries inside their rows, so every entry's row
   // (nsrc) is the same before and after them
   if (m > 1) TC_TRY(want_perm ? launch_row_sorts<true>(ctx, g, b) : launch_row_sorts<false>(ctx, g, b));
-  if (!PLACE_SRC) TC_TRY(launch_expand_src(ctx, b.nrowptr, g.n, m, b.nsrc));
+  if (TC_PLACE_SRC == 0 || (SORT_SRC && m <= 1)) TC_TRY(launch_expand_src(ctx, b.nrowptr, g.n, m, b.nsrc));
   out->n = g.n;
   out->m = m;
   out->rowptr = b.nrowptr;
