@@ -662,6 +662,7 @@ __device__ __forceinline__ void reg_keep(int32_t &k, uint32_t &v, int32_t ok, ui
 
 template <int E, bool VALS>
 __device__ __forceinline__ void warp_sort_blocked(int32_t (&k)[E], uint32_t (&v)[E], int lane) {
+  static_assert(E >= 2 && (E & (E - 1)) == 0, "2, 4, 8, ... keys per lane");
   constexpr int P = 32 * E;
 #pragma unroll
   for (int lv = 2; lv <= P; lv <<= 1) {
@@ -681,17 +682,19 @@ __device__ __forceinline__ void warp_sort_blocked(int32_t (&k)[E], uint32_t (&v)
         }
       }
     } else {
+      // entries x and E-1-x trade with the partner's E-1-x and x: both keys
+      // are read before either is replaced, so no second key array is held
       const int pl = lane ^ (lv / E - 1);
       const bool lower = ((lane * E) & (lv >> 1)) == 0;
-      int32_t ok[E];
-      uint32_t ov[E];
 #pragma unroll
-      for (int x = 0; x < E; ++x) {
-        ok[x] = __shfl_sync(TC_FULL_MASK, k[E - 1 - x], pl);
-        if (VALS) ov[x] = __shfl_sync(TC_FULL_MASK, v[E - 1 - x], pl);
+      for (int x = 0; x < E / 2; ++x) {
+        const int y = E - 1 - x;
+        const int32_t o1 = __shfl_sync(TC_FULL_MASK, k[y], pl), o2 = __shfl_sync(TC_FULL_MASK, k[x], pl);
+        const uint32_t w1 = VALS ? __shfl_sync(TC_FULL_MASK, v[y], pl) : 0u;
+        const uint32_t w2 = VALS ? __shfl_sync(TC_FULL_MASK, v[x], pl) : 0u;
+        reg_keep<VALS>(k[x], v[x], o1, w1, lower);
+        reg_keep<VALS>(k[y], v[y], o2, w2, lower);
       }
-#pragma unroll
-      for (int x = 0; x < E; ++x) reg_keep<VALS>(k[x], v[x], ok[x], VALS ? ov[x] : 0u, lower);
     }
 #pragma unroll
     for (int j = lv >> 2; j >= 1; j >>= 1) {
@@ -825,7 +828,7 @@ __global__ void __launch_bounds__(WB_WARPS * 32) seg_sort_warpbits_kernel(const 
         for (int q = lane; q < W; q += 32) bm[q] = 0u;
       }
     }
-    if (!fits) {
+    if (!fits) {  // wider window (or duplicate ids): left to the block sort
       if (lane == 0) defer[atomicAdd(defer_count, 1u)] = r;
       __syncwarp();
       continue;
