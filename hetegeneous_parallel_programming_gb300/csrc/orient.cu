@@ -22,6 +22,12 @@ constexpr int OR_PER = ENTRY_TILE / OR_THREADS;  // 8 entries per thread per til
 #endif
 constexpr bool PLACE_SRC = TC_PLACE_SRC == 1;
 constexpr bool SORT_SRC = TC_PLACE_SRC == 2;
+// 1: the placement reads each row's destination base from rowbase_kernel's
+// per-vertex array; 0: it gathers nrowptr[rank u] and orowptr[u] itself
+#ifndef TC_PLACE_ROWBASE
+#define TC_PLACE_ROWBASE 1
+#endif
+constexpr bool PLACE_ROWBASE = TC_PLACE_ROWBASE != 0;
 
 // src[b .. b + L) = r by threads tid, tid + nt, ... (the row sorts' nsrc writes)
 __device__ __forceinline__ void put_row_src(int32_t *__restrict__ src, int64_t b, int L, int32_t r, int tid, int nt) {
@@ -262,6 +268,16 @@ __global__ void dnew_kernel(const int64_t *__restrict__ kept, const int32_t *__r
   if (blockIdx.x == 0 && threadIdx.x == 0) dnew[n] = 0;
 }
 
+// Where the placement puts row u's kept entries: relabelled slot
+// rowbase[u] + p for kept entry p (input order) of row u, rowbase[u] =
+// nrowptr[rank u] - orowptr[u].  One pass over the vertices, so that the
+// placement reads one value per row instead of gathering nrowptr[rank u].
+__global__ void rowbase_kernel(const int32_t *__restrict__ rank, const int64_t *__restrict__ nrowptr,
+                               const int64_t *__restrict__ orowptr, int64_t n, int64_t *__restrict__ rowbase) {
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x)
+    rowbase[u] = nrowptr[rank[u]] - orowptr[u];
+}
+
 // Rows of the relabelled DAG longer than a warp's registers go to list-driven
 // sorts: up to SEG_WARP_MAX entries one warp in its own shared-memory slice,
 // up to SEG_SMEM_MAX one block in shared memory, beyond that one block in
@@ -342,6 +358,10 @@ tc_status orient_phase_a(tc_ctx *ctx, const DevCSR &g, OrientBufs &b) {
   classify_rows_kernel<<<grid_for(ctx, g.n, 256, 8), 256, 0, ctx->stream>>>(b.dnew, g.n, b.mid_list, b.big_list,
                                                                             b.huge_list, b.seg_counts);
   TC_CHECK_LAUNCH(ctx);
+  if (PLACE_ROWBASE) {  // into b.kept, whose counts are spent once orowptr and dnew are made
+    rowbase_kernel<<<grid_for(ctx, g.n, 256, 8), 256, 0, ctx->stream>>>(b.rank, b.nrowptr, b.orowptr, g.n, b.kept);
+    TC_CHECK_LAUNCH(ctx);
+  }
   return TC_OK;
 }
 
@@ -360,7 +380,8 @@ __global__ void __launch_bounds__(OR_THREADS, 6) place_kernel(const int64_t *__r
                                                           int32_t *__restrict__ ncol, int32_t *__restrict__ nsrc,
                                                           uint32_t *__restrict__ perm,
                                                           int32_t *__restrict__ dag_col,
-                                                          const int32_t *__restrict__ rv_in) {
+                                                          const int32_t *__restrict__ rv_in,
+                                                          const int64_t *__restrict__ rowbase) {
   __shared__ int rows[row_slots<ENTRY_TILE>()];
   __shared__ int scan_tmp[32];
   __shared__ long long s_wbase[OR_THREADS / 32 + 1];
@@ -416,10 +437,9 @@ __global__ void __launch_bounds__(OR_THREADS, 6) place_kernel(const int64_t *__r
         const long long p = pos + __popc(bal[k] & lt);
         const int u = uu[k];
         if (RELABEL) {
-          const int32_t ru = rank[u];
-          const long long dst = nrowptr[ru] + (p - orowptr[u]);
+          const long long dst = PLACE_ROWBASE ? rowbase[u] + p : nrowptr[rank[u]] + (p - orowptr[u]);
           ncol[dst] = rv[k];
-          if (PLACE_SRC) nsrc[dst] = ru;
+          if (PLACE_SRC) nsrc[dst] = rank[u];
           if (VALS) perm[dst] = (uint32_t)p;
         }
         if (DAGCOL) dag_col[p] = vv[k];
@@ -1070,7 +1090,7 @@ tc_status orient_phase_b(tc_ctx *ctx, const DevCSR &g, OrientBufs &b, int64_t m,
 #define TC_PLACE(V, D, R)                                                                                        \
   place_kernel<V, D, R><<<b.G, OR_THREADS, 0, ctx->stream>>>(g.rowptr, g.col, g.n, g.nnz, b.chunk, b.rank, b.bcount, \
                                                              b.orowptr, b.nrowptr, b.ncol, b.nsrc, b.perm, b.dag_col, \
-                                                             b.rv)
+                                                             b.rv, b.kept)
     if (!relabel) TC_PLACE(false, true, false);
     else if (want_perm && want_dag_cols) TC_PLACE(true, true, true);
     else if (want_perm) TC_PLACE(true, false, true);
