@@ -33,6 +33,60 @@ static tc_status check_csr_args(tc_ctx *ctx, const tc_csr *g) {
   return TC_OK;
 }
 
+// Host-to-device copies of page-locked caller memory by the SMs: the
+// kernel reads the host buffer through its mapping over the C2C link.  On the
+// GB300 machines measured, the copy engines' rate fell from 211 GB/s to 100-157
+// GB/s for some copies after seconds of device load, while this kernel held
+// 211 GB/s throughout.  dst is 16-byte aligned (arena); src is whatever the
+// caller passed: a 16-byte body when both share their offset mod 16, else
+// 4-byte words (the CSR's element size), with the bytes' count a multiple of 4.
+__global__ void h2d_copy_kernel(const char *__restrict__ src, char *__restrict__ dst, size_t bytes) {
+  const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x, nt = (size_t)gridDim.x * blockDim.x;
+  const size_t head = (16 - (reinterpret_cast<uintptr_t>(dst) & 15)) & 15;
+  if (((reinterpret_cast<uintptr_t>(src) ^ reinterpret_cast<uintptr_t>(dst)) & 15) == 0 && bytes >= head) {
+    for (size_t i = tid; i < head / 4; i += nt)
+      reinterpret_cast<uint32_t *>(dst)[i] = reinterpret_cast<const uint32_t *>(src)[i];
+    const size_t n16 = (bytes - head) / 16;
+    const uint4 *s16 = reinterpret_cast<const uint4 *>(src + head);
+    uint4 *d16 = reinterpret_cast<uint4 *>(dst + head);
+    for (size_t i = tid; i < n16; i += nt) d16[i] = s16[i];
+    const size_t done = head + 16 * n16;
+    for (size_t i = tid; i < (bytes - done) / 4; i += nt)
+      reinterpret_cast<uint32_t *>(dst + done)[i] = reinterpret_cast<const uint32_t *>(src + done)[i];
+  } else {
+    for (size_t i = tid; i < bytes / 4; i += nt)
+      reinterpret_cast<uint32_t *>(dst)[i] = reinterpret_cast<const uint32_t *>(src)[i];
+  }
+}
+
+// The device address of page-locked host memory, or null (pageable memory,
+// or TC_H2D_KERNEL 0): the caller then copies with cudaMemcpyAsync.
+#ifndef TC_H2D_KERNEL
+#define TC_H2D_KERNEL 1
+#endif
+static const void *mapped_host(const void *p) {
+  if (!TC_H2D_KERNEL || !p) return nullptr;
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+static tc_status h2d_copy(tc_ctx *ctx, void *dst, const void *src, const void *src_dev, size_t bytes,
+                          cudaStream_t st) {
+  if (bytes == 0) return TC_OK;
+  if (src_dev) {
+    h2d_copy_kernel<<<ctx->num_sms * 2, 256, 0, st>>>(static_cast<const char *>(src_dev),
+                                                     static_cast<char *>(dst), bytes);
+    TC_CHECK_LAUNCH(ctx);
+  } else {
+    TC_CHECK_CUDA(ctx, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
+  }
+  return TC_OK;
+}
+
 // Device copies of a caller CSR (no copy when already on the device).
 tc_status stage_csr(tc_ctx *ctx, const tc_csr *g, Bump &bump, DevCSR &d, uint64_t *h2d, int pieces) {
   d.n = g->n;
@@ -45,8 +99,9 @@ tc_status stage_csr(tc_ctx *ctx, const tc_csr *g, Bump &bump, DevCSR &d, uint64_
   int64_t *rp = bump.take<int64_t>(g->n + 1);
   int32_t *cl = bump.take<int32_t>(g->nnz);
   if (bump.overflow) return set_error(ctx, TC_ERR_OOM, "arena overflow staging the graph");
-  TC_CHECK_CUDA(ctx, cudaMemcpyAsync(rp, g->rowptr, sizeof(int64_t) * (size_t)(g->n + 1), cudaMemcpyHostToDevice,
-                                     ctx->stream));
+  const void *rp_dev = mapped_host(g->rowptr);
+  const char *cl_dev = static_cast<const char *>(g->nnz > 0 ? mapped_host(g->colidx) : nullptr);
+  TC_TRY(h2d_copy(ctx, rp, g->rowptr, rp_dev, sizeof(int64_t) * (size_t)(g->n + 1), ctx->stream));
   if (pieces > 1) {
     // piece k = blocks [k * per, (k + 1) * per) of the kept-count geometry
     int G;
@@ -59,13 +114,12 @@ tc_status stage_csr(tc_ctx *ctx, const tc_csr *g, Bump &bump, DevCSR &d, uint64_
       const int64_t e0 = std::min<int64_t>(g->nnz, (int64_t)k * per * chunk);
       const int64_t e1 = std::min<int64_t>(g->nnz, (int64_t)(k + 1) * per * chunk);
       if (e1 > e0)
-        TC_CHECK_CUDA(ctx, cudaMemcpyAsync(cl + e0, g->colidx + e0, sizeof(int32_t) * (size_t)(e1 - e0),
-                                           cudaMemcpyHostToDevice, ctx->copy_stream));
+        TC_TRY(h2d_copy(ctx, cl + e0, g->colidx + e0, cl_dev ? cl_dev + sizeof(int32_t) * (size_t)e0 : nullptr,
+                        sizeof(int32_t) * (size_t)(e1 - e0), ctx->copy_stream));
       TC_CHECK_CUDA(ctx, cudaEventRecord(ctx->piece_ev[k], ctx->copy_stream));
     }
   } else if (g->nnz > 0) {
-    TC_CHECK_CUDA(ctx, cudaMemcpyAsync(cl, g->colidx, sizeof(int32_t) * (size_t)g->nnz, cudaMemcpyHostToDevice,
-                                       ctx->stream));
+    TC_TRY(h2d_copy(ctx, cl, g->colidx, cl_dev, sizeof(int32_t) * (size_t)g->nnz, ctx->stream));
   }
   *h2d += sizeof(int64_t) * (size_t)(g->n + 1) + sizeof(int32_t) * (size_t)g->nnz;
   d.rowptr = rp;
