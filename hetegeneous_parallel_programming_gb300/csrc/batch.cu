@@ -6,8 +6,9 @@
 // graph owns a contiguous range of ranks and therefore of relabelled edges;
 // the count kernels pull (graph, tile) items from the per-arm queues of that
 // one union graph and a segmented sum yields every graph's exact total.  The
-// orient-back-half -> count -> per-graph-sum pipeline is captured once as a
-// CUDA graph per batch shape and replayed.
+// orientation's front half (up to the host read of the oriented edge count)
+// and the back half -> count -> per-graph-sum pipeline are each captured once
+// as a CUDA graph per batch shape and replayed.
 #include <algorithm>
 #include <vector>
 
