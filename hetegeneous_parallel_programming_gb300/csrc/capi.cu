@@ -64,6 +64,9 @@ __global__ void h2d_copy_kernel(const char *__restrict__ src, char *__restrict__
 #ifndef TC_H2D_KERNEL
 #define TC_H2D_KERNEL 1
 #endif
+#ifndef TC_H2D_BLOCKS_PER_SM
+#define TC_H2D_BLOCKS_PER_SM 1  // R-MAT scale 24 e2e: 1 60.76 ms, 2 61.31, 4 62.59 (the copy shares the SMs)
+#endif
 static const void *mapped_host(const void *p) {
   if (!TC_H2D_KERNEL || !p) return nullptr;
   cudaPointerAttributes a{};
@@ -78,7 +81,7 @@ static tc_status h2d_copy(tc_ctx *ctx, void *dst, const void *src, const void *s
                           cudaStream_t st) {
   if (bytes == 0) return TC_OK;
   if (src_dev) {
-    h2d_copy_kernel<<<ctx->num_sms * 2, 256, 0, st>>>(static_cast<const char *>(src_dev),
+    h2d_copy_kernel<<<ctx->num_sms * TC_H2D_BLOCKS_PER_SM, 256, 0, st>>>(static_cast<const char *>(src_dev),
                                                      static_cast<char *>(dst), bytes);
     TC_CHECK_LAUNCH(ctx);
   } else {
